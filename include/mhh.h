@@ -1,0 +1,249 @@
+/*
+ * mhh.h -- C-ABI of the GB300 LES/DNS time step (libmhh_gb300.so).
+ *
+ * Plain C: device pointers, sizes and a cudaStream_t; no C++ or torch types.
+ * Every entry point returns 0 on success or a negative mhh_status; the text
+ * of the last error is available from mhh_last_error().  Nothing allocates
+ * device memory except mhh_ctx_create (all scratch of the pressure solver,
+ * the reductions and the surface layer lives in the context).
+ *
+ * Fields use the reference's ghost-cell layout (include/grid.h:48-138):
+ * element (i,j,k) of a 3-D field is at i + j*icells + k*ijcells, with the
+ * interior at istart..iend-1, jstart..jend-1, kstart..kend-1.  2-D boundary
+ * arrays have icells*jcells elements.  The element type is double for
+ * MHH_FP64 contexts and float for MHH_FP32 contexts (the FP32 form keeps the
+ * tridiagonal solve, the mean-mode pressure solve, the surface layer and all
+ * reductions in double).
+ *
+ * Each entry point names the reference member function it replaces (paths
+ * relative to the MicroHH source tree); see INTEGRATION.md for the bindings.
+ */
+#ifndef MHH_H
+#define MHH_H
+
+#include <stddef.h>
+#include <cuda_runtime.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum mhh_status
+{
+    MHH_OK = 0,
+    MHH_ERR_ARG = -1,         /* invalid argument (NULL pointer, bad size, bad switch) */
+    MHH_ERR_CUDA = -2,        /* a CUDA call failed */
+    MHH_ERR_UNSUPPORTED = -3, /* e.g. an FFT length with a prime factor above 7 */
+    MHH_ERR_NONFINITE = -4,   /* a reduction returned NaN or inf */
+    MHH_ERR_TIMEOUT = -5      /* a bounded device wait ran out */
+};
+
+enum mhh_precision { MHH_FP64 = 64, MHH_FP32 = 32 };
+enum mhh_advec { MHH_ADVEC_2 = 2, MHH_ADVEC_2I5 = 25 };
+enum mhh_diff { MHH_DIFF_NONE = 0, MHH_DIFF_2 = 2, MHH_DIFF_SMAG2 = 7 };
+/* include/boundary.h:42 Boundary_type */
+enum mhh_bc { MHH_BC_DIRICHLET = 0, MHH_BC_NEUMANN = 1, MHH_BC_FLUX = 2 };
+/* src/boundary_cyclic.cxx:370 Edge */
+enum mhh_edge { MHH_EDGE_EW = 1, MHH_EDGE_NS = 2, MHH_EDGE_BOTH = 3 };
+
+typedef struct mhh_ctx mhh_ctx;
+
+/* Grid description: the inputs of Grid<TF> (src/grid.cxx:47-100) plus the
+   ghost-cell counts the schemes ask for (Advec_2i5: 3,3,1; otherwise 1,1,1). */
+typedef struct
+{
+    int itot, jtot, ktot;
+    int igc, jgc, kgc;
+    double xsize, ysize, zsize;
+} mhh_grid_desc;
+
+/* Derived grid data (mirrors Grid_data, include/grid.h:48-138). */
+typedef struct
+{
+    int itot, jtot, ktot;
+    int igc, jgc, kgc;
+    int icells, jcells, kcells, ijcells;
+    int istart, iend, jstart, jend, kstart, kend;
+    long long ncells;
+    double dx, dy, zsize;
+    int precision;
+} mhh_grid;
+
+/* Physics constants the modules read from the .ini file. */
+typedef struct
+{
+    double visc, svisc;        /* [fields] visc, svisc */
+    double cs, tpr, dnmax;     /* [diff] cs, tPr, dnmax */
+    int swmason;               /* [diff] swmason */
+    double cflmax;             /* [advec] cflmax */
+    double thref0;             /* [thermo] thref0 (Boussinesq) */
+    int thermo;                /* 1: dry thermodynamics with prognostic scalar */
+    int surface;               /* 1: swboundary=surface */
+    double z0m, z0h;           /* [boundary] z0m, z0h (homogeneous roughness) */
+} mhh_physics;
+
+/* Device pointers of the prognostic state (ghost layout, ncells each). */
+typedef struct
+{
+    void *u, *v, *w, *s;           /* s: the thermodynamic scalar (th) or NULL */
+    void *ut, *vt, *wt, *st;       /* tendencies */
+    void *evisc;                   /* eddy viscosity (Smagorinsky) or NULL */
+    void *p;                       /* pressure (ghost layout) */
+} mhh_fields;
+
+/* 2-D boundary arrays (icells*jcells, device): bottom/top value, gradient and
+   flux of u, v and s (Field3d fld_bot/grad_bot/flux_bot..., include/field3d.h). */
+typedef struct
+{
+    void *u_bot, *u_top, *u_gradbot, *u_gradtop, *u_fluxbot, *u_fluxtop;
+    void *v_bot, *v_top, *v_gradbot, *v_gradtop, *v_fluxbot, *v_fluxtop;
+    void *s_bot, *s_top, *s_gradbot, *s_gradtop, *s_fluxbot, *s_fluxtop;
+} mhh_bcfields;
+
+/* ---------------------------------------------------------------------- */
+/* Context                                                                 */
+/* ---------------------------------------------------------------------- */
+
+/* Grid<TF>::init + Grid<TF>::create/calculate (src/grid.cxx:105-305) and the
+   device set-up of Pres_2 (src/pres_2.cu:221-245, FFT plans of
+   src/pres.cu:208-285): computes the 2nd-order vertical metrics from the ktot
+   full levels z, uploads them and allocates all scratch. */
+int mhh_ctx_create(const mhh_grid_desc* desc, const double* z, int precision,
+                   const mhh_physics* phys, mhh_ctx** out);
+int mhh_ctx_destroy(mhh_ctx* ctx);
+int mhh_ctx_get_grid(const mhh_ctx* ctx, mhh_grid* out);
+/* Vertical profile (z zh dz dzh dzi dzhi rhoref rhorefh) to host, kcells doubles. */
+int mhh_ctx_get_profile(const mhh_ctx* ctx, const char* name, double* out);
+const char* mhh_last_error(void);
+/* Kernels this library launched since load (for launch accounting). */
+long long mhh_launch_count(void);
+
+/* ---------------------------------------------------------------------- */
+/* Boundaries                                                              */
+/* ---------------------------------------------------------------------- */
+
+/* Boundary_cyclic<TF>::exec (src/boundary_cyclic.cxx:370-440): periodic
+   ghost cells of one 3-D field over all levels. */
+int mhh_boundary_cyclic(mhh_ctx* ctx, void* data, int edges, cudaStream_t stream);
+
+/* Boundary<TF>::set_values (src/boundary.cxx:615-700): fills the 2-D
+   value/gradient/flux arrays of one field for a homogeneous BC. */
+int mhh_boundary_set_bc(mhh_ctx* ctx, void* val, void* grad, void* flux, int bc_type,
+                        double aval, double visc, int set_flux_grad, cudaStream_t stream);
+
+/* Boundary<TF>::set_ghost_cells, 2nd order (src/boundary.cxx:700-760,
+   :933-998) for one field: bottom and top ghost level from the BC types. */
+int mhh_boundary_ghost_cells(mhh_ctx* ctx, void* a, int bot_type, const void* abot, const void* agradbot,
+                             int top_type, const void* atop, const void* agradtop, cudaStream_t stream);
+
+/* Boundary_surface<TF>::exec (src/boundary_surface.cxx:836-994), lookup-table
+   Obukhov solver with homogeneous z0m/z0h (from mhh_physics), noslip momentum
+   and a flux or Dirichlet scalar: updates the surface fluxes and gradients and
+   the MO gradients kept in the context (used by the next Diff_smag2
+   viscosity).  thermo_bc is the scalar's bottom BC type. */
+int mhh_boundary_surface_exec(mhh_ctx* ctx, const mhh_fields* f, const mhh_bcfields* bc,
+                              int thermo_bc, cudaStream_t stream);
+/* Cold-start state of the surface layer (src/boundary_surface.cxx:545-580)
+   and the z/L lookup table (include/boundary_surface_kernels.h:77-130). */
+int mhh_boundary_surface_init(mhh_ctx* ctx, int thermo_bc);
+/* Surface 2-D arrays to host (icells*jcells doubles): ustar obuk dudz dvdz dbdz. */
+int mhh_boundary_surface_get(mhh_ctx* ctx, const char* name, double* out);
+
+/* ---------------------------------------------------------------------- */
+/* Advection                                                               */
+/* ---------------------------------------------------------------------- */
+
+/* Advec_2i5<TF>::exec (src/advec_2i5.cxx:995-1063): adds the 5th-order
+   upwind advection tendencies to ut, vt, wt and st. */
+int mhh_advec_2i5_exec(mhh_ctx* ctx, const mhh_fields* f, cudaStream_t stream);
+/* Advec_2<TF>::exec (src/advec_2.cxx:280-351). */
+int mhh_advec_2_exec(mhh_ctx* ctx, const mhh_fields* f, cudaStream_t stream);
+/* Advec_2i5<TF>::get_cfl / Advec_2<TF>::get_cfl (src/advec_2i5.cxx:953-971,
+   src/advec_2.cxx:232-244): the CFL number times dt, in double; synchronises. */
+int mhh_advec_get_cfl(mhh_ctx* ctx, int scheme, const mhh_fields* f, double dt, double* cfl, cudaStream_t stream);
+/* Advec::get_time_limit (src/advec_2i5.cxx:974-992). */
+int mhh_advec_get_time_limit(mhh_ctx* ctx, int scheme, const mhh_fields* f, unsigned long long idt,
+                             double dt, unsigned long long* idt_lim, cudaStream_t stream);
+
+/* ---------------------------------------------------------------------- */
+/* Diffusion                                                               */
+/* ---------------------------------------------------------------------- */
+
+/* Diff_smag2<TF>::exec_viscosity (src/diff_smag2.cxx:473-607): strain rate,
+   N2 of the dry thermodynamics, eddy viscosity, wall mirror and cyclic fill. */
+int mhh_diff_smag2_exec_viscosity(mhh_ctx* ctx, const mhh_fields* f, const mhh_bcfields* bc, cudaStream_t stream);
+/* Diff_smag2<TF>::exec (src/diff_smag2.cxx:380-471). */
+int mhh_diff_smag2_exec(mhh_ctx* ctx, const mhh_fields* f, const mhh_bcfields* bc, cudaStream_t stream);
+/* Diff_smag2<TF>::get_dn (src/diff_smag2.cxx:336-356); synchronises. */
+int mhh_diff_smag2_get_dn(mhh_ctx* ctx, const mhh_fields* f, double dt, double* dn, cudaStream_t stream);
+/* Diff_2<TF>::exec (src/diff_2.cxx:166-192). */
+int mhh_diff_2_exec(mhh_ctx* ctx, const mhh_fields* f, cudaStream_t stream);
+/* Diff_2<TF>::get_dn (src/diff_2.cxx:133-160): constant multiplier times dt. */
+int mhh_diff_2_get_dn(mhh_ctx* ctx, double dt, double* dn);
+
+/* ---------------------------------------------------------------------- */
+/* Thermodynamics and forcing                                              */
+/* ---------------------------------------------------------------------- */
+
+/* Thermo_dry<TF>::exec, 2nd order (src/thermo_dry.cxx:610-627): buoyancy
+   tendency on w. */
+int mhh_thermo_dry_exec(mhh_ctx* ctx, const mhh_fields* f, cudaStream_t stream);
+/* Force<TF>::exec with swlspres=dpdx (src/force.cxx:626-636). */
+int mhh_force_dpdx_exec(mhh_ctx* ctx, const mhh_fields* f, double dpdx, cudaStream_t stream);
+
+/* ---------------------------------------------------------------------- */
+/* Pressure                                                                */
+/* ---------------------------------------------------------------------- */
+
+/* Pres_2<TF>::exec (src/pres_2.cxx:65-94): divergence of the predicted
+   velocity, x/y real FFTs (hand-written, no cuFFT), tridiagonal solve in z in
+   double, inverse FFTs and the pressure gradient into ut, vt, wt. */
+int mhh_pres_2_exec(mhh_ctx* ctx, const mhh_fields* f, double sub_dt, cudaStream_t stream);
+/* Pres_2<TF>::check_divergence (src/pres_2.cxx:97-105, :389-422): maximum
+   absolute divergence, in double; synchronises. */
+int mhh_pres_2_get_divergence(mhh_ctx* ctx, const mhh_fields* f, double* div, cudaStream_t stream);
+/* Halfcomplex x/y transforms of a packed itot*jtot*ktot array in place
+   (FFT<TF>::exec_forward / exec_backward, src/fft.cxx:337-452). */
+int mhh_fft_forward(mhh_ctx* ctx, void* data, cudaStream_t stream);
+int mhh_fft_backward(mhh_ctx* ctx, void* data, cudaStream_t stream);
+
+/* ---------------------------------------------------------------------- */
+/* Time integration                                                        */
+/* ---------------------------------------------------------------------- */
+
+/* Timeloop<TF>::exec with rkorder=3 (src/timeloop.cxx:250-286, :358-387) for
+   one field pair: a += cB[substep]*dt*at; at *= cA[substep+1], or at = 0
+   over all cells after the last substep. */
+int mhh_timeloop_rk3(mhh_ctx* ctx, void* a, void* at, int substep, double dt, cudaStream_t stream);
+
+/* ---------------------------------------------------------------------- */
+/* Fused substep (the GB300 path used by the C++ Model)                    */
+/* ---------------------------------------------------------------------- */
+
+/* Configuration of a whole substep. */
+typedef struct
+{
+    int advec;                 /* mhh_advec */
+    int diff;                  /* mhh_diff */
+    int swlspres;              /* 1: constant pressure gradient */
+    double dpdx;
+    int mbcbot, mbctop;        /* momentum BC types */
+    int sbcbot, sbctop;        /* scalar BC types */
+} mhh_substep_config;
+
+/* One RK3 substep in the order of src/model.cxx:356-505, split where the host
+   may pick the time step (set_time_step needs this substep's viscosity):
+   begin = periodic and wall ghost cells, Smagorinsky viscosity;
+   end   = surface layer, ghost cells, advection + diffusion + buoyancy +
+           forcing in one fused tendency kernel, pressure solve, and the
+           pressure gradient fused with the RK3 update of all fields.
+   dt is the full time step; substep is 0, 1 or 2.  Neither synchronises. */
+int mhh_substep_begin(mhh_ctx* ctx, const mhh_substep_config* cfg, const mhh_fields* f,
+                      const mhh_bcfields* bc, cudaStream_t stream);
+int mhh_substep_end(mhh_ctx* ctx, const mhh_substep_config* cfg, const mhh_fields* f,
+                    const mhh_bcfields* bc, int substep, double dt, cudaStream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,56 @@
+/*
+ * mhh_model.h -- C entry points of the host layer (libmhh_host.so): a whole
+ * LES/DNS model driven from reference-style .ini text, with host buffers in
+ * and out.  This is the call a user of the framework makes; it corresponds to
+ * Model<TF> (src/model.cxx:67-581) with the fields injected instead of read
+ * from restart files.  Fields are passed in double in the ghost-cell layout
+ * (kcells x jcells x icells) whatever the precision of the model.
+ */
+#ifndef MHH_MODEL_H
+#define MHH_MODEL_H
+
+#include "mhh.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct mhh_model mhh_model;
+
+/* Model<TF>::Model + init + load_or_save (cold start), src/model.cxx:109-300;
+   z holds the ktot full levels (the "z" of <case>_input.nc). */
+int mhh_model_create(const char* ini_text, const double* z, int ktot, int precision, mhh_model** out);
+int mhh_model_destroy(mhh_model* m);
+const char* mhh_model_last_error(void);
+
+/* Fields: u v w th ut vt wt tht p evisc. */
+int mhh_model_set_field(mhh_model* m, const char* name, const double* data);
+int mhh_model_get_field(mhh_model* m, const char* name, double* data);
+
+/* The time loop of src/model.cxx:356-505: n RK3 steps or substeps.
+   fused = 1: one fused tendency kernel and a fused pressure-gradient + RK3
+   kernel per substep; fused = 0: the module-by-module call sequence. */
+int mhh_model_run_steps(mhh_model* m, int n, int fused);
+int mhh_model_run_substeps(mhh_model* m, int n, int fused);
+
+/* Status diagnostics, src/model.cxx:819-873 (after the periodic fill). */
+int mhh_model_get_cfl(mhh_model* m, double* out);
+int mhh_model_get_dn(mhh_model* m, double* out);
+int mhh_model_get_div(mhh_model* m, double* out);
+int mhh_model_get_dt(mhh_model* m, double* out);
+int mhh_model_get_time(mhh_model* m, double* out);
+int mhh_model_get_substep(mhh_model* m, int* out);
+int mhh_model_get_grid(mhh_model* m, mhh_grid* out);
+int mhh_model_get_profile(mhh_model* m, const char* name, double* out);
+int mhh_model_get_surface(mhh_model* m, const char* name, double* out);
+
+/* Streams and device access for batched drivers. */
+int mhh_model_set_stream(mhh_model* m, cudaStream_t s);
+int mhh_model_synchronize(mhh_model* m);
+int mhh_model_get_device_fields(mhh_model* m, mhh_fields* f, mhh_bcfields* bc);
+mhh_ctx* mhh_model_get_ctx(mhh_model* m);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

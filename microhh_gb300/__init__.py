@@ -1,0 +1,258 @@
+"""GB300-native LES/DNS time step of MicroHH: Python bindings.
+
+The arithmetic lives in the sm_103a CUDA kernels of lib/libmhh_gb300.so
+(C-ABI: include/mhh.h) driven by the C++ host layer in lib/libmhh_host.so
+(include/mhh_model.h).  This module only binds them with ctypes; there is no
+Python or CPU fallback -- importing the bindings without the built libraries
+raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import cases  # noqa: F401
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIBDIR = os.path.join(PKG, "lib")
+
+FP64, FP32 = 64, 32
+ADVEC_2, ADVEC_2I5 = 2, 25
+DIFF_NONE, DIFF_2, DIFF_SMAG2 = 0, 2, 7
+
+
+class MhhError(RuntimeError):
+    pass
+
+
+class GridDesc(ctypes.Structure):
+    _fields_ = [("itot", ctypes.c_int), ("jtot", ctypes.c_int), ("ktot", ctypes.c_int),
+                ("igc", ctypes.c_int), ("jgc", ctypes.c_int), ("kgc", ctypes.c_int),
+                ("xsize", ctypes.c_double), ("ysize", ctypes.c_double), ("zsize", ctypes.c_double)]
+
+
+class Grid(ctypes.Structure):
+    _fields_ = [("itot", ctypes.c_int), ("jtot", ctypes.c_int), ("ktot", ctypes.c_int),
+                ("igc", ctypes.c_int), ("jgc", ctypes.c_int), ("kgc", ctypes.c_int),
+                ("icells", ctypes.c_int), ("jcells", ctypes.c_int), ("kcells", ctypes.c_int),
+                ("ijcells", ctypes.c_int),
+                ("istart", ctypes.c_int), ("iend", ctypes.c_int), ("jstart", ctypes.c_int),
+                ("jend", ctypes.c_int), ("kstart", ctypes.c_int), ("kend", ctypes.c_int),
+                ("ncells", ctypes.c_longlong), ("dx", ctypes.c_double), ("dy", ctypes.c_double),
+                ("zsize", ctypes.c_double), ("precision", ctypes.c_int)]
+
+
+class Physics(ctypes.Structure):
+    _fields_ = [("visc", ctypes.c_double), ("svisc", ctypes.c_double),
+                ("cs", ctypes.c_double), ("tpr", ctypes.c_double), ("dnmax", ctypes.c_double),
+                ("swmason", ctypes.c_int), ("cflmax", ctypes.c_double), ("thref0", ctypes.c_double),
+                ("thermo", ctypes.c_int), ("surface", ctypes.c_int),
+                ("z0m", ctypes.c_double), ("z0h", ctypes.c_double)]
+
+
+class Fields(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in ("u", "v", "w", "s", "ut", "vt", "wt", "st", "evisc", "p")]
+
+
+class BcFields(ctypes.Structure):
+    _fields_ = [(f"{f}_{k}", ctypes.c_void_p) for f in ("u", "v", "s")
+                for k in ("bot", "top", "gradbot", "gradtop", "fluxbot", "fluxtop")]
+
+
+class SubstepConfig(ctypes.Structure):
+    _fields_ = [("advec", ctypes.c_int), ("diff", ctypes.c_int), ("swlspres", ctypes.c_int),
+                ("dpdx", ctypes.c_double), ("mbcbot", ctypes.c_int), ("mbctop", ctypes.c_int),
+                ("sbcbot", ctypes.c_int), ("sbctop", ctypes.c_int)]
+
+
+_kern = None
+_host = None
+
+
+def _declare(lib, name, restype, argtypes):
+    f = getattr(lib, name)
+    f.restype = restype
+    f.argtypes = argtypes
+    return f
+
+
+def load():
+    """Loads both native libraries (building them first if needed)."""
+    global _kern, _host
+    if _host is not None:
+        return _kern, _host
+    kpath = os.path.join(LIBDIR, "libmhh_gb300.so")
+    hpath = os.path.join(LIBDIR, "libmhh_host.so")
+    if not (os.path.exists(kpath) and os.path.exists(hpath)):
+        from . import build
+        build.build()
+    kern = ctypes.CDLL(kpath, mode=ctypes.RTLD_GLOBAL)
+    host = ctypes.CDLL(hpath)
+    P, I, D = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+    dp = ctypes.POINTER(ctypes.c_double)
+    S = ctypes.c_void_p  # cudaStream_t
+    # C-ABI of the kernels (include/mhh.h)
+    _declare(kern, "mhh_last_error", ctypes.c_char_p, [])
+    _declare(kern, "mhh_launch_count", ctypes.c_longlong, [])
+    _declare(kern, "mhh_ctx_create", I, [ctypes.POINTER(GridDesc), dp, I, ctypes.POINTER(Physics), ctypes.POINTER(P)])
+    _declare(kern, "mhh_ctx_destroy", I, [P])
+    _declare(kern, "mhh_ctx_get_grid", I, [P, ctypes.POINTER(Grid)])
+    _declare(kern, "mhh_ctx_get_profile", I, [P, ctypes.c_char_p, dp])
+    _declare(kern, "mhh_boundary_cyclic", I, [P, P, I, S])
+    _declare(kern, "mhh_boundary_set_bc", I, [P, P, P, P, I, D, D, I, S])
+    _declare(kern, "mhh_boundary_ghost_cells", I, [P, P, I, P, P, I, P, P, S])
+    _declare(kern, "mhh_boundary_surface_exec", I, [P, ctypes.POINTER(Fields), ctypes.POINTER(BcFields), I, S])
+    _declare(kern, "mhh_boundary_surface_init", I, [P, I])
+    _declare(kern, "mhh_boundary_surface_get", I, [P, ctypes.c_char_p, dp])
+    for n in ("mhh_advec_2i5_exec", "mhh_advec_2_exec", "mhh_diff_2_exec", "mhh_thermo_dry_exec"):
+        _declare(kern, n, I, [P, ctypes.POINTER(Fields), S])
+    _declare(kern, "mhh_advec_get_cfl", I, [P, I, ctypes.POINTER(Fields), D, dp, S])
+    _declare(kern, "mhh_advec_get_time_limit", I, [P, I, ctypes.POINTER(Fields), ctypes.c_ulonglong, D,
+                                                  ctypes.POINTER(ctypes.c_ulonglong), S])
+    _declare(kern, "mhh_diff_smag2_exec_viscosity", I, [P, ctypes.POINTER(Fields), ctypes.POINTER(BcFields), S])
+    _declare(kern, "mhh_diff_smag2_exec", I, [P, ctypes.POINTER(Fields), ctypes.POINTER(BcFields), S])
+    _declare(kern, "mhh_diff_smag2_get_dn", I, [P, ctypes.POINTER(Fields), D, dp, S])
+    _declare(kern, "mhh_diff_2_get_dn", I, [P, D, dp])
+    _declare(kern, "mhh_force_dpdx_exec", I, [P, ctypes.POINTER(Fields), D, S])
+    _declare(kern, "mhh_pres_2_exec", I, [P, ctypes.POINTER(Fields), D, S])
+    _declare(kern, "mhh_pres_2_get_divergence", I, [P, ctypes.POINTER(Fields), dp, S])
+    _declare(kern, "mhh_fft_forward", I, [P, P, S])
+    _declare(kern, "mhh_fft_backward", I, [P, P, S])
+    _declare(kern, "mhh_timeloop_rk3", I, [P, P, P, I, D, S])
+    _declare(kern, "mhh_substep_begin", I, [P, ctypes.POINTER(SubstepConfig), ctypes.POINTER(Fields),
+                                           ctypes.POINTER(BcFields), S])
+    _declare(kern, "mhh_substep_end", I, [P, ctypes.POINTER(SubstepConfig), ctypes.POINTER(Fields),
+                                         ctypes.POINTER(BcFields), I, D, S])
+    # Host layer (include/mhh_model.h)
+    _declare(host, "mhh_model_last_error", ctypes.c_char_p, [])
+    _declare(host, "mhh_model_create", I, [ctypes.c_char_p, dp, I, I, ctypes.POINTER(P)])
+    _declare(host, "mhh_model_destroy", I, [P])
+    _declare(host, "mhh_model_set_field", I, [P, ctypes.c_char_p, dp])
+    _declare(host, "mhh_model_get_field", I, [P, ctypes.c_char_p, dp])
+    _declare(host, "mhh_model_run_steps", I, [P, I, I])
+    _declare(host, "mhh_model_run_substeps", I, [P, I, I])
+    for n in ("mhh_model_get_cfl", "mhh_model_get_dn", "mhh_model_get_div", "mhh_model_get_dt", "mhh_model_get_time"):
+        _declare(host, n, I, [P, dp])
+    _declare(host, "mhh_model_get_substep", I, [P, ctypes.POINTER(ctypes.c_int)])
+    _declare(host, "mhh_model_get_grid", I, [P, ctypes.POINTER(Grid)])
+    _declare(host, "mhh_model_get_profile", I, [P, ctypes.c_char_p, dp])
+    _declare(host, "mhh_model_get_surface", I, [P, ctypes.c_char_p, dp])
+    _declare(host, "mhh_model_set_stream", I, [P, S])
+    _declare(host, "mhh_model_synchronize", I, [P])
+    _declare(host, "mhh_model_get_device_fields", I, [P, ctypes.POINTER(Fields), ctypes.POINTER(BcFields)])
+    _declare(host, "mhh_model_get_ctx", P, [P])
+    _kern, _host = kern, host
+    return kern, host
+
+
+def check(rc, what="mhh"):
+    if rc != 0:
+        kern, host = load()
+        msg = host.mhh_model_last_error() or kern.mhh_last_error() or b""
+        raise MhhError(f"{what} failed ({rc}): {msg.decode(errors='replace')}")
+
+
+def launch_count():
+    kern, _ = load()
+    return int(kern.mhh_launch_count())
+
+
+def _dptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class Model:
+    """A device-resident model built from reference-style .ini text.
+
+    ``Model(case)`` takes a cases.Case; ``Model(ini=..., z=...)`` raw input.
+    """
+
+    def __init__(self, case=None, precision=FP64, ini=None, z=None):
+        kern, host = load()
+        self.host = host
+        self.kern = kern
+        if case is not None:
+            ini, z = case.to_ini(), case.z
+        self._z = np.ascontiguousarray(z, dtype=np.float64)
+        h = ctypes.c_void_p()
+        check(host.mhh_model_create(ini.encode(), _dptr(self._z), len(self._z), precision, ctypes.byref(h)),
+              "mhh_model_create")
+        self.h = h
+        self.precision = precision
+        g = Grid()
+        check(host.mhh_model_get_grid(self.h, ctypes.byref(g)))
+        self.grid = g
+        self.shape = (g.kcells, g.jcells, g.icells)
+        if case is not None:
+            for n in case.prognostic_names():
+                self.set(n, case.embed(case.fields[n]))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.host.mhh_model_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set(self, name, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64).reshape(self.shape)
+        check(self.host.mhh_model_set_field(self.h, name.encode(), _dptr(a)), f"set {name}")
+
+    def get(self, name):
+        a = np.empty(self.shape, dtype=np.float64)
+        check(self.host.mhh_model_get_field(self.h, name.encode(), _dptr(a)), f"get {name}")
+        return a
+
+    def run_steps(self, n, fused=True):
+        check(self.host.mhh_model_run_steps(self.h, n, 1 if fused else 0), "run_steps")
+
+    def run_substeps(self, n, fused=True):
+        check(self.host.mhh_model_run_substeps(self.h, n, 1 if fused else 0), "run_substeps")
+
+    def _scalar(self, fn):
+        v = ctypes.c_double()
+        check(fn(self.h, ctypes.byref(v)))
+        return v.value
+
+    def cfl(self):
+        return self._scalar(self.host.mhh_model_get_cfl)
+
+    def dn(self):
+        return self._scalar(self.host.mhh_model_get_dn)
+
+    def div(self):
+        return self._scalar(self.host.mhh_model_get_div)
+
+    def dt(self):
+        return self._scalar(self.host.mhh_model_get_dt)
+
+    def time(self):
+        return self._scalar(self.host.mhh_model_get_time)
+
+    def profile(self, name):
+        a = np.empty(self.grid.kcells, dtype=np.float64)
+        check(self.host.mhh_model_get_profile(self.h, name.encode(), _dptr(a)))
+        return a
+
+    def surface(self, name):
+        a = np.empty((self.grid.jcells, self.grid.icells), dtype=np.float64)
+        check(self.host.mhh_model_get_surface(self.h, name.encode(), _dptr(a)))
+        return a
+
+    def set_stream(self, stream_handle):
+        check(self.host.mhh_model_set_stream(self.h, ctypes.c_void_p(stream_handle)))
+
+    def synchronize(self):
+        check(self.host.mhh_model_synchronize(self.h))
+
+    def device_fields(self):
+        f, b = Fields(), BcFields()
+        check(self.host.mhh_model_get_device_fields(self.h, ctypes.byref(f), ctypes.byref(b)))
+        return f, b
+
+    def ctx(self):
+        return self.host.mhh_model_get_ctx(self.h)

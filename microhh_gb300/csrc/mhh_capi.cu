@@ -1,0 +1,790 @@
+// mhh_capi.cu -- the C-ABI of include/mhh.h: context set-up (grid metrics,
+// device profiles, all scratch) and the module entry points that the
+// reference's Advec / Diff / Pres / Timeloop / Boundary classes would call.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "mhh_kernels.cuh"
+
+namespace
+{
+    thread_local std::string g_last_error;
+    std::atomic<long long> g_launches{0};
+}
+
+void mhh_set_last_error(const char* msg) { g_last_error = msg ? msg : ""; }
+
+namespace mhh
+{
+    void count_launch(int n) { g_launches += n; }
+    long long launch_count() { return g_launches.load(); }
+
+    template<typename TF>
+    __global__ void k_pres_out(Dims d, Prof<TF> pr, const TF* __restrict__ p,
+                               TF* __restrict__ ut, TF* __restrict__ vt, TF* __restrict__ wt)
+    {
+        const int i = d.istart + blockIdx.x*blockDim.x + threadIdx.x;
+        const int j = d.jstart + blockIdx.y*blockDim.y + threadIdx.y;
+        const int k = d.kstart + blockIdx.z;
+        if (i >= d.iend || j >= d.jend) return;
+        const long long c = ijk(d, i, j, k);
+        const TF pc = ld(p, c);
+        ut[c] -= (pc - ld(p, c-1))*TF(d.dxi);
+        vt[c] -= (pc - ld(p, c-d.icells))*TF(d.dyi);
+        wt[c] -= (pc - ld(p, c-d.ijcells))*ld(pr.dzhi, k);
+    }
+}
+
+using namespace mhh;
+
+struct mhh_ctx
+{
+    mhh_grid g;
+    Dims d;
+    int prec;
+    mhh_physics phys;
+
+    // Host profiles (double), device profiles (one precision).
+    std::vector<double> h[10];
+    void* dprof[10];
+    Prof<double> pd;
+    Prof<float> pf;
+
+    PresWork pw;
+    SurfWork sw;
+    int surf_ready;
+
+    unsigned long long* red;      // device reduction word
+    unsigned long long* red_host; // pinned host copy
+    double dnmul2;                // Diff_2 multiplier
+};
+
+namespace
+{
+    enum { P_Z, P_ZH, P_DZ, P_DZH, P_DZI, P_DZHI, P_RHO, P_RHOH, P_TH, P_THH };
+    const char* prof_names[10] = {"z", "zh", "dz", "dzh", "dzi", "dzhi", "rhoref", "rhorefh", "thref", "threfh"};
+
+    int fail(int code, const char* msg) { mhh_set_last_error(msg); return code; }
+
+    template<typename TF> const Prof<TF>& prof(const mhh_ctx* c);
+    template<> const Prof<double>& prof<double>(const mhh_ctx* c) { return c->pd; }
+    template<> const Prof<float>& prof<float>(const mhh_ctx* c) { return c->pf; }
+
+    int check_cuda(const char* where)
+    {
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess)
+        {
+            std::string m = std::string(where) + ": " + cudaGetErrorString(e);
+            mhh_set_last_error(m.c_str());
+            return MHH_ERR_CUDA;
+        }
+        return MHH_OK;
+    }
+
+    // src/grid.cxx:245-305, second order.
+    void grid_metrics(mhh_ctx* c, const double* zin)
+    {
+        const Dims& d = c->d;
+        for (auto& v : c->h) v.assign(d.kcells, 0.);
+        auto& z = c->h[P_Z]; auto& zh = c->h[P_ZH]; auto& dz = c->h[P_DZ];
+        auto& dzh = c->h[P_DZH]; auto& dzi = c->h[P_DZI]; auto& dzhi = c->h[P_DZHI];
+        const int ks = d.kstart, ke = d.kend, kc = d.kcells;
+        for (int k=0; k<d.ktot; ++k) z[k + ks] = zin[k];
+        z[ks-1] = -z[ks];
+        z[ke] = 2.*d.zsize - z[ke-1];
+        for (int k=ks+1; k<ke; ++k) zh[k] = 0.5*(z[k-1] + z[k]);
+        zh[ks] = 0.;
+        zh[ke] = d.zsize;
+        for (int k=1; k<kc; ++k) { dzh[k] = z[k] - z[k-1]; dzhi[k] = 1./dzh[k]; }
+        dzh[ks-1] = dzh[ks+1]; dzhi[ks-1] = dzhi[ks+1];
+        for (int k=1; k<kc-1; ++k) { dz[k] = zh[k+1] - zh[k]; dzi[k] = 1./dz[k]; }
+        dz[ks-1] = dz[ks]; dzi[ks-1] = dzi[ks];
+        dz[ke] = dz[ke-1]; dzi[ke] = dzi[ke-1];
+        // Boussinesq base state, src/thermo_dry.cxx:547-559.
+        for (int k=0; k<kc; ++k)
+        {
+            c->h[P_RHO][k] = 1.; c->h[P_RHOH][k] = 1.;
+            c->h[P_TH][k] = c->phys.thref0; c->h[P_THH][k] = c->phys.thref0;
+        }
+    }
+
+    // Squared Smagorinsky mixing length per level: src/diff_smag2.cxx:176-180
+    // (resolved walls), :213-265 (Mason, n = 2, with buoyancy), :108-140
+    // (neutral, Mason n = 1).
+    std::vector<double> mixing_length2(const mhh_ctx* c)
+    {
+        const Dims& d = c->d;
+        const mhh_physics& p = c->phys;
+        std::vector<double> m2(d.kcells, 0.);
+        const double dx = c->d.dx, dy = c->d.dy;
+        for (int k=d.kstart; k<d.kend; ++k)
+        {
+            const double mlen0 = p.cs*std::pow(dx*dy*c->h[P_DZ][k], 1./3.);
+            double mlen = mlen0;
+            if (p.surface && p.swmason)
+            {
+                const double n = p.thermo ? 2. : 1.;
+                mlen = std::pow(1./(1./std::pow(mlen0, n) + 1./std::pow(KAPPA*(c->h[P_Z][k] + p.z0m), n)), 1./n);
+            }
+            m2[k] = mlen*mlen;
+        }
+        return m2;
+    }
+
+    template<typename TF>
+    int upload_profiles(mhh_ctx* c)
+    {
+        const int kc = c->d.kcells;
+        std::vector<TF> tmp(kc);
+        for (int q=0; q<10; ++q)
+        {
+            if (cudaMalloc(&c->dprof[q], sizeof(TF)*kc) != cudaSuccess) return fail(MHH_ERR_CUDA, "cudaMalloc profiles");
+            for (int k=0; k<kc; ++k) tmp[k] = TF(c->h[q][k]);
+            cudaMemcpy(c->dprof[q], tmp.data(), sizeof(TF)*kc, cudaMemcpyHostToDevice);
+        }
+        Prof<TF> p;
+        p.z = (const TF*)c->dprof[P_Z]; p.zh = (const TF*)c->dprof[P_ZH];
+        p.dz = (const TF*)c->dprof[P_DZ]; p.dzh = (const TF*)c->dprof[P_DZH];
+        p.dzi = (const TF*)c->dprof[P_DZI]; p.dzhi = (const TF*)c->dprof[P_DZHI];
+        p.rhoref = (const TF*)c->dprof[P_RHO]; p.rhorefh = (const TF*)c->dprof[P_RHOH];
+        p.thref = (const TF*)c->dprof[P_TH]; p.threfh = (const TF*)c->dprof[P_THH];
+        if constexpr (sizeof(TF) == 8) c->pd = *reinterpret_cast<Prof<double>*>(&p);
+        else c->pf = *reinterpret_cast<Prof<float>*>(&p);
+        return MHH_OK;
+    }
+
+    template<typename T>
+    int dalloc(T** p, size_t n, bool zero = true)
+    {
+        if (cudaMalloc((void**)p, sizeof(T)*(n ? n : 1)) != cudaSuccess) return fail(MHH_ERR_CUDA, "cudaMalloc scratch");
+        if (zero) cudaMemset(*p, 0, sizeof(T)*(n ? n : 1));
+        return MHH_OK;
+    }
+
+    int upload(double* dst, const std::vector<double>& v)
+    {
+        return cudaMemcpy(dst, v.data(), sizeof(double)*v.size(), cudaMemcpyHostToDevice) == cudaSuccess
+            ? MHH_OK : fail(MHH_ERR_CUDA, "cudaMemcpy");
+    }
+
+    // Pressure-solver constants, src/pres_2.cxx:124-153.
+    int setup_pres(mhh_ctx* c)
+    {
+        const Dims& d = c->d;
+        const long long n = (long long)d.itot*d.jtot*d.ktot;
+        int rc;
+        if ((rc = fft_plan_init(&c->pw.px, d.itot)) != MHH_OK) return fail(rc, "itot has a prime factor above 7");
+        if ((rc = fft_plan_init(&c->pw.py, d.jtot)) != MHH_OK) return fail(rc, "jtot has a prime factor above 7");
+        const size_t tfb = c->prec == MHH_FP64 ? 8 : 4;
+        if (cudaMalloc(&c->pw.pk, tfb*n) != cudaSuccess) return fail(MHH_ERR_CUDA, "cudaMalloc pressure");
+        if ((rc = dalloc(&c->pw.work, 2*(size_t)n, false))) return rc;
+        if ((rc = dalloc(&c->pw.bmati, d.itot)) || (rc = dalloc(&c->pw.bmatj, d.jtot))) return rc;
+        if ((rc = dalloc(&c->pw.a, d.ktot)) || (rc = dalloc(&c->pw.c, d.ktot))) return rc;
+        if ((rc = dalloc(&c->pw.dz2, d.ktot)) || (rc = dalloc(&c->pw.dz2rho, d.ktot))) return rc;
+
+        const double dxidxi = 1./(d.dx*d.dx), dyidyi = 1./(d.dy*d.dy);
+        const double pi = std::acos(-1.);
+        std::vector<double> bi(d.itot), bj(d.jtot), a(d.ktot), cc(d.ktot), dz2(d.ktot), dz2r(d.ktot);
+        for (int j=0; j<d.jtot/2+1; ++j) bj[j] = 2.*(std::cos(2.*pi*(double)j/(double)d.jtot) - 1.)*dyidyi;
+        for (int j=d.jtot/2+1; j<d.jtot; ++j) bj[j] = bj[d.jtot-j];
+        for (int i=0; i<d.itot/2+1; ++i) bi[i] = 2.*(std::cos(2.*pi*(double)i/(double)d.itot) - 1.)*dxidxi;
+        for (int i=d.itot/2+1; i<d.itot; ++i) bi[i] = bi[d.itot-i];
+        const auto& dz = c->h[P_DZ]; const auto& dzhi = c->h[P_DZHI];
+        const auto& rh = c->h[P_RHOH]; const auto& r = c->h[P_RHO];
+        for (int k=0; k<d.ktot; ++k)
+        {
+            const int kg = k + d.kgc;
+            a[k] = dz[kg]*rh[kg]*dzhi[kg];
+            cc[k] = dz[kg]*rh[kg+1]*dzhi[kg+1];
+            dz2[k] = dz[kg]*dz[kg];
+            dz2r[k] = dz[kg]*dz[kg]*r[kg];
+        }
+        if ((rc = upload(c->pw.bmati, bi)) || (rc = upload(c->pw.bmatj, bj))) return rc;
+        if ((rc = upload(c->pw.a, a)) || (rc = upload(c->pw.c, cc))) return rc;
+        if ((rc = upload(c->pw.dz2, dz2)) || (rc = upload(c->pw.dz2rho, dz2r))) return rc;
+        return MHH_OK;
+    }
+
+    // z/L lookup table, include/boundary_surface_kernels.h:77-130.
+    double fm_host(double zsl, double z0m, double L)
+    {
+        auto phim_u = [](double z) { return std::pow(1. + 3.6*std::pow(std::fabs(z), 2./3.), -1./2.); };
+        auto psim_u = [&](double z) { return 3.*std::log((1. + 1./phim_u(z))/2.); };
+        auto psim_s = [](double z) { const double a = 1., b = 2./3., cc = 5., dd = 0.35;
+                                     return -b*(z - (cc/dd))*std::exp(-dd*z) - a*z - (b*cc)/dd; };
+        return L <= 0. ? KAPPA/(std::log(zsl/z0m) - psim_u(zsl/L) + psim_u(z0m/L))
+                       : KAPPA/(std::log(zsl/z0m) - psim_s(zsl/L) + psim_s(z0m/L));
+    }
+    double fh_host(double zsl, double z0h, double L)
+    {
+        auto phih_u = [](double z) { return std::pow(1. + 7.9*std::pow(std::fabs(z), 2./3.), -1./2.); };
+        auto psih_u = [&](double z) { return 3.*std::log((1. + 1./phih_u(z))/2.); };
+        auto psih_s = [](double z) { const double a = 1., b = 2./3., cc = 5., dd = 0.35;
+                                     return -b*(z - (cc/dd))*std::exp(-dd*z) - std::pow(1. + b*a*z, 1.5) - (b*cc)/dd + 1.; };
+        return L <= 0. ? KAPPA/(std::log(zsl/z0h) - psih_u(zsl/L) + psih_u(z0h/L))
+                       : KAPPA/(std::log(zsl/z0h) - psih_s(zsl/L) + psih_s(z0h/L));
+    }
+
+    void prepare_lut(std::vector<float>& zL, std::vector<float>& f, double zsl, double z0m, double z0h, int thermo_bc)
+    {
+        const int N = NZL_LUT;
+        std::vector<double> zt(N);
+        const double zLrange_min = -5., zL_max = 10., zL_min = -1.e4;
+        double dzL = (zL_max - zLrange_min) / (9.*N/10. - 1.);
+        zt[0] = -zL_max;
+        for (int n=1; n<9*N/10; ++n) zt[n] = zt[n-1] + dzL;
+        const double zLend = -(zL_min - zLrange_min);
+        double r = 1.01, r0 = 1.e30;
+        while (std::fabs((r - r0)/r0) > 1.e-10)
+        {
+            r0 = r;
+            r = std::pow(1. - (zLend/dzL)*(1. - r), (1./(N/10.)));
+        }
+        for (int n=9*N/10; n<N; ++n) { zt[n] = zt[n-1] + dzL; dzL *= r; }
+        zL.resize(N); f.resize(N);
+        for (int n=0; n<N; ++n) zL[n] = (float)(-zt[N-n-1]);
+        for (int n=0; n<N; ++n)
+        {
+            const double L = zsl/(double)zL[n];
+            if (thermo_bc == MHH_BC_DIRICHLET)
+                f[n] = (float)((double)zL[n]*std::pow(fm_host(zsl, z0m, L), 2)/fh_host(zsl, z0h, L));
+            else
+                f[n] = (float)((double)zL[n]*std::pow(fm_host(zsl, z0m, L), 3));
+        }
+    }
+
+    int reduce_to_host(mhh_ctx* c, cudaStream_t s, double* out)
+    {
+        cudaMemcpyAsync(c->red_host, c->red, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) return fail(MHH_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
+        long long bits = (long long)*c->red_host;
+        double v;
+        std::memcpy(&v, &bits, sizeof(double));
+        *out = v;
+        if (!std::isfinite(v)) return fail(MHH_ERR_NONFINITE, "reduction is not finite");
+        return MHH_OK;
+    }
+
+    template<typename TF> TF* T(void* p) { return static_cast<TF*>(p); }
+    template<typename TF> const TF* CT(const void* p) { return static_cast<const TF*>(p); }
+
+    template<typename TF>
+    TendArgs<TF> tend_args(const mhh_ctx* c, const mhh_fields* f, const mhh_bcfields* bc)
+    {
+        TendArgs<TF> a{};
+        a.u = CT<TF>(f->u); a.v = CT<TF>(f->v); a.w = CT<TF>(f->w); a.s = CT<TF>(f->s);
+        a.evisc = CT<TF>(f->evisc);
+        a.ut = T<TF>(f->ut); a.vt = T<TF>(f->vt); a.wt = T<TF>(f->wt); a.st = T<TF>(f->st);
+        if (bc)
+        {
+            a.u_fluxbot = CT<TF>(bc->u_fluxbot); a.u_fluxtop = CT<TF>(bc->u_fluxtop);
+            a.v_fluxbot = CT<TF>(bc->v_fluxbot); a.v_fluxtop = CT<TF>(bc->v_fluxtop);
+            a.s_fluxbot = CT<TF>(bc->s_fluxbot); a.s_fluxtop = CT<TF>(bc->s_fluxtop);
+        }
+        a.visc = TF(c->phys.visc); a.svisc = TF(c->phys.svisc);
+        a.tpri = TF(1)/TF(c->phys.tpr);
+        a.fbody = TF(0);
+        a.dxidxi = 1./(c->d.dx*c->d.dx);
+        a.dyidyi = 1./(c->d.dy*c->d.dy);
+        return a;
+    }
+
+    // ---------------------------------------------------------------------
+    // Templated bodies
+    // ---------------------------------------------------------------------
+    template<typename TF>
+    int pres_exec(mhh_ctx* c, const mhh_fields* f, double sub_dt, bool with_out, cudaStream_t s)
+    {
+        const Dims& d = c->d;
+        const Prof<TF>& pr = prof<TF>(c);
+        FieldList<TF> fl;
+        fl.n = 1; fl.p[0] = T<TF>(f->ut); launch_cyclic(fl, d, MHH_EDGE_EW, s);
+        fl.p[0] = T<TF>(f->vt); launch_cyclic(fl, d, MHH_EDGE_NS, s);
+        TF* pk = T<TF>(c->pw.pk);
+        launch_pres_in<TF>(d, pr, CT<TF>(f->u), CT<TF>(f->v), CT<TF>(f->w), CT<TF>(f->ut), CT<TF>(f->vt), CT<TF>(f->wt),
+                           pk, 1./sub_dt, s);
+        launch_fft_x<TF>(c->pw.px, pk, d.jtot*d.ktot, false, 1., s);
+        launch_fft_y<TF>(c->pw.py, pk, d.itot, d.jtot, d.ktot, false, 1., s);
+        launch_tdma<TF>(d, c->pw, pk, s);
+        launch_fft_y<TF>(c->pw.py, pk, d.itot, d.jtot, d.ktot, true, 1./d.jtot, s);
+        launch_fft_x<TF>(c->pw.px, pk, d.jtot*d.ktot, true, 1./d.itot, s);
+        launch_pres_scatter<TF>(d, pk, T<TF>(f->p), s);
+        fl.p[0] = T<TF>(f->p); launch_cyclic(fl, d, MHH_EDGE_BOTH, s);
+        if (with_out)
+        {
+            dim3 block(32, 8), grid((d.itot + 31)/32, (d.jtot + 7)/8, d.ktot);
+            k_pres_out<TF><<<grid, block, 0, s>>>(d, pr, CT<TF>(f->p), T<TF>(f->ut), T<TF>(f->vt), T<TF>(f->wt));
+            count_launch();
+        }
+        return check_cuda("pres_2");
+    }
+
+    template<typename TF>
+    int viscosity(mhh_ctx* c, const mhh_fields* f, cudaStream_t s)
+    {
+        if (!f->evisc) return fail(MHH_ERR_ARG, "evisc is NULL");
+        const bool surf = c->phys.surface != 0, thermo = c->phys.thermo != 0 && f->s;
+        if (surf && !c->surf_ready) return fail(MHH_ERR_ARG, "surface layer not initialised");
+        launch_viscosity<TF>(c->d, prof<TF>(c), CT<TF>(f->u), CT<TF>(f->v), CT<TF>(f->w), CT<TF>(f->s), T<TF>(f->evisc),
+                             c->sw.mlen2, c->sw.dudz, c->sw.dvdz, c->sw.dbdz, c->phys.cs, c->phys.tpr, c->phys.visc,
+                             c->phys.swmason, surf, thermo, s);
+        return check_cuda("viscosity");
+    }
+
+    template<typename TF>
+    int surface_exec(mhh_ctx* c, const mhh_fields* f, const mhh_bcfields* bc, int thermo_bc, cudaStream_t s)
+    {
+        if (!c->surf_ready) return fail(MHH_ERR_ARG, "surface layer not initialised");
+        const int thermo = (c->phys.thermo && f->s) ? 1 : 0;
+        launch_surface<TF>(c->d, prof<TF>(c), c->sw, CT<TF>(f->u), CT<TF>(f->v), CT<TF>(f->s),
+                           T<TF>(bc->u_bot), T<TF>(bc->v_bot), T<TF>(bc->u_fluxbot), T<TF>(bc->v_fluxbot),
+                           T<TF>(bc->u_gradbot), T<TF>(bc->v_gradbot),
+                           T<TF>(bc->s_bot), T<TF>(bc->s_fluxbot), T<TF>(bc->s_gradbot),
+                           thermo, thermo_bc, c->phys.z0m, c->phys.z0h, s);
+        return check_cuda("surface");
+    }
+
+    template<typename TF>
+    void ghost_all(mhh_ctx* c, const mhh_substep_config* cfg, const mhh_fields* f, const mhh_bcfields* bc,
+                   bool momentum, cudaStream_t s)
+    {
+        GhostList<TF> gl{};
+        auto add = [&](void* a, int bt, void* abot, void* agb, int tt, void* atop, void* agt)
+        {
+            const int q = gl.n++;
+            gl.a[q] = T<TF>(a); gl.bot_type[q] = bt; gl.top_type[q] = tt;
+            gl.abot[q] = CT<TF>(abot); gl.agradbot[q] = CT<TF>(agb);
+            gl.atop[q] = CT<TF>(atop); gl.agradtop[q] = CT<TF>(agt);
+        };
+        if (momentum)
+        {
+            add(f->u, cfg->mbcbot, bc->u_bot, bc->u_gradbot, cfg->mbctop, bc->u_top, bc->u_gradtop);
+            add(f->v, cfg->mbcbot, bc->v_bot, bc->v_gradbot, cfg->mbctop, bc->v_top, bc->v_gradtop);
+        }
+        if (f->s)
+            add(f->s, cfg->sbcbot, bc->s_bot, bc->s_gradbot, cfg->sbctop, bc->s_top, bc->s_gradtop);
+        if (gl.n) launch_ghost<TF>(gl, c->d, prof<TF>(c).dzh, s);
+    }
+
+    template<typename TF>
+    int substep_begin(mhh_ctx* c, const mhh_substep_config* cfg, const mhh_fields* f, const mhh_bcfields* bc, cudaStream_t s)
+    {
+        FieldList<TF> fl{};
+        fl.p[fl.n++] = T<TF>(f->u); fl.p[fl.n++] = T<TF>(f->v); fl.p[fl.n++] = T<TF>(f->w);
+        if (f->s) fl.p[fl.n++] = T<TF>(f->s);
+        launch_cyclic(fl, c->d, MHH_EDGE_BOTH, s);
+        ghost_all<TF>(c, cfg, f, bc, true, s);
+        if (cfg->diff == MHH_DIFF_SMAG2)
+            return viscosity<TF>(c, f, s);
+        return check_cuda("substep_begin");
+    }
+
+    template<typename TF>
+    int substep_end(mhh_ctx* c, const mhh_substep_config* cfg, const mhh_fields* f, const mhh_bcfields* bc,
+                    int substep, double dt, cudaStream_t s)
+    {
+        const Dims& d = c->d;
+        const Prof<TF>& pr = prof<TF>(c);
+        const bool surf = c->phys.surface != 0;
+        if (surf)
+        {
+            int rc = surface_exec<TF>(c, f, bc, cfg->sbcbot, s);
+            if (rc) return rc;
+            ghost_all<TF>(c, cfg, f, bc, false, s);
+        }
+        TendArgs<TF> a = tend_args<TF>(c, f, bc);
+        const bool force = cfg->swlspres != 0;
+        a.fbody = TF(-1.*cfg->dpdx);
+        const bool scal = f->s != nullptr;
+        const bool buoy = scal && c->phys.thermo;
+        launch_tendency<TF>(d, pr, a, cfg->advec, cfg->diff, surf, scal, buoy, force, s);
+        const double cB[3] = {1./3., 15./16., 8./15.};
+        int rc = pres_exec<TF>(c, f, cB[substep]*dt, false, s);
+        if (rc) return rc;
+        launch_presout_rk3<TF>(d, pr, CT<TF>(f->p), T<TF>(f->u), T<TF>(f->v), T<TF>(f->w), T<TF>(f->s),
+                               T<TF>(f->ut), T<TF>(f->vt), T<TF>(f->wt), T<TF>(f->st), substep, dt, s);
+        return check_cuda("substep_end");
+    }
+}
+
+#define DISPATCH(c, call) ((c)->prec == MHH_FP64 ? call<double> : call<float>)
+
+extern "C" {
+
+const char* mhh_last_error(void) { return g_last_error.c_str(); }
+long long mhh_launch_count(void) { return mhh::launch_count(); }
+
+int mhh_ctx_create(const mhh_grid_desc* desc, const double* z, int precision, const mhh_physics* phys, mhh_ctx** out)
+{
+    if (!desc || !z || !phys || !out) return fail(MHH_ERR_ARG, "NULL argument");
+    if (precision != MHH_FP64 && precision != MHH_FP32) return fail(MHH_ERR_ARG, "precision must be 64 or 32");
+    if (desc->itot < 1 || desc->jtot < 1 || desc->ktot < 1 || desc->igc < 1 || desc->jgc < 1 || desc->kgc != 1)
+        return fail(MHH_ERR_ARG, "bad grid sizes or ghost cells (kgc must be 1)");
+    if (desc->igc > desc->itot || desc->jgc > desc->jtot)
+        return fail(MHH_ERR_ARG, "more ghost cells than interior cells");
+    if ((desc->igc >= 3 || desc->jgc >= 3) && desc->ktot < 6)
+        return fail(MHH_ERR_ARG, "the 5th-order scheme needs ktot >= 6");
+    const double ncells = double(desc->itot + 2*desc->igc)*(desc->jtot + 2*desc->jgc)*(desc->ktot + 2);
+    if (ncells > 4.0e9) return fail(MHH_ERR_ARG, "grid too large for 32-bit plane indexing");
+
+    mhh_ctx* c = new mhh_ctx();
+    std::memset(c->dprof, 0, sizeof(c->dprof));
+    std::memset(&c->pw, 0, sizeof(c->pw));
+    std::memset(&c->sw, 0, sizeof(c->sw));
+    c->prec = precision;
+    c->phys = *phys;
+    Dims& d = c->d;
+    d.itot = desc->itot; d.jtot = desc->jtot; d.ktot = desc->ktot;
+    d.igc = desc->igc; d.jgc = desc->jgc; d.kgc = desc->kgc;
+    d.icells = d.itot + 2*d.igc; d.jcells = d.jtot + 2*d.jgc; d.kcells = d.ktot + 2*d.kgc;
+    d.ijcells = d.icells*d.jcells;
+    d.ncells = (long long)d.ijcells*d.kcells;
+    d.istart = d.igc; d.iend = d.itot + d.igc;
+    d.jstart = d.jgc; d.jend = d.jtot + d.jgc;
+    d.kstart = d.kgc; d.kend = d.ktot + d.kgc;
+    d.dx = desc->xsize / d.itot; d.dy = desc->ysize / d.jtot;
+    d.dxi = 1./d.dx; d.dyi = 1./d.dy;
+    d.zsize = desc->zsize;
+
+    mhh_grid& g = c->g;
+    g.itot = d.itot; g.jtot = d.jtot; g.ktot = d.ktot; g.igc = d.igc; g.jgc = d.jgc; g.kgc = d.kgc;
+    g.icells = d.icells; g.jcells = d.jcells; g.kcells = d.kcells; g.ijcells = d.ijcells;
+    g.istart = d.istart; g.iend = d.iend; g.jstart = d.jstart; g.jend = d.jend; g.kstart = d.kstart; g.kend = d.kend;
+    g.ncells = d.ncells; g.dx = d.dx; g.dy = d.dy; g.zsize = d.zsize; g.precision = precision;
+
+    grid_metrics(c, z);
+    int rc = precision == MHH_FP64 ? upload_profiles<double>(c) : upload_profiles<float>(c);
+    if (!rc) rc = setup_pres(c);
+    if (!rc) rc = dalloc(&c->red, 1);
+    if (!rc && cudaMallocHost((void**)&c->red_host, sizeof(unsigned long long)) != cudaSuccess)
+        rc = fail(MHH_ERR_CUDA, "cudaMallocHost");
+    // Surface and viscosity arrays (always allocated; small).
+    if (!rc) rc = dalloc(&c->sw.ustar, d.ijcells);
+    if (!rc) rc = dalloc(&c->sw.obuk, d.ijcells);
+    if (!rc) rc = dalloc(&c->sw.dudz, d.ijcells);
+    if (!rc) rc = dalloc(&c->sw.dvdz, d.ijcells);
+    if (!rc) rc = dalloc(&c->sw.dbdz, d.ijcells);
+    if (!rc) rc = dalloc(&c->sw.dutot, d.ijcells);
+    if (!rc) rc = dalloc(&c->sw.nobuk, d.ijcells);
+    if (!rc) rc = dalloc(&c->sw.zL, NZL_LUT);
+    if (!rc) rc = dalloc(&c->sw.f, NZL_LUT);
+    if (!rc) rc = dalloc(&c->sw.mlen2, d.kcells);
+    if (!rc) rc = upload(c->sw.mlen2, mixing_length2(c));
+    c->sw.zsl = c->h[P_Z][d.kstart];
+    c->sw.thref_s = c->h[P_TH][d.kstart];
+    c->sw.threfh_s = c->h[P_THH][d.kstart];
+    // Diff_2 multiplier, src/diff_2.cxx:143-155.
+    {
+        const double viscmax = phys->thermo ? std::max(phys->visc, phys->svisc) : phys->visc;
+        double dn = 0.;
+        for (int k=d.kstart; k<d.kend; ++k)
+        {
+            const double dzk = c->h[P_DZ][k];
+            dn = std::max(dn, std::fabs(viscmax*(1./(d.dx*d.dx) + 1./(d.dy*d.dy) + 1./(dzk*dzk))));
+        }
+        c->dnmul2 = dn;
+    }
+    if (rc) { mhh_ctx_destroy(c); return rc; }
+    if (cudaDeviceSynchronize() != cudaSuccess) { mhh_ctx_destroy(c); return fail(MHH_ERR_CUDA, "set-up failed"); }
+    *out = c;
+    return MHH_OK;
+}
+
+int mhh_ctx_destroy(mhh_ctx* c)
+{
+    if (!c) return MHH_OK;
+    for (auto& p : c->dprof) if (p) cudaFree(p);
+    fft_plan_free(&c->pw.px); fft_plan_free(&c->pw.py);
+    void* ptrs[] = {c->pw.pk, c->pw.work, c->pw.bmati, c->pw.bmatj, c->pw.a, c->pw.c, c->pw.dz2, c->pw.dz2rho,
+                    c->red, c->sw.ustar, c->sw.obuk, c->sw.dudz, c->sw.dvdz, c->sw.dbdz, c->sw.dutot,
+                    c->sw.nobuk, c->sw.zL, c->sw.f, c->sw.mlen2};
+    for (void* p : ptrs) if (p) cudaFree(p);
+    if (c->red_host) cudaFreeHost(c->red_host);
+    delete c;
+    return MHH_OK;
+}
+
+int mhh_ctx_get_grid(const mhh_ctx* c, mhh_grid* out)
+{
+    if (!c || !out) return fail(MHH_ERR_ARG, "NULL argument");
+    *out = c->g;
+    return MHH_OK;
+}
+
+int mhh_ctx_get_profile(const mhh_ctx* c, const char* name, double* out)
+{
+    if (!c || !name || !out) return fail(MHH_ERR_ARG, "NULL argument");
+    for (int q=0; q<10; ++q)
+        if (!std::strcmp(name, prof_names[q]))
+        {
+            std::memcpy(out, c->h[q].data(), sizeof(double)*c->h[q].size());
+            return MHH_OK;
+        }
+    return fail(MHH_ERR_ARG, "unknown profile");
+}
+
+int mhh_boundary_cyclic(mhh_ctx* c, void* data, int edges, cudaStream_t s)
+{
+    if (!c || !data || edges < 1 || edges > 3) return fail(MHH_ERR_ARG, "bad argument");
+    if (c->prec == MHH_FP64) { FieldList<double> fl{}; fl.n = 1; fl.p[0] = (double*)data; launch_cyclic(fl, c->d, edges, s); }
+    else { FieldList<float> fl{}; fl.n = 1; fl.p[0] = (float*)data; launch_cyclic(fl, c->d, edges, s); }
+    return check_cuda("cyclic");
+}
+
+int mhh_boundary_set_bc(mhh_ctx* c, void* val, void* grad, void* flux, int type, double aval, double visc,
+                        int sfg, cudaStream_t s)
+{
+    if (!c || !val || !grad || !flux || type < 0 || type > 2) return fail(MHH_ERR_ARG, "bad argument");
+    if (c->prec == MHH_FP64) launch_set_bc<double>((double*)val, (double*)grad, (double*)flux, type, aval, visc, sfg, c->d, s);
+    else launch_set_bc<float>((float*)val, (float*)grad, (float*)flux, type, aval, visc, sfg, c->d, s);
+    return check_cuda("set_bc");
+}
+
+int mhh_boundary_ghost_cells(mhh_ctx* c, void* a, int bt, const void* abot, const void* agb,
+                             int tt, const void* atop, const void* agt, cudaStream_t s)
+{
+    if (!c || !a || !abot || !agb || !atop || !agt) return fail(MHH_ERR_ARG, "NULL argument");
+    if (c->prec == MHH_FP64)
+    {
+        GhostList<double> gl{}; gl.n = 1; gl.a[0] = (double*)a; gl.bot_type[0] = bt; gl.top_type[0] = tt;
+        gl.abot[0] = (const double*)abot; gl.agradbot[0] = (const double*)agb;
+        gl.atop[0] = (const double*)atop; gl.agradtop[0] = (const double*)agt;
+        launch_ghost<double>(gl, c->d, c->pd.dzh, s);
+    }
+    else
+    {
+        GhostList<float> gl{}; gl.n = 1; gl.a[0] = (float*)a; gl.bot_type[0] = bt; gl.top_type[0] = tt;
+        gl.abot[0] = (const float*)abot; gl.agradbot[0] = (const float*)agb;
+        gl.atop[0] = (const float*)atop; gl.agradtop[0] = (const float*)agt;
+        launch_ghost<float>(gl, c->d, c->pf.dzh, s);
+    }
+    return check_cuda("ghost_cells");
+}
+
+int mhh_boundary_surface_init(mhh_ctx* c, int thermo_bc)
+{
+    if (!c) return fail(MHH_ERR_ARG, "NULL argument");
+    if (thermo_bc != MHH_BC_FLUX && thermo_bc != MHH_BC_DIRICHLET)
+        return fail(MHH_ERR_ARG, "surface model needs a flux or Dirichlet scalar BC");
+    std::vector<float> zL, f;
+    prepare_lut(zL, f, c->sw.zsl, c->phys.z0m, c->phys.z0h, thermo_bc);
+    cudaMemcpy(c->sw.zL, zL.data(), sizeof(float)*zL.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(c->sw.f, f.data(), sizeof(float)*f.size(), cudaMemcpyHostToDevice);
+    const int n = c->d.ijcells;
+    std::vector<double> obuk(n, DSMALL), ustar(n, 1e-2);
+    cudaMemcpy(c->sw.obuk, obuk.data(), sizeof(double)*n, cudaMemcpyHostToDevice);
+    cudaMemcpy(c->sw.ustar, ustar.data(), sizeof(double)*n, cudaMemcpyHostToDevice);
+    cudaMemset(c->sw.nobuk, 0, sizeof(int)*n);
+    cudaMemset(c->sw.dudz, 0, sizeof(double)*n);
+    cudaMemset(c->sw.dvdz, 0, sizeof(double)*n);
+    cudaMemset(c->sw.dbdz, 0, sizeof(double)*n);
+    c->surf_ready = 1;
+    return check_cuda("surface_init");
+}
+
+int mhh_boundary_surface_exec(mhh_ctx* c, const mhh_fields* f, const mhh_bcfields* bc, int thermo_bc, cudaStream_t s)
+{
+    if (!c || !f || !bc) return fail(MHH_ERR_ARG, "NULL argument");
+    return c->prec == MHH_FP64 ? surface_exec<double>(c, f, bc, thermo_bc, s) : surface_exec<float>(c, f, bc, thermo_bc, s);
+}
+
+int mhh_boundary_surface_get(mhh_ctx* c, const char* name, double* out)
+{
+    if (!c || !name || !out) return fail(MHH_ERR_ARG, "NULL argument");
+    const double* src = nullptr;
+    if (!std::strcmp(name, "ustar")) src = c->sw.ustar;
+    else if (!std::strcmp(name, "obuk")) src = c->sw.obuk;
+    else if (!std::strcmp(name, "dudz")) src = c->sw.dudz;
+    else if (!std::strcmp(name, "dvdz")) src = c->sw.dvdz;
+    else if (!std::strcmp(name, "dbdz")) src = c->sw.dbdz;
+    if (!src) return fail(MHH_ERR_ARG, "unknown surface array");
+    if (cudaMemcpy(out, src, sizeof(double)*c->d.ijcells, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return fail(MHH_ERR_CUDA, "cudaMemcpy");
+    return MHH_OK;
+}
+
+static int tend_only(mhh_ctx* c, const mhh_fields* f, const mhh_bcfields* bc, int adv, int dif, bool buoy, bool force,
+                     double fbody, cudaStream_t s)
+{
+    if (!c || !f || !f->u || !f->v || !f->w || !f->ut || !f->vt || !f->wt) return fail(MHH_ERR_ARG, "NULL field");
+    const bool scal = f->s && f->st;
+    const bool surf = dif == MHH_DIFF_SMAG2 && c->phys.surface;
+    if (adv == MHH_ADVEC_2I5 && (c->d.igc < 3 || c->d.jgc < 3)) return fail(MHH_ERR_ARG, "Advec_2i5 needs 3 ghost cells");
+    if (surf && !bc) return fail(MHH_ERR_ARG, "surface diffusion needs the boundary arrays");
+    if (dif == MHH_DIFF_SMAG2 && !f->evisc) return fail(MHH_ERR_ARG, "evisc is NULL");
+    if (buoy && !f->s) return fail(MHH_ERR_ARG, "buoyancy needs the scalar");
+    if (c->prec == MHH_FP64)
+    {
+        TendArgs<double> a = tend_args<double>(c, f, bc); a.fbody = fbody;
+        launch_tendency<double>(c->d, c->pd, a, adv, dif, surf, scal && !buoy, buoy, force, s);
+    }
+    else
+    {
+        TendArgs<float> a = tend_args<float>(c, f, bc); a.fbody = float(fbody);
+        launch_tendency<float>(c->d, c->pf, a, adv, dif, surf, scal && !buoy, buoy, force, s);
+    }
+    return check_cuda("tendency");
+}
+
+int mhh_advec_2i5_exec(mhh_ctx* c, const mhh_fields* f, cudaStream_t s)
+{ return tend_only(c, f, nullptr, MHH_ADVEC_2I5, 0, false, false, 0., s); }
+
+int mhh_advec_2_exec(mhh_ctx* c, const mhh_fields* f, cudaStream_t s)
+{ return tend_only(c, f, nullptr, MHH_ADVEC_2, 0, false, false, 0., s); }
+
+int mhh_diff_smag2_exec(mhh_ctx* c, const mhh_fields* f, const mhh_bcfields* bc, cudaStream_t s)
+{ return tend_only(c, f, bc, 0, MHH_DIFF_SMAG2, false, false, 0., s); }
+
+int mhh_diff_2_exec(mhh_ctx* c, const mhh_fields* f, cudaStream_t s)
+{ return tend_only(c, f, nullptr, 0, MHH_DIFF_2, false, false, 0., s); }
+
+int mhh_thermo_dry_exec(mhh_ctx* c, const mhh_fields* f, cudaStream_t s)
+{
+    if (!c || !f || !f->s) return fail(MHH_ERR_ARG, "buoyancy needs the scalar");
+    mhh_fields g = *f; g.st = nullptr;   // only wt changes
+    return tend_only(c, &g, nullptr, 0, 0, true, false, 0., s);
+}
+
+int mhh_force_dpdx_exec(mhh_ctx* c, const mhh_fields* f, double dpdx, cudaStream_t s)
+{
+    if (!c || !f) return fail(MHH_ERR_ARG, "NULL argument");
+    mhh_fields g = *f; g.s = nullptr; g.st = nullptr;
+    return tend_only(c, &g, nullptr, 0, 0, false, true, -1.*dpdx, s);
+}
+
+int mhh_diff_smag2_exec_viscosity(mhh_ctx* c, const mhh_fields* f, const mhh_bcfields* bc, cudaStream_t s)
+{
+    (void)bc;
+    if (!c || !f) return fail(MHH_ERR_ARG, "NULL argument");
+    return c->prec == MHH_FP64 ? viscosity<double>(c, f, s) : viscosity<float>(c, f, s);
+}
+
+static int reduce(mhh_ctx* c, int what, const mhh_fields* f, double* out, cudaStream_t s)
+{
+    cudaMemsetAsync(c->red, 0, sizeof(unsigned long long), s);
+    const double tprfi = 1./std::min(1., c->phys.tpr);
+    if (c->prec == MHH_FP64)
+        launch_reduce<double>(what, c->d, c->pd, (const double*)f->u, (const double*)f->v, (const double*)f->w,
+                              (const double*)f->evisc, tprfi, c->red, s);
+    else
+        launch_reduce<float>(what, c->d, c->pf, (const float*)f->u, (const float*)f->v, (const float*)f->w,
+                             (const float*)f->evisc, tprfi, c->red, s);
+    int rc = check_cuda("reduce");
+    if (rc) return rc;
+    return reduce_to_host(c, s, out);
+}
+
+int mhh_advec_get_cfl(mhh_ctx* c, int scheme, const mhh_fields* f, double dt, double* cfl, cudaStream_t s)
+{
+    if (!c || !f || !cfl) return fail(MHH_ERR_ARG, "NULL argument");
+    if (scheme == MHH_ADVEC_2I5 && (c->d.igc < 3 || c->d.jgc < 3)) return fail(MHH_ERR_ARG, "Advec_2i5 needs 3 ghost cells");
+    double v;
+    int rc = reduce(c, scheme == MHH_ADVEC_2I5 ? 0 : 1, f, &v, s);
+    *cfl = v*dt;
+    return rc;
+}
+
+int mhh_advec_get_time_limit(mhh_ctx* c, int scheme, const mhh_fields* f, unsigned long long idt, double dt,
+                             unsigned long long* lim, cudaStream_t s)
+{
+    double cfl;
+    int rc = mhh_advec_get_cfl(c, scheme, f, dt, &cfl, s);
+    if (rc) return rc;
+    cfl = std::max(1.e-5, cfl);
+    *lim = (unsigned long long)((double)idt*c->phys.cflmax/cfl);
+    return MHH_OK;
+}
+
+int mhh_diff_smag2_get_dn(mhh_ctx* c, const mhh_fields* f, double dt, double* dn, cudaStream_t s)
+{
+    if (!c || !f || !dn || !f->evisc) return fail(MHH_ERR_ARG, "NULL argument");
+    double v;
+    int rc = reduce(c, 2, f, &v, s);
+    *dn = v*dt;
+    return rc;
+}
+
+int mhh_diff_2_get_dn(mhh_ctx* c, double dt, double* dn)
+{
+    if (!c || !dn) return fail(MHH_ERR_ARG, "NULL argument");
+    *dn = c->dnmul2*dt;
+    return MHH_OK;
+}
+
+int mhh_pres_2_exec(mhh_ctx* c, const mhh_fields* f, double sub_dt, cudaStream_t s)
+{
+    if (!c || !f || !f->p) return fail(MHH_ERR_ARG, "NULL argument");
+    return c->prec == MHH_FP64 ? pres_exec<double>(c, f, sub_dt, true, s) : pres_exec<float>(c, f, sub_dt, true, s);
+}
+
+int mhh_pres_2_get_divergence(mhh_ctx* c, const mhh_fields* f, double* div, cudaStream_t s)
+{
+    if (!c || !f || !div) return fail(MHH_ERR_ARG, "NULL argument");
+    return reduce(c, 3, f, div, s);
+}
+
+int mhh_fft_forward(mhh_ctx* c, void* data, cudaStream_t s)
+{
+    if (!c || !data) return fail(MHH_ERR_ARG, "NULL argument");
+    const Dims& d = c->d;
+    if (c->prec == MHH_FP64)
+    {
+        launch_fft_x<double>(c->pw.px, (double*)data, d.jtot*d.ktot, false, 1., s);
+        launch_fft_y<double>(c->pw.py, (double*)data, d.itot, d.jtot, d.ktot, false, 1., s);
+    }
+    else
+    {
+        launch_fft_x<float>(c->pw.px, (float*)data, d.jtot*d.ktot, false, 1., s);
+        launch_fft_y<float>(c->pw.py, (float*)data, d.itot, d.jtot, d.ktot, false, 1., s);
+    }
+    return check_cuda("fft_forward");
+}
+
+int mhh_fft_backward(mhh_ctx* c, void* data, cudaStream_t s)
+{
+    if (!c || !data) return fail(MHH_ERR_ARG, "NULL argument");
+    const Dims& d = c->d;
+    if (c->prec == MHH_FP64)
+    {
+        launch_fft_y<double>(c->pw.py, (double*)data, d.itot, d.jtot, d.ktot, true, 1., s);
+        launch_fft_x<double>(c->pw.px, (double*)data, d.jtot*d.ktot, true, 1., s);
+    }
+    else
+    {
+        launch_fft_y<float>(c->pw.py, (float*)data, d.itot, d.jtot, d.ktot, true, 1., s);
+        launch_fft_x<float>(c->pw.px, (float*)data, d.jtot*d.ktot, true, 1., s);
+    }
+    return check_cuda("fft_backward");
+}
+
+int mhh_timeloop_rk3(mhh_ctx* c, void* a, void* at, int substep, double dt, cudaStream_t s)
+{
+    if (!c || !a || !at || substep < 0 || substep > 2) return fail(MHH_ERR_ARG, "bad argument");
+    if (c->prec == MHH_FP64) launch_rk3<double>((double*)a, (double*)at, c->d, substep, dt, s);
+    else launch_rk3<float>((float*)a, (float*)at, c->d, substep, dt, s);
+    return check_cuda("rk3");
+}
+
+int mhh_substep_begin(mhh_ctx* c, const mhh_substep_config* cfg, const mhh_fields* f, const mhh_bcfields* bc,
+                      cudaStream_t s)
+{
+    if (!c || !cfg || !f || !bc) return fail(MHH_ERR_ARG, "NULL argument");
+    return c->prec == MHH_FP64 ? substep_begin<double>(c, cfg, f, bc, s) : substep_begin<float>(c, cfg, f, bc, s);
+}
+
+int mhh_substep_end(mhh_ctx* c, const mhh_substep_config* cfg, const mhh_fields* f, const mhh_bcfields* bc,
+                    int substep, double dt, cudaStream_t s)
+{
+    if (!c || !cfg || !f || !bc || !f->p || substep < 0 || substep > 2) return fail(MHH_ERR_ARG, "bad argument");
+    if (cfg->advec == MHH_ADVEC_2I5 && (c->d.igc < 3 || c->d.jgc < 3)) return fail(MHH_ERR_ARG, "Advec_2i5 needs 3 ghost cells");
+    if (cfg->diff == MHH_DIFF_SMAG2 && !f->evisc) return fail(MHH_ERR_ARG, "evisc is NULL");
+    return c->prec == MHH_FP64 ? substep_end<double>(c, cfg, f, bc, substep, dt, s)
+                               : substep_end<float>(c, cfg, f, bc, substep, dt, s);
+}
+
+}

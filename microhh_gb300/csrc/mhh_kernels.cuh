@@ -1,0 +1,109 @@
+// mhh_kernels.cuh -- launchers of the device kernels (host-side declarations).
+#pragma once
+
+#include "mhh_common.cuh"
+
+namespace mhh
+{
+    void count_launch(int n = 1);
+    long long launch_count();
+
+    template<typename TF>
+    struct FieldList
+    {
+        int n;
+        TF* p[8];
+    };
+
+    template<typename TF>
+    struct GhostList
+    {
+        int n;
+        TF* a[4];
+        int bot_type[4], top_type[4];
+        const TF* abot[4];
+        const TF* agradbot[4];
+        const TF* atop[4];
+        const TF* agradtop[4];
+    };
+
+    template<typename TF>
+    struct TendArgs
+    {
+        const TF *u, *v, *w, *s, *evisc;
+        TF *ut, *vt, *wt, *st;
+        const TF *u_fluxbot, *u_fluxtop, *v_fluxbot, *v_fluxtop, *s_fluxbot, *s_fluxtop;
+        TF visc, svisc, tpri, fbody;
+        double dxidxi, dyidyi;
+    };
+
+    template<typename TF> void launch_cyclic(const FieldList<TF>& fl, const Dims& d, int edges, cudaStream_t s);
+    template<typename TF> void launch_cyclic2d(TF* a, const Dims& d, cudaStream_t s);
+    template<typename TF> void launch_set_bc(TF* val, TF* grad, TF* flux, int type, double aval, double visc,
+                                             int sfg, const Dims& d, cudaStream_t s);
+    template<typename TF> void launch_ghost(const GhostList<TF>& gl, const Dims& d, const TF* dzh, cudaStream_t s);
+    template<typename TF> void launch_viscosity(const Dims& d, const Prof<TF>& pr, const TF* u, const TF* v, const TF* w,
+                                                const TF* th, TF* evisc, const double* mlen2, const double* dudz,
+                                                const double* dvdz, const double* dbdz, double cs, double tpr,
+                                                double visc, int mason, bool surf, bool thermo, cudaStream_t s);
+    template<typename TF> void launch_tendency(const Dims& d, const Prof<TF>& pr, const TendArgs<TF>& a, int adv, int dif,
+                                               bool surf, bool scal, bool buoy, bool force, cudaStream_t s);
+    template<typename TF> void launch_rk3(TF* a, TF* at, const Dims& d, int substep, double dt, cudaStream_t s);
+    template<typename TF> void launch_presout_rk3(const Dims& d, const Prof<TF>& pr, const TF* p, TF* u, TF* v, TF* w,
+                                                  TF* s, TF* ut, TF* vt, TF* wt, TF* st, int substep, double dt,
+                                                  cudaStream_t strm);
+    template<typename TF> void launch_reduce(int what, const Dims& d, const Prof<TF>& pr, const TF* u, const TF* v,
+                                             const TF* w, const TF* ev, double tprfi, unsigned long long* out,
+                                             cudaStream_t s);
+
+    // ---- pressure solver (mhh_pres.cu) ----
+    struct FftPlan
+    {
+        int n;
+        int nfac;
+        int fac[16];
+        double* tw_d;     // exp(-2 pi i k/n), k < n, as (re, im) pairs (double)
+        float* tw_f;      // the same in float
+    };
+
+    int fft_plan_init(FftPlan* pl, int n);
+    void fft_plan_free(FftPlan* pl);
+
+    struct PresWork
+    {
+        FftPlan px, py;
+        void* pk;             // packed itot*jtot*ktot field (TF)
+        double* bmati;        // itot
+        double* bmatj;        // jtot
+        double* a;            // ktot
+        double* c;            // ktot
+        double* dz2;          // ktot: dz^2
+        double* dz2rho;       // ktot: dz^2 * rhoref
+        double* work;         // itot*jtot*ktot doubles: Thomas coefficients
+    };
+
+    template<typename TF> void launch_pres_in(const Dims& d, const Prof<TF>& pr, const TF* u, const TF* v, const TF* w,
+                                              const TF* ut, const TF* vt, const TF* wt, TF* pk, double dti, cudaStream_t s);
+    template<typename TF> void launch_fft_x(const FftPlan& pl, TF* data, int nrows, bool inverse, double scale, cudaStream_t s);
+    template<typename TF> void launch_fft_y(const FftPlan& pl, TF* data, int itot, int jtot, int ktot, bool inverse,
+                                            double scale, cudaStream_t s);
+    template<typename TF> void launch_tdma(const Dims& d, const PresWork& pw, TF* pk, cudaStream_t s);
+    template<typename TF> void launch_pres_scatter(const Dims& d, const TF* pk, TF* p, cudaStream_t s);
+
+    // ---- surface layer (mhh_surface.cu) ----
+    struct SurfWork
+    {
+        double *ustar, *obuk, *dudz, *dvdz, *dbdz, *dutot;
+        int* nobuk;
+        float *zL, *f;
+        double *mlen2;   // kcells: squared Smagorinsky mixing length per level
+        double zsl;      // height of the first full level
+        double thref_s, threfh_s;  // reference potential temperature at kstart (full, half)
+    };
+
+    template<typename TF> void launch_surface(const Dims& d, const Prof<TF>& pr, const SurfWork& sw,
+                                              const TF* u, const TF* v, const TF* s,
+                                              TF* u_bot, TF* v_bot, TF* u_flux, TF* v_flux, TF* u_grad, TF* v_grad,
+                                              TF* s_bot, TF* s_flux, TF* s_grad,
+                                              int thermo, int thermo_bc, double z0m, double z0h, cudaStream_t st);
+}

@@ -1,0 +1,571 @@
+// mhh_stencil.cu -- grid-point kernels of the LES/DNS time step: periodic and
+// wall ghost cells, Smagorinsky viscosity, the fused tendency kernel
+// (advection + diffusion + buoyancy + forcing), the pressure-gradient + RK3
+// update and the CFL / diffusion-number / divergence reductions.
+#include "mhh_kernels.cuh"
+#include "mhh_stencil.cuh"
+
+namespace mhh
+{
+    // ---------------------------------------------------------------------
+    // Periodic ghost cells, src/boundary_cyclic.cxx:370-440.  A ghost cell
+    // (i,j) takes the interior value at the periodic image of (i,j); this
+    // equals the reference's east-west-then-north-south copy, corners
+    // included, and reads interior cells only.
+    // ---------------------------------------------------------------------
+    template<typename TF>
+    __global__ void k_cyclic(FieldList<TF> fl, Dims d, int edges)
+    {
+        const int nghost_i = 2*d.igc, nghost_j = 2*d.jgc;
+        // Work items: the ghost columns (all j) and the ghost rows: interior i
+        // when the columns are filled too, every i for a north-south-only fill
+        // (src/boundary_cyclic.cxx:404-422 copies whole rows).
+        const int rowlen = (edges & 1) ? d.itot : d.icells;
+        const int row0 = (edges & 1) ? d.istart : 0;
+        const long long ncol = (long long)nghost_i*d.jcells;
+        const long long nrow = (long long)nghost_j*rowlen;
+        const long long nitem = ((edges & 1) ? ncol : 0) + ((edges & 2) ? nrow : 0);
+        const int k = blockIdx.y;
+        for (long long n = blockIdx.x*(long long)blockDim.x + threadIdx.x; n < nitem; n += (long long)gridDim.x*blockDim.x)
+        {
+            int i, j;
+            long long m = n;
+            if ((edges & 1) && m < ncol)
+            {
+                j = (int)(m / nghost_i);
+                const int g = (int)(m % nghost_i);
+                i = g < d.igc ? g : d.iend + (g - d.igc);
+            }
+            else
+            {
+                if (edges & 1) m -= ncol;
+                const int g = (int)(m / rowlen);
+                i = row0 + (int)(m % rowlen);
+                j = g < d.jgc ? g : d.jend + (g - d.jgc);
+            }
+            int si = i, sj = j;
+            if (edges & 1)
+            {
+                if (i < d.istart) si = i + d.itot;
+                else if (i >= d.iend) si = i - d.itot;
+            }
+            if (edges & 2)
+            {
+                if (j < d.jstart) sj = j + d.jtot;
+                else if (j >= d.jend) sj = j - d.jtot;
+            }
+            const long long dst = ijk(d, i, j, k), src = ijk(d, si, sj, k);
+            for (int f=0; f<fl.n; ++f)
+                fl.p[f][dst] = fl.p[f][src];
+        }
+    }
+
+    template<typename TF>
+    void launch_cyclic(const FieldList<TF>& fl, const Dims& d, int edges, cudaStream_t s)
+    {
+        const long long nitem = 2LL*d.igc*d.jcells + 2LL*d.jgc*d.icells;
+        const int threads = 128;
+        int bx = (int)((nitem + threads - 1) / threads);
+        if (bx > 64) bx = 64;
+        dim3 grid(bx, d.kcells);
+        k_cyclic<TF><<<grid, threads, 0, s>>>(fl, d, edges);
+        count_launch();
+    }
+
+    // Periodic fill of a 2-D array (icells*jcells).
+    template<typename TF>
+    __global__ void k_cyclic2d(TF* a, Dims d)
+    {
+        const int n = blockIdx.x*blockDim.x + threadIdx.x;
+        if (n >= d.ijcells) return;
+        const int i = n % d.icells, j = n / d.icells;
+        if (i >= d.istart && i < d.iend && j >= d.jstart && j < d.jend) return;
+        int si = i, sj = j;
+        if (i < d.istart) si += d.itot; else if (i >= d.iend) si -= d.itot;
+        if (j < d.jstart) sj += d.jtot; else if (j >= d.jend) sj -= d.jtot;
+        a[n] = a[si + sj*d.icells];
+    }
+
+    template<typename TF>
+    void launch_cyclic2d(TF* a, const Dims& d, cudaStream_t s)
+    {
+        k_cyclic2d<TF><<<(d.ijcells + 255)/256, 256, 0, s>>>(a, d);
+        count_launch();
+    }
+
+    // ---------------------------------------------------------------------
+    // Homogeneous boundary values, src/boundary.cxx:50-100.
+    // ---------------------------------------------------------------------
+    template<typename TF>
+    __global__ void k_set_bc(TF* val, TF* grad, TF* flux, int type, TF aval, TF visc, int set_flux_grad, int n)
+    {
+        const int q = blockIdx.x*blockDim.x + threadIdx.x;
+        if (q >= n) return;
+        if (type == MHH_BC_DIRICHLET) val[q] = aval;
+        else if (type == MHH_BC_NEUMANN) { grad[q] = aval; if (set_flux_grad) flux[q] = -aval*visc; }
+        else if (type == MHH_BC_FLUX) { flux[q] = aval; if (set_flux_grad) grad[q] = -aval/visc; }
+    }
+
+    template<typename TF>
+    void launch_set_bc(TF* val, TF* grad, TF* flux, int type, double aval, double visc, int sfg, const Dims& d, cudaStream_t s)
+    {
+        k_set_bc<TF><<<(d.ijcells + 255)/256, 256, 0, s>>>(val, grad, flux, type, TF(aval), TF(visc), sfg, d.ijcells);
+        count_launch();
+    }
+
+    // ---------------------------------------------------------------------
+    // Wall ghost levels, 2nd order, src/boundary.cxx:700-760.
+    // ---------------------------------------------------------------------
+    template<typename TF>
+    __global__ void k_ghost(GhostList<TF> gl, Dims d, const TF* dzh)
+    {
+        const int n = blockIdx.x*blockDim.x + threadIdx.x;
+        if (n >= d.ijcells) return;
+        const TF dzhb = dzh[d.kstart], dzht = dzh[d.kend];
+        for (int f=0; f<gl.n; ++f)
+        {
+            TF* a = gl.a[f];
+            const long long cb = n + (long long)d.kstart*d.ijcells;
+            const long long ct = n + (long long)(d.kend-1)*d.ijcells;
+            if (gl.bot_type[f] == MHH_BC_DIRICHLET)
+                a[cb - d.ijcells] = TF(2)*gl.abot[f][n] - a[cb];
+            else
+                a[cb - d.ijcells] = -gl.agradbot[f][n]*dzhb + a[cb];
+            if (gl.top_type[f] == MHH_BC_DIRICHLET)
+                a[ct + d.ijcells] = TF(2)*gl.atop[f][n] - a[ct];
+            else
+                a[ct + d.ijcells] = gl.agradtop[f][n]*dzht + a[ct];
+        }
+    }
+
+    template<typename TF>
+    void launch_ghost(const GhostList<TF>& gl, const Dims& d, const TF* dzh, cudaStream_t s)
+    {
+        k_ghost<TF><<<(d.ijcells + 255)/256, 256, 0, s>>>(gl, d, dzh);
+        count_launch();
+    }
+
+    // ---------------------------------------------------------------------
+    // Smagorinsky viscosity: strain rate (include/diff_kernels.h:34-142),
+    // N2 of the dry thermodynamics (src/thermo_dry.cxx:64-75) and the eddy
+    // viscosity (src/diff_smag2.cxx:47-269) in one pass; evisc holds the
+    // result at interior cells.
+    // ---------------------------------------------------------------------
+    template<typename TF, bool SURF, bool THERMO>
+    __global__ void __launch_bounds__(256)
+    k_viscosity(Dims d, Prof<TF> pr, const TF* __restrict__ u, const TF* __restrict__ v, const TF* __restrict__ w,
+                const TF* __restrict__ th, TF* __restrict__ evisc, const double* __restrict__ mlen2,
+                const double* __restrict__ dudz, const double* __restrict__ dvdz, const double* __restrict__ dbdz,
+                TF cs, TF tpr, TF visc, int mason)
+    {
+        const int i = d.istart + blockIdx.x*blockDim.x + threadIdx.x;
+        const int j = d.jstart + blockIdx.y*blockDim.y + threadIdx.y;
+        const int k = d.kstart + blockIdx.z;
+        if (i >= d.iend || j >= d.jend) return;
+        const long long ii = 1, jj = d.icells, kk = d.ijcells;
+        const long long c = ijk(d, i, j, k);
+        const long long ij = i + (long long)j*jj;
+        const TF dxi = TF(d.dxi), dyi = TF(d.dyi);
+
+        TF acc = sq((ld(u, c+ii)-ld(u, c))*dxi)
+               + sq((ld(v, c+jj)-ld(v, c))*dyi)
+               + sq((ld(w, c+kk)-ld(w, c))*ld(pr.dzi, k))
+               + TF(0.125)*sq((ld(u, c      )-ld(u, c   -jj))*dyi + (ld(v, c      )-ld(v, c-ii   ))*dxi)
+               + TF(0.125)*sq((ld(u, c+ii   )-ld(u, c+ii-jj))*dyi + (ld(v, c+ii   )-ld(v, c      ))*dxi)
+               + TF(0.125)*sq((ld(u, c   +jj)-ld(u, c      ))*dyi + (ld(v, c   +jj)-ld(v, c-ii+jj))*dxi)
+               + TF(0.125)*sq((ld(u, c+ii+jj)-ld(u, c+ii   ))*dyi + (ld(v, c+ii+jj)-ld(v, c   +jj))*dxi);
+        if (SURF && k == d.kstart)
+        {
+            acc += TF(0.5)*sq(TF(dudz[ij]))
+                 + TF(0.125)*sq((ld(w, c      )-ld(w, c-ii   ))*dxi)
+                 + TF(0.125)*sq((ld(w, c+ii   )-ld(w, c      ))*dxi)
+                 + TF(0.125)*sq((ld(w, c   +kk)-ld(w, c-ii+kk))*dxi)
+                 + TF(0.125)*sq((ld(w, c+ii+kk)-ld(w, c   +kk))*dxi)
+                 + TF(0.5)*sq(TF(dvdz[ij]))
+                 + TF(0.125)*sq((ld(w, c      )-ld(w, c-jj   ))*dyi)
+                 + TF(0.125)*sq((ld(w, c+jj   )-ld(w, c      ))*dyi)
+                 + TF(0.125)*sq((ld(w, c   +kk)-ld(w, c-jj+kk))*dyi)
+                 + TF(0.125)*sq((ld(w, c+jj+kk)-ld(w, c   +kk))*dyi);
+        }
+        else
+        {
+            const TF dzb = ld(pr.dzhi, k), dzt = ld(pr.dzhi, k+1);
+            acc += TF(0.125)*sq((ld(u, c      )-ld(u, c   -kk))*dzb + (ld(w, c      )-ld(w, c-ii   ))*dxi)
+                 + TF(0.125)*sq((ld(u, c+ii   )-ld(u, c+ii-kk))*dzb + (ld(w, c+ii   )-ld(w, c      ))*dxi)
+                 + TF(0.125)*sq((ld(u, c   +kk)-ld(u, c      ))*dzt + (ld(w, c   +kk)-ld(w, c-ii+kk))*dxi)
+                 + TF(0.125)*sq((ld(u, c+ii+kk)-ld(u, c+ii   ))*dzt + (ld(w, c+ii+kk)-ld(w, c   +kk))*dxi)
+                 + TF(0.125)*sq((ld(v, c      )-ld(v, c   -kk))*dzb + (ld(w, c      )-ld(w, c-jj   ))*dyi)
+                 + TF(0.125)*sq((ld(v, c+jj   )-ld(v, c+jj-kk))*dzb + (ld(w, c+jj   )-ld(w, c      ))*dyi)
+                 + TF(0.125)*sq((ld(v, c   +kk)-ld(v, c      ))*dzt + (ld(w, c   +kk)-ld(w, c-jj+kk))*dyi)
+                 + TF(0.125)*sq((ld(v, c+jj+kk)-ld(v, c+jj   ))*dzt + (ld(w, c+jj+kk)-ld(w, c   +kk))*dyi);
+        }
+        const TF s2 = TF(2)*acc + TF(DSMALL);
+
+        // The squared mixing length is precomputed per level (and with the
+        // Mason wall correction per level and column when z0m is uniform).
+        const TF ml2 = TF(mlen2[k]);
+        TF ev;
+        if (THERMO)
+        {
+            TF n2;
+            if (SURF && k == d.kstart)
+                n2 = TF(dbdz[ij]);
+            else
+                n2 = TF(GRAV)/ld(pr.thref, k)*TF(0.5)*(ld(th, c+kk) - ld(th, c-kk))*ld(pr.dzi, k);
+            TF ratio = n2 / s2 / tpr;
+            ratio = fmin(ratio, TF(1.-DSMALL));
+            ev = ml2*sqrt(s2)*sqrt(TF(1)-ratio);
+        }
+        else if (SURF)
+            ev = ml2*sqrt(s2);
+        else
+        {
+            // Van Driest wall damping of the neutral resolved-wall case,
+            // src/diff_smag2.cxx:74-101.
+            const long long cb = ijk(d, i, j, d.kstart), ct = ijk(d, i, j, d.kend);
+            const TF dzhb = ld(pr.dzhi, d.kstart), dzht = ld(pr.dzhi, d.kend);
+            const TF utb = pow(sq(visc*(ld(u, cb)-ld(u, cb-kk))*dzhb) + sq(visc*(ld(v, cb)-ld(v, cb-kk))*dzhb), TF(0.25));
+            const TF utt = pow(sq(visc*(ld(u, ct)-ld(u, ct-kk))*dzht) + sq(visc*(ld(v, ct)-ld(v, ct-kk))*dzht), TF(0.25));
+            const TF zk = ld(pr.z, k);
+            const TF fb = TF(1) - exp(-(zk*utb)/(TF(26)*visc));
+            const TF ft = TF(1) - exp(-((TF(d.zsize) - zk)*utt)/(TF(26)*visc));
+            const TF fac = fmin(fb, ft);
+            ev = sq(fac)*ml2*sqrt(s2);
+        }
+        evisc[c] = ev;
+    }
+
+    // Mirror of the eddy viscosity over resolved walls, src/diff_smag2.cxx:195-207.
+    template<typename TF>
+    __global__ void k_evisc_mirror(TF* evisc, Dims d)
+    {
+        const int n = blockIdx.x*blockDim.x + threadIdx.x;
+        if (n >= d.ijcells) return;
+        const long long cb = n + (long long)d.kstart*d.ijcells;
+        const long long ct = n + (long long)(d.kend-1)*d.ijcells;
+        evisc[cb - d.ijcells] = evisc[cb];
+        evisc[ct + d.ijcells] = evisc[ct];
+    }
+
+    template<typename TF>
+    void launch_viscosity(const Dims& d, const Prof<TF>& pr, const TF* u, const TF* v, const TF* w, const TF* th,
+                          TF* evisc, const double* mlen2, const double* dudz, const double* dvdz, const double* dbdz,
+                          double cs, double tpr, double visc, int mason, bool surf, bool thermo, cudaStream_t s)
+    {
+        dim3 block(32, 8);
+        dim3 grid((d.itot + 31)/32, (d.jtot + 7)/8, d.ktot);
+        if (surf && thermo)
+            k_viscosity<TF, true, true><<<grid, block, 0, s>>>(d, pr, u, v, w, th, evisc, mlen2, dudz, dvdz, dbdz, TF(cs), TF(tpr), TF(visc), mason);
+        else if (surf)
+            k_viscosity<TF, true, false><<<grid, block, 0, s>>>(d, pr, u, v, w, th, evisc, mlen2, dudz, dvdz, dbdz, TF(cs), TF(tpr), TF(visc), mason);
+        else if (thermo)
+            k_viscosity<TF, false, true><<<grid, block, 0, s>>>(d, pr, u, v, w, th, evisc, mlen2, dudz, dvdz, dbdz, TF(cs), TF(tpr), TF(visc), mason);
+        else
+            k_viscosity<TF, false, false><<<grid, block, 0, s>>>(d, pr, u, v, w, th, evisc, mlen2, dudz, dvdz, dbdz, TF(cs), TF(tpr), TF(visc), mason);
+        count_launch();
+        if (!surf)
+        {
+            k_evisc_mirror<TF><<<(d.ijcells + 255)/256, 256, 0, s>>>(evisc, d);
+            count_launch();
+        }
+        FieldList<TF> fl; fl.n = 1; fl.p[0] = evisc;
+        launch_cyclic(fl, d, 3, s);
+    }
+
+    // ---------------------------------------------------------------------
+    // Fused tendency kernel: every term a substep adds to ut, vt, wt and st
+    // before the pressure solve (thermo buoyancy, advection, diffusion,
+    // large-scale pressure force), one interior cell per thread.
+    // ---------------------------------------------------------------------
+    template<typename TF, int ADV, int DIF, bool SURF, bool SCAL, bool BUOY, bool FORCE>
+    __global__ void __launch_bounds__(256)
+    k_tendency(Dims d, Prof<TF> pr, TendArgs<TF> a)
+    {
+        const int i = d.istart + blockIdx.x*blockDim.x + threadIdx.x;
+        const int j = d.jstart + blockIdx.y*blockDim.y + threadIdx.y;
+        const int k = d.kstart + blockIdx.z;
+        if (i >= d.iend || j >= d.jend) return;
+        const long long c = ijk(d, i, j, k);
+        const long long ij = i + (long long)j*d.icells;
+        const TF dxi = TF(d.dxi), dyi = TF(d.dyi);
+        const TF* u = a.u; const TF* v = a.v; const TF* w = a.w;
+
+        // u
+        {
+            TF t = TF(0);
+            if (ADV == MHH_ADVEC_2I5) t += advec_2i5_u(d, pr, u, v, w, c, k, dxi, dyi);
+            else if (ADV == MHH_ADVEC_2) t += advec_2_u(d, pr, u, v, w, c, k, dxi, dyi);
+            if (DIF == MHH_DIFF_SMAG2) t += diff_smag2_u(d, pr, u, v, w, a.evisc, a.u_fluxbot, a.u_fluxtop, SURF, c, ij, k, dxi, dyi, a.visc);
+            else if (DIF == MHH_DIFF_2) t += diff_2_c(d, pr, u, c, k, a.dxidxi, a.dyidyi, a.visc);
+            if (FORCE) t += a.fbody;
+            a.ut[c] += t;
+        }
+        // v
+        {
+            TF t = TF(0);
+            if (ADV == MHH_ADVEC_2I5) t += advec_2i5_v(d, pr, u, v, w, c, k, dxi, dyi);
+            else if (ADV == MHH_ADVEC_2) t += advec_2_v(d, pr, u, v, w, c, k, dxi, dyi);
+            if (DIF == MHH_DIFF_SMAG2) t += diff_smag2_v(d, pr, u, v, w, a.evisc, a.v_fluxbot, a.v_fluxtop, SURF, c, ij, k, dxi, dyi, a.visc);
+            else if (DIF == MHH_DIFF_2) t += diff_2_c(d, pr, v, c, k, a.dxidxi, a.dyidyi, a.visc);
+            a.vt[c] += t;
+        }
+        // w (half levels above the wall)
+        if (k > d.kstart)
+        {
+            TF t = TF(0);
+            if (BUOY) t += TF(GRAV)/ld(pr.threfh, k)*(i2(ld(a.s, c-d.ijcells), ld(a.s, c)) - ld(pr.threfh, k));
+            if (ADV == MHH_ADVEC_2I5) t += advec_2i5_w(d, pr, u, v, w, c, k, dxi, dyi);
+            else if (ADV == MHH_ADVEC_2) t += advec_2_w(d, pr, u, v, w, c, k, dxi, dyi);
+            if (DIF == MHH_DIFF_SMAG2) t += diff_smag2_w(d, pr, u, v, w, a.evisc, c, k, dxi, dyi, a.visc);
+            else if (DIF == MHH_DIFF_2) t += diff_2_w(d, pr, w, c, k, a.dxidxi, a.dyidyi, a.visc);
+            a.wt[c] += t;
+        }
+        // scalar
+        if (SCAL)
+        {
+            TF t = TF(0);
+            if (ADV == MHH_ADVEC_2I5) t += advec_2i5_s(d, pr, a.s, u, v, w, c, k, dxi, dyi);
+            else if (ADV == MHH_ADVEC_2) t += advec_2_s(d, pr, a.s, u, v, w, c, k, dxi, dyi);
+            if (DIF == MHH_DIFF_SMAG2)
+                t += diff_smag2_s(d, pr, a.s, a.evisc, a.s_fluxbot, a.s_fluxtop, SURF, c, ij, k,
+                                  TF(a.dxidxi), TF(a.dyidyi), a.tpri, a.svisc);
+            else if (DIF == MHH_DIFF_2) t += diff_2_c(d, pr, a.s, c, k, a.dxidxi, a.dyidyi, a.svisc);
+            a.st[c] += t;
+        }
+    }
+
+    template<typename TF, int ADV, int DIF, bool SURF, bool SCAL, bool BUOY, bool FORCE>
+    static void launch_tend_t(const Dims& d, const Prof<TF>& pr, const TendArgs<TF>& a, cudaStream_t s)
+    {
+        dim3 block(32, 8);
+        dim3 grid((d.itot + 31)/32, (d.jtot + 7)/8, d.ktot);
+        k_tendency<TF, ADV, DIF, SURF, SCAL, BUOY, FORCE><<<grid, block, 0, s>>>(d, pr, a);
+        count_launch();
+    }
+
+    template<typename TF, int ADV, int DIF>
+    static void launch_tend_b(const Dims& d, const Prof<TF>& pr, const TendArgs<TF>& a,
+                              bool surf, bool scal, bool buoy, bool force, cudaStream_t s)
+    {
+        // One instantiation per combination of the four switches.
+        const int mask = (surf ? 8 : 0) | (scal ? 4 : 0) | (buoy ? 2 : 0) | (force ? 1 : 0);
+        switch (mask)
+        {
+#define MHH_TEND_CASE(M) case M: launch_tend_t<TF, ADV, DIF, ((M) & 8) != 0, ((M) & 4) != 0, ((M) & 2) != 0, ((M) & 1) != 0>(d, pr, a, s); break;
+            MHH_TEND_CASE(0) MHH_TEND_CASE(1) MHH_TEND_CASE(2) MHH_TEND_CASE(3)
+            MHH_TEND_CASE(4) MHH_TEND_CASE(5) MHH_TEND_CASE(6) MHH_TEND_CASE(7)
+            MHH_TEND_CASE(8) MHH_TEND_CASE(9) MHH_TEND_CASE(10) MHH_TEND_CASE(11)
+            MHH_TEND_CASE(12) MHH_TEND_CASE(13) MHH_TEND_CASE(14) MHH_TEND_CASE(15)
+#undef MHH_TEND_CASE
+        }
+    }
+
+    template<typename TF>
+    void launch_tendency(const Dims& d, const Prof<TF>& pr, const TendArgs<TF>& a, int adv, int dif,
+                         bool surf, bool scal, bool buoy, bool force, cudaStream_t s)
+    {
+        // With scalar work requested but no scalar pointer, or buoyancy without
+        // a scalar, fall back to the switches the arguments support.
+        if (adv == MHH_ADVEC_2I5)
+        {
+            if (dif == MHH_DIFF_SMAG2) launch_tend_b<TF, MHH_ADVEC_2I5, MHH_DIFF_SMAG2>(d, pr, a, surf, scal, buoy, force, s);
+            else if (dif == MHH_DIFF_2) launch_tend_b<TF, MHH_ADVEC_2I5, MHH_DIFF_2>(d, pr, a, surf, scal, buoy, force, s);
+            else launch_tend_b<TF, MHH_ADVEC_2I5, 0>(d, pr, a, surf, scal, buoy, force, s);
+        }
+        else if (adv == MHH_ADVEC_2)
+        {
+            if (dif == MHH_DIFF_SMAG2) launch_tend_b<TF, MHH_ADVEC_2, MHH_DIFF_SMAG2>(d, pr, a, surf, scal, buoy, force, s);
+            else if (dif == MHH_DIFF_2) launch_tend_b<TF, MHH_ADVEC_2, MHH_DIFF_2>(d, pr, a, surf, scal, buoy, force, s);
+            else launch_tend_b<TF, MHH_ADVEC_2, 0>(d, pr, a, surf, scal, buoy, force, s);
+        }
+        else
+        {
+            if (dif == MHH_DIFF_SMAG2) launch_tend_b<TF, 0, MHH_DIFF_SMAG2>(d, pr, a, surf, scal, buoy, force, s);
+            else if (dif == MHH_DIFF_2) launch_tend_b<TF, 0, MHH_DIFF_2>(d, pr, a, surf, scal, buoy, force, s);
+            else launch_tend_b<TF, 0, 0>(d, pr, a, surf, scal, buoy, force, s);
+        }
+    }
+
+    // ---------------------------------------------------------------------
+    // RK3, src/timeloop.cxx:250-286: a += cB*dt*at; at *= cA(next), or zero
+    // at over all cells (ghosts included) after the last substep.
+    // ---------------------------------------------------------------------
+    template<typename TF>
+    __global__ void k_rk3(TF* __restrict__ a, TF* __restrict__ at, Dims d, TF cbdt, TF ca, int last)
+    {
+        const long long n = blockIdx.x*(long long)blockDim.x + threadIdx.x;
+        if (n >= d.ncells) return;
+        const int i = (int)(n % d.icells);
+        const int j = (int)((n / d.icells) % d.jcells);
+        const int k = (int)(n / d.ijcells);
+        const bool interior = i >= d.istart && i < d.iend && j >= d.jstart && j < d.jend && k >= d.kstart && k < d.kend;
+        if (interior)
+        {
+            const TF t = at[n];
+            a[n] += cbdt*t;
+            at[n] = last ? TF(0) : t*ca;
+        }
+        else if (last)
+            at[n] = TF(0);
+    }
+
+    template<typename TF>
+    void launch_rk3(TF* a, TF* at, const Dims& d, int substep, double dt, cudaStream_t s)
+    {
+        const double cA[3] = {0., -5./9., -153./128.};
+        const double cB[3] = {1./3., 15./16., 8./15.};
+        const int sn = (substep + 1) % 3;
+        const long long n = d.ncells;
+        k_rk3<TF><<<(unsigned)((n + 255)/256), 256, 0, s>>>(a, at, d, TF(cB[substep]*dt), TF(cA[sn]), sn == 0);
+        count_launch();
+    }
+
+    // ---------------------------------------------------------------------
+    // Pressure gradient (src/pres_2.cxx:364-387) fused with the RK3 update
+    // of all prognostic fields (src/timeloop.cxx:250-286).  One thread per
+    // cell of the full ghost layout so that the tendencies' ghost cells are
+    // zeroed after the last substep as on the CPU.
+    // ---------------------------------------------------------------------
+    template<typename TF, bool SCAL>
+    __global__ void __launch_bounds__(256)
+    k_presout_rk3(Dims d, Prof<TF> pr, const TF* __restrict__ p,
+                  TF* __restrict__ u, TF* __restrict__ v, TF* __restrict__ w, TF* __restrict__ s,
+                  TF* __restrict__ ut, TF* __restrict__ vt, TF* __restrict__ wt, TF* __restrict__ st,
+                  TF cbdt, TF ca, int last)
+    {
+        const int i = blockIdx.x*blockDim.x + threadIdx.x;
+        const int j = blockIdx.y*blockDim.y + threadIdx.y;
+        const int k = blockIdx.z;
+        if (i >= d.icells || j >= d.jcells) return;
+        const long long c = ijk(d, i, j, k);
+        const bool interior = i >= d.istart && i < d.iend && j >= d.jstart && j < d.jend && k >= d.kstart && k < d.kend;
+        if (interior)
+        {
+            const TF pc = ld(p, c);
+            TF tu = ut[c] - (pc - ld(p, c-1))*TF(d.dxi);
+            TF tv = vt[c] - (pc - ld(p, c-d.icells))*TF(d.dyi);
+            TF tw = wt[c] - (pc - ld(p, c-d.ijcells))*ld(pr.dzhi, k);
+            u[c] += cbdt*tu; v[c] += cbdt*tv; w[c] += cbdt*tw;
+            ut[c] = last ? TF(0) : tu*ca;
+            vt[c] = last ? TF(0) : tv*ca;
+            wt[c] = last ? TF(0) : tw*ca;
+            if (SCAL)
+            {
+                const TF ts = st[c];
+                s[c] += cbdt*ts;
+                st[c] = last ? TF(0) : ts*ca;
+            }
+        }
+        else if (last)
+        {
+            ut[c] = TF(0); vt[c] = TF(0); wt[c] = TF(0);
+            if (SCAL) st[c] = TF(0);
+        }
+    }
+
+    template<typename TF>
+    void launch_presout_rk3(const Dims& d, const Prof<TF>& pr, const TF* p, TF* u, TF* v, TF* w, TF* s,
+                            TF* ut, TF* vt, TF* wt, TF* st, int substep, double dt, cudaStream_t strm)
+    {
+        const double cA[3] = {0., -5./9., -153./128.};
+        const double cB[3] = {1./3., 15./16., 8./15.};
+        const int sn = (substep + 1) % 3;
+        dim3 block(32, 8);
+        dim3 grid((d.icells + 31)/32, (d.jcells + 7)/8, d.kcells);
+        if (s)
+            k_presout_rk3<TF, true><<<grid, block, 0, strm>>>(d, pr, p, u, v, w, s, ut, vt, wt, st, TF(cB[substep]*dt), TF(cA[sn]), sn == 0);
+        else
+            k_presout_rk3<TF, false><<<grid, block, 0, strm>>>(d, pr, p, u, v, w, s, ut, vt, wt, st, TF(cB[substep]*dt), TF(cA[sn]), sn == 0);
+        count_launch();
+    }
+
+    // ---------------------------------------------------------------------
+    // Max reductions in double: CFL of Advec_2i5 (src/advec_2i5.cxx:59-148)
+    // and Advec_2 (src/advec_2.cxx:50-80), diffusion number of Diff_smag2
+    // (include/diff_kernels.h:486-511), divergence (src/pres_2.cxx:389-422).
+    // ---------------------------------------------------------------------
+    template<typename TF, int WHAT>
+    __global__ void __launch_bounds__(256)
+    k_reduce(Dims d, Prof<TF> pr, const TF* __restrict__ u, const TF* __restrict__ v, const TF* __restrict__ w,
+             const TF* __restrict__ ev, double tprfi, unsigned long long* out)
+    {
+        const int i = d.istart + blockIdx.x*blockDim.x + threadIdx.x;
+        const int j = d.jstart + blockIdx.y*blockDim.y + threadIdx.y;
+        const int k = d.kstart + blockIdx.z;
+        double val = 0.;
+        if (i < d.iend && j < d.jend)
+        {
+            const long long ii = 1, jj = d.icells, kk = d.ijcells;
+            const long long c = ijk(d, i, j, k);
+            if (WHAT == 0)
+            {
+                // CFL 2i5: w interpolated with 2nd/4th/6th order by level.
+                const int ord = face_order_w(d, k);
+                TF wc;
+                if (ord == 2) wc = f2(w, c+kk, kk);
+                else if (ord == 4) wc = f4(w, c+kk, kk);
+                else wc = f6(w, c+kk, kk);
+                val = double(fabs(f6(u, c+ii, ii))*TF(d.dxi) + fabs(f6(v, c+jj, jj))*TF(d.dyi) + fabs(wc)*ld(pr.dzi, k));
+            }
+            else if (WHAT == 1)
+            {
+                val = double(fabs(i2(ld(u, c), ld(u, c+ii)))*TF(d.dxi) + fabs(i2(ld(v, c), ld(v, c+jj)))*TF(d.dyi)
+                           + fabs(i2(ld(w, c), ld(w, c+kk)))*ld(pr.dzi, k));
+            }
+            else if (WHAT == 2)
+            {
+                const double dzi = double(ld(pr.dzi, k));
+                val = fabs(double(ld(ev, c))*tprfi*(d.dxi*d.dxi + d.dyi*d.dyi + dzi*dzi));
+            }
+            else
+            {
+                const double div = double(ld(pr.rhoref, k))*(double(ld(u, c+ii)-ld(u, c))*d.dxi + double(ld(v, c+jj)-ld(v, c))*d.dyi)
+                                 + (double(ld(pr.rhorefh, k+1))*double(ld(w, c+kk)) - double(ld(pr.rhorefh, k))*double(ld(w, c)))*double(ld(pr.dzi, k));
+                val = fabs(div);
+            }
+        }
+        // Block max, then one atomic per block.
+        for (int o=16; o>0; o>>=1)
+            val = fmax(val, __shfl_xor_sync(0xffffffffu, val, o));
+        __shared__ double sm[8];
+        const int lane = (threadIdx.x + threadIdx.y*blockDim.x) & 31;
+        const int warp = (threadIdx.x + threadIdx.y*blockDim.x) >> 5;
+        if (lane == 0) sm[warp] = val;
+        __syncthreads();
+        if (warp == 0)
+        {
+            val = lane < (int)(blockDim.x*blockDim.y/32) ? sm[lane] : 0.;
+            for (int o=16; o>0; o>>=1)
+                val = fmax(val, __shfl_xor_sync(0xffffffffu, val, o));
+            if (lane == 0) atomic_max_nonneg(out, val);
+        }
+    }
+
+    template<typename TF>
+    void launch_reduce(int what, const Dims& d, const Prof<TF>& pr, const TF* u, const TF* v, const TF* w,
+                       const TF* ev, double tprfi, unsigned long long* out, cudaStream_t s)
+    {
+        dim3 block(32, 8);
+        dim3 grid((d.itot + 31)/32, (d.jtot + 7)/8, d.ktot);
+        if (what == 0) k_reduce<TF, 0><<<grid, block, 0, s>>>(d, pr, u, v, w, ev, tprfi, out);
+        else if (what == 1) k_reduce<TF, 1><<<grid, block, 0, s>>>(d, pr, u, v, w, ev, tprfi, out);
+        else if (what == 2) k_reduce<TF, 2><<<grid, block, 0, s>>>(d, pr, u, v, w, ev, tprfi, out);
+        else k_reduce<TF, 3><<<grid, block, 0, s>>>(d, pr, u, v, w, ev, tprfi, out);
+        count_launch();
+    }
+
+#define MHH_INSTANTIATE(TF) \
+    template void launch_cyclic<TF>(const FieldList<TF>&, const Dims&, int, cudaStream_t); \
+    template void launch_cyclic2d<TF>(TF*, const Dims&, cudaStream_t); \
+    template void launch_set_bc<TF>(TF*, TF*, TF*, int, double, double, int, const Dims&, cudaStream_t); \
+    template void launch_ghost<TF>(const GhostList<TF>&, const Dims&, const TF*, cudaStream_t); \
+    template void launch_viscosity<TF>(const Dims&, const Prof<TF>&, const TF*, const TF*, const TF*, const TF*, TF*, \
+        const double*, const double*, const double*, const double*, double, double, double, int, bool, bool, cudaStream_t); \
+    template void launch_tendency<TF>(const Dims&, const Prof<TF>&, const TendArgs<TF>&, int, int, bool, bool, bool, bool, cudaStream_t); \
+    template void launch_rk3<TF>(TF*, TF*, const Dims&, int, double, cudaStream_t); \
+    template void launch_presout_rk3<TF>(const Dims&, const Prof<TF>&, const TF*, TF*, TF*, TF*, TF*, TF*, TF*, TF*, TF*, int, double, cudaStream_t); \
+    template void launch_reduce<TF>(int, const Dims&, const Prof<TF>&, const TF*, const TF*, const TF*, const TF*, double, unsigned long long*, cudaStream_t);
+
+    MHH_INSTANTIATE(double)
+    MHH_INSTANTIATE(float)
+}

@@ -1,0 +1,319 @@
+// mhh_host.h -- C++ host layer with the reference's class API for the
+// LES/DNS time step (Input, Grid, Fields, Boundary, Thermo_dry, Force, Advec,
+// Diff, Pres, Timeloop, Model), device-resident, on top of the C-ABI of
+// include/mhh.h.  Class and member names follow the reference
+// (include/advec.h:45-70, include/diff.h:37-71, include/pres.h:39-85,
+// include/timeloop.h:49-139, src/model.cxx) so that a caller of those classes
+// finds the same entry points; the arithmetic runs in the CUDA kernels behind
+// the C-ABI.  Errors raise std::runtime_error, as in the reference.
+#pragma once
+
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "mhh.h"
+
+namespace mhh_host
+{
+    // ---- .ini input, src/input.cxx:77-222 -------------------------------
+    class Input
+    {
+        public:
+            explicit Input(const std::string& ini_text);
+            template<typename T> T get_item(const std::string& group, const std::string& key, const std::string& sub);
+            template<typename T> T get_item(const std::string& group, const std::string& key, const std::string& sub, const T def);
+            std::vector<std::string> unused_items() const;
+        private:
+            bool find(const std::string& g, const std::string& k, const std::string& s, std::string& out);
+            // group -> key -> subkey -> (value, used)
+            std::map<std::string, std::map<std::string, std::map<std::string, std::pair<std::string, bool>>>> items;
+    };
+
+    void check(int rc, const char* what);
+
+    template<typename TF> class Grid;
+    template<typename TF> class Fields;
+
+    // Statistics are out of scope; the hooks the modules call are kept.
+    template<typename TF> struct Stats { void calc_tend(const std::string&, const std::string&) {} };
+
+    // ---- Grid, src/grid.cxx ----------------------------------------------
+    template<typename TF>
+    class Grid
+    {
+        public:
+            Grid(Input&, int igc);
+            ~Grid();
+            void create(const std::vector<double>& z);
+            const mhh_grid& get_grid_data() const { return gd; }
+            mhh_ctx* ctx() const { return ctx_; }
+            std::vector<double> profile(const std::string& name) const;
+            mhh_grid_desc desc;
+            mhh_physics phys;
+        private:
+            mhh_grid gd;
+            mhh_ctx* ctx_ = nullptr;
+    };
+
+    // ---- Field3d / Fields, include/field3d.h, include/fields.h ----------
+    template<typename TF>
+    struct Field3d
+    {
+        std::string name;
+        TF* fld_g = nullptr;
+        TF *fld_bot_g = nullptr, *fld_top_g = nullptr;
+        TF *grad_bot_g = nullptr, *grad_top_g = nullptr;
+        TF *flux_bot_g = nullptr, *flux_top_g = nullptr;
+        double visc = 0.;
+        Field3d(const std::string& n, long long ncells, int ijcells);
+        ~Field3d();
+    };
+
+    template<typename TF>
+    class Fields
+    {
+        public:
+            Fields(Grid<TF>&, Input&, bool with_scalar, bool with_evisc);
+            std::map<std::string, std::shared_ptr<Field3d<TF>>> mp, mt, sp, st, sd;
+            double visc, svisc;
+            mhh_fields dev() const;          // device pointers for the C-ABI
+            mhh_bcfields bc() const;
+            void set_from_host(const std::string& name, const double* data);
+            void get_to_host(const std::string& name, double* data) const;
+        private:
+            Grid<TF>& grid;
+            Field3d<TF>* by_name(const std::string& name) const;
+    };
+
+    // ---- Boundary, src/boundary.cxx + src/boundary_surface.cxx -----------
+    template<typename TF>
+    class Boundary
+    {
+        public:
+            Boundary(Grid<TF>&, Fields<TF>&, Input&);
+            void set_values();
+            void set_prognostic_cyclic_bcs(cudaStream_t);
+            void set_ghost_cells(cudaStream_t);
+            void exec(cudaStream_t);                 // surface layer when swboundary=surface
+            std::string get_switch() const { return swboundary; }
+            int mbcbot, mbctop, sbcbot, sbctop;
+            double ubot, utop, vbot, vtop, sbot, stop;
+        private:
+            Grid<TF>& grid;
+            Fields<TF>& fields;
+            std::string swboundary;
+    };
+
+    template<typename TF>
+    class Thermo_dry
+    {
+        public:
+            Thermo_dry(Grid<TF>&, Fields<TF>&, Input&);
+            bool enabled() const { return swthermo; }
+            void exec(double dt, cudaStream_t);      // src/thermo_dry.cxx:610-644
+        private:
+            Grid<TF>& grid;
+            Fields<TF>& fields;
+            bool swthermo;
+    };
+
+    template<typename TF>
+    class Force
+    {
+        public:
+            Force(Grid<TF>&, Fields<TF>&, Input&);
+            void exec(double dt, cudaStream_t);      // src/force.cxx:610-640
+            bool dpdx_on;
+            double dpdx;
+        private:
+            Grid<TF>& grid;
+            Fields<TF>& fields;
+    };
+
+    // ---- Advec, include/advec.h:45-70 ------------------------------------
+    template<typename TF>
+    class Advec
+    {
+        public:
+            Advec(Grid<TF>&, Fields<TF>&, Input&);
+            virtual ~Advec() {}
+            static std::unique_ptr<Advec> factory(Grid<TF>&, Fields<TF>&, Input&);
+            virtual void create(Stats<TF>&) {}
+            virtual void exec(Stats<TF>&) = 0;
+            virtual unsigned long get_time_limit(unsigned long idt, double dt);
+            virtual double get_cfl(double dt);
+            virtual int get_switch() const = 0;
+            void set_stream(cudaStream_t s) { stream = s; }
+        protected:
+            Grid<TF>& grid;
+            Fields<TF>& fields;
+            double cflmax;
+            const double cflmin = 1.e-5;
+            cudaStream_t stream = 0;
+    };
+
+    template<typename TF>
+    class Advec_2i5 : public Advec<TF>
+    {
+        public:
+            using Advec<TF>::Advec;
+            void exec(Stats<TF>&) override;
+            int get_switch() const override { return MHH_ADVEC_2I5; }
+    };
+
+    template<typename TF>
+    class Advec_2 : public Advec<TF>
+    {
+        public:
+            using Advec<TF>::Advec;
+            void exec(Stats<TF>&) override;
+            int get_switch() const override { return MHH_ADVEC_2; }
+    };
+
+    // ---- Diff, include/diff.h:37-71 --------------------------------------
+    template<typename TF>
+    class Diff
+    {
+        public:
+            Diff(Grid<TF>&, Fields<TF>&, Boundary<TF>&, Input&);
+            virtual ~Diff() {}
+            static std::unique_ptr<Diff> factory(Grid<TF>&, Fields<TF>&, Boundary<TF>&, Input&);
+            virtual void create(Stats<TF>&, const bool) {}
+            virtual void exec_viscosity(Stats<TF>&, Thermo_dry<TF>&) {}
+            virtual void exec(Stats<TF>&) = 0;
+            virtual unsigned long get_time_limit(unsigned long idt, double dt) = 0;
+            virtual double get_dn(double dt) = 0;
+            virtual int get_switch() const = 0;
+            void set_stream(cudaStream_t s) { stream = s; }
+            TF tPr;
+        protected:
+            Grid<TF>& grid;
+            Fields<TF>& fields;
+            Boundary<TF>& boundary;
+            double dnmax;
+            cudaStream_t stream = 0;
+    };
+
+    template<typename TF>
+    class Diff_smag2 : public Diff<TF>
+    {
+        public:
+            Diff_smag2(Grid<TF>&, Fields<TF>&, Boundary<TF>&, Input&);
+            void exec_viscosity(Stats<TF>&, Thermo_dry<TF>&) override;
+            void exec(Stats<TF>&) override;
+            unsigned long get_time_limit(unsigned long idt, double dt) override;
+            double get_dn(double dt) override;
+            int get_switch() const override { return MHH_DIFF_SMAG2; }
+    };
+
+    template<typename TF>
+    class Diff_2 : public Diff<TF>
+    {
+        public:
+            using Diff<TF>::Diff;
+            void exec(Stats<TF>&) override;
+            unsigned long get_time_limit(unsigned long idt, double dt) override;
+            double get_dn(double dt) override;
+            int get_switch() const override { return MHH_DIFF_2; }
+    };
+
+    // ---- Pres, include/pres.h:39-85 --------------------------------------
+    template<typename TF>
+    class Pres
+    {
+        public:
+            Pres(Grid<TF>&, Fields<TF>&, Input&);
+            virtual ~Pres() {}
+            static std::unique_ptr<Pres> factory(Grid<TF>&, Fields<TF>&, Input&);
+            virtual void exec(double dt, Stats<TF>&) = 0;
+            virtual TF check_divergence() = 0;
+            void set_stream(cudaStream_t s) { stream = s; }
+        protected:
+            Grid<TF>& grid;
+            Fields<TF>& fields;
+            cudaStream_t stream = 0;
+    };
+
+    template<typename TF>
+    class Pres_2 : public Pres<TF>
+    {
+        public:
+            using Pres<TF>::Pres;
+            void exec(double dt, Stats<TF>&) override;
+            TF check_divergence() override;
+    };
+
+    // ---- Timeloop, include/timeloop.h:49-139 (RK3) -----------------------
+    template<typename TF>
+    class Timeloop
+    {
+        public:
+            Timeloop(Grid<TF>&, Fields<TF>&, Input&);
+            void exec(cudaStream_t);
+            double get_sub_time_step() const;
+            void set_time_step_limit() { idtlim = idtmax; }
+            void set_time_step_limit(unsigned long lim) { idtlim = std::min(idtlim, lim); }
+            void set_time_step();
+            bool in_substep() const { return substep > 0; }
+            void step_time();
+            double get_dt() const { return dt; }
+            unsigned long get_idt() const { return idt; }
+            unsigned long get_itime() const { return itime; }
+            int get_substep() const { return substep; }
+            int get_iteration() const { return iteration; }
+            double get_time() const { return time; }
+            void advance_substep() { substep = (substep + 1) % 3; }
+        private:
+            Grid<TF>& grid;
+            Fields<TF>& fields;
+            bool adaptivestep;
+            double dt, dtmax, time;
+            unsigned long itime, idt, idtmax, idtlim;
+            int substep, iteration;
+    };
+
+    // ---- Model, src/model.cxx:327-581 -------------------------------------
+    template<typename TF>
+    class Model
+    {
+        public:
+            explicit Model(const std::string& ini_text);
+            ~Model();
+            // Grid::create with the ktot full levels, then the modules in the
+            // order of src/model.cxx:109-300 (cold start).
+            void init(const std::vector<double>& z);
+            void set_field(const std::string& name, const double* data);
+            void get_field(const std::string& name, double* data);
+            // n full RK3 steps; fused = one fused tendency kernel + fused
+            // pressure-gradient/RK3 per substep, else the module-by-module
+            // sequence of the reference loop.
+            void run_steps(int n, bool fused);
+            void run_substeps(int n, bool fused);
+            double get_cfl();
+            double get_dn();
+            double get_div();
+            Grid<TF>& get_grid() { return *grid; }
+            Fields<TF>& get_fields() { return *fields; }
+            Timeloop<TF>& get_timeloop() { return *timeloop; }
+            cudaStream_t stream = 0;
+        private:
+            void set_time_step();
+            void substep_modules();
+            void substep_fused();
+            std::unique_ptr<Input> input;
+            std::unique_ptr<Grid<TF>> grid;
+            std::unique_ptr<Fields<TF>> fields;
+            std::unique_ptr<Boundary<TF>> boundary;
+            std::unique_ptr<Thermo_dry<TF>> thermo;
+            std::unique_ptr<Force<TF>> force;
+            std::unique_ptr<Advec<TF>> advec;
+            std::unique_ptr<Diff<TF>> diff;
+            std::unique_ptr<Pres<TF>> pres;
+            std::unique_ptr<Timeloop<TF>> timeloop;
+            Stats<TF> stats;
+            mhh_substep_config cfg;
+    };
+}

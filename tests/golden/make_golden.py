@@ -58,6 +58,9 @@ def run_reference(case, ref=True):
     names = case.prognostic_names() + ["p"] + (["evisc"] if case.diff == "smag2" else [])
     for n in names:
         res["out_" + n] = m.get(n)
+    # The status diagnostics run after the periodic and wall ghost-cell fill
+    # of the next substep (src/model.cxx:367-382).
+    m.lib.orc_set_cyclic_and_ghost(m.h)
     for n in DIAG:
         res["diag_" + n] = np.float64(getattr(m, n)())
     res["diag_dt"] = np.float64(m.dt())

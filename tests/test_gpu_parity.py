@@ -1,0 +1,164 @@
+"""CUDA path against the oracle and the reference's golden fixtures.
+
+All calls go through the C-ABI (libmhh_gb300.so) and the host layer
+(libmhh_host.so).  FP64: 1e-12 relative per field after one RK3 step (the
+tolerance of the spec parity requirement).  FP32 form: compared with the
+FP64 oracle at the tolerance stated per test.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from microhh_gb300 import cases
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = sorted(glob.glob(os.path.join(HERE, "golden", "*.npz")))
+TOL64 = 1e-12
+
+
+def rel_err(a, b):
+    scale = np.abs(b).max()
+    return float(np.abs(a - b).max() / (scale if scale > 0 else 1.0))
+
+
+@pytest.fixture(scope="module")
+def mhh():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import microhh_gb300
+    microhh_gb300.load()
+    return microhh_gb300
+
+
+def golden_case(name):
+    from tests.golden.make_golden import golden_cases
+    return golden_cases()[name]
+
+
+@pytest.mark.parametrize("fused", [True, False], ids=["fused", "modules"])
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
+def test_golden_fp64(mhh, path, fused):
+    name = os.path.basename(path)[:-4]
+    g = np.load(path)
+    case = golden_case(name)
+    m = mhh.Model(case, precision=mhh.FP64)
+    for n in case.prognostic_names():
+        m.set(n, g["in_" + n])
+    m.run_substeps(3, fused=fused)
+    for key in g.files:
+        if key.startswith("out_"):
+            n = key[4:]
+            err = rel_err(m.get(n), g[key])
+            assert err <= TOL64, (name, n, err)
+    assert m.dt() == float(g["diag_dt"])
+    for d in ("cfl", "dn"):
+        ref = float(g["diag_" + d])
+        got = getattr(m, d)()
+        assert abs(got - ref) <= TOL64 * abs(ref), (name, d, got, ref)
+    from tests.test_oracle import div_scale
+    assert m.div() <= TOL64 * div_scale(case, g), (name, m.div())
+
+
+LARGER = [
+    ("cbl_64x48x32", lambda: cases.drycbl(64, 48, 32, 6400., 4800., 3200., seed=21, noise_z=800.)),
+    ("cbl_60x40x24_radix35", lambda: cases.drycbl(60, 40, 24, 6000., 4000., 2400., seed=22, noise_z=600.)),
+    ("channel_48x36x32", lambda: cases.channel(48, 36, 32, seed=23, dt=5e-4, adaptivestep=True)),
+]
+
+
+@pytest.mark.parametrize("name,make", LARGER, ids=[n for n, _ in LARGER])
+def test_against_oracle_fp64(mhh, oracle_lib, name, make):
+    case = make()
+    m = mhh.Model(case, precision=mhh.FP64)
+    o = oracle_lib.model_from_case(case)
+    m.run_steps(2, fused=True)
+    o.run_substeps(6)
+    for n in case.prognostic_names() + ["p"]:
+        err = rel_err(m.get(n), o.get(n))
+        assert err <= TOL64, (name, n, err)
+
+
+def test_fp32_form_against_fp64_oracle(mhh, oracle_lib):
+    """FP32 storage/stencils/FFTs with FP64 z-solve and reductions: one RK3
+    step within 2e-5 of the FP64 oracle (relative to each field's maximum)."""
+    case = cases.drycbl(64, 48, 32, 6400., 4800., 3200., seed=31, noise_z=800.)
+    m = mhh.Model(case, precision=mhh.FP32)
+    o = oracle_lib.model_from_case(case)
+    m.run_steps(1, fused=True)
+    o.run_substeps(3)
+    for n in ("u", "v", "w"):
+        err = rel_err(m.get(n), o.get(n))
+        assert err <= 2e-5, (n, err)
+    # Potential temperature is ~300 K: compare its deviation from the initial state.
+    th0 = case.embed(case.fields["th"])
+    ok = case.interior(o.get("th") - th0)
+    gk = case.interior(m.get("th") - th0)
+    assert rel_err(gk, ok) <= 2e-4
+
+
+def test_fft_roundtrip_and_dft(mhh):
+    """Forward transforms against numpy's DFT in halfcomplex order, and the
+    inverse pair returns itot*jtot times the input."""
+    import ctypes
+    import torch
+    itot, jtot, ktot = 48, 40, 3
+    desc = mhh.GridDesc(itot, jtot, ktot, 1, 1, 1, 1.0, 1.0, 1.0)
+    phys = mhh.Physics(visc=1e-5, svisc=1e-5, cs=0.23, tpr=1/3., dnmax=0.4, swmason=1, cflmax=1.,
+                       thref0=300., thermo=0, surface=0, z0m=0.1, z0h=0.1)
+    z = np.linspace(0.1, 0.9, ktot)
+    h = ctypes.c_void_p()
+    kern, _ = mhh.load()
+    mhh.check(kern.mhh_ctx_create(ctypes.byref(desc), z.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                  64, ctypes.byref(phys), ctypes.byref(h)))
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal((ktot, jtot, itot))
+    t = torch.tensor(x, dtype=torch.float64, device="cuda")
+    mhh.check(kern.mhh_fft_forward(h, ctypes.c_void_p(t.data_ptr()), None))
+    torch.cuda.synchronize()
+    got = t.cpu().numpy()
+    X = np.fft.fft2(x, axes=(1, 2))   # complex (ky, kx)
+    # Halfcomplex along x then along y: build the expected array.
+    def hc(a, axis):
+        n = a.shape[axis]
+        F = np.fft.fft(a, axis=axis)
+        out = np.empty(a.shape)
+        idx = [slice(None)] * a.ndim
+        for k in range(n // 2 + 1):
+            idx[axis] = k
+            out[tuple(idx)] = F[tuple(idx)].real
+        for k in range(1, (n + 1) // 2):
+            idx[axis] = n - k
+            src = list(idx); src[axis] = k
+            out[tuple(idx)] = F[tuple(src)].imag
+        return out
+    exp = hc(hc(x, 2), 1)
+    assert np.abs(got - exp).max() <= 1e-12 * np.abs(exp).max()
+    mhh.check(kern.mhh_fft_backward(h, ctypes.c_void_p(t.data_ptr()), None))
+    torch.cuda.synchronize()
+    back = t.cpu().numpy()
+    assert np.abs(back - itot * jtot * x).max() <= 1e-12 * itot * jtot * np.abs(x).max()
+    kern.mhh_ctx_destroy(h)
+    del X
+
+
+def test_divergence_after_projection(mhh):
+    case = cases.drycbl(48, 32, 24, 4800., 3200., 2400., seed=41, noise_z=800.)
+    for prec, tol in ((mhh.FP64, 1e-12), (mhh.FP32, 1e-4)):
+        m = mhh.Model(case, precision=prec)
+        m.run_steps(2)
+        w = np.abs(case.interior(m.get("w"))).max()
+        dz = case.zsize / case.ktot
+        assert m.div() <= tol * max(w / dz, 1e-30), (prec, m.div(), w / dz)
+
+
+def test_launches_counted(mhh):
+    case = cases.drycbl(32, 24, 16, 3200., 2400., 1600., seed=5)
+    m = mhh.Model(case)
+    n0 = mhh.launch_count()
+    m.run_steps(1)
+    assert mhh.launch_count() - n0 >= 3 * 10

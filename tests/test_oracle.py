@@ -22,6 +22,14 @@ def rel_err(a, b):
     return np.abs(a - b).max() / (scale if scale > 0 else 1.0)
 
 
+def div_scale(case, g):
+    """Velocity-gradient scale max|u|/min(dx, dy, dz) of a fixture's output."""
+    vmax = max(np.abs(g["out_" + n]).max() for n in ("u", "v", "w"))
+    z = case.z
+    dz = np.diff(np.concatenate(([0.], 0.5 * (z[1:] + z[:-1]), [case.zsize]))).min()
+    return vmax / min(case.xsize / case.itot, case.ysize / case.jtot, dz)
+
+
 def golden_case(name):
     from tests.golden.make_golden import golden_cases
     return golden_cases()[name]
@@ -41,10 +49,14 @@ def test_restatement_matches_reference(oracle_lib, path):
             n = key[4:]
             err = rel_err(m.get(n), g[key])
             assert err <= TOL, (name, n, err)
-    for d in ("cfl", "dn", "div"):
+    m.lib.orc_set_cyclic_and_ghost(m.h)
+    for d in ("cfl", "dn"):
         ref = float(g["diag_" + d])
         got = getattr(m, d)()
-        assert abs(got - ref) <= TOL * max(abs(ref), 1e-300) + 1e-300, (name, d, got, ref)
+        assert abs(got - ref) <= TOL * abs(ref), (name, d, got, ref)
+    # After the projection the divergence is round-off: both must be below
+    # 1e-12 of the velocity-gradient scale.
+    assert max(m.div(), float(g["diag_div"])) <= TOL * div_scale(case, g), name
     assert m.dt() == float(g["diag_dt"])
 
 
