@@ -118,6 +118,16 @@ const char* mhh_last_error(void);
 /* Kernels this library launched since load (for launch accounting). */
 long long mhh_launch_count(void);
 
+/* Live per-kernel-group timing with CUDA events recorded on the launching
+   stream (no counterpart in the reference, which has no event timing):
+   enable, run, then collect (waits for the recorded events) and read the
+   accumulated count and milliseconds per group. */
+int mhh_timing_enable(int on);
+int mhh_timing_reset(void);
+int mhh_timing_collect(void);
+int mhh_timing_count(void);
+int mhh_timing_get(int idx, const char** name, long long* count, double* total_ms);
+
 /* ---------------------------------------------------------------------- */
 /* Boundaries                                                              */
 /* ---------------------------------------------------------------------- */

@@ -26,6 +26,11 @@ const char* mhh_model_last_error(void);
 /* Fields: u v w th ut vt wt tht p evisc. */
 int mhh_model_set_field(mhh_model* m, const char* name, const double* data);
 int mhh_model_get_field(mhh_model* m, const char* name, double* data);
+/* The same with host buffers in the model's own precision (double for FP64,
+   float for FP32), copied on the model's stream without a conversion;
+   asynchronous for page-locked buffers (call mhh_model_synchronize). */
+int mhh_model_set_field_native(mhh_model* m, const char* name, const void* data);
+int mhh_model_get_field_native(mhh_model* m, const char* name, void* data);
 
 /* The time loop of src/model.cxx:356-505: n RK3 steps or substeps.
    fused = 1: one fused tendency kernel and a fused pressure-gradient + RK3

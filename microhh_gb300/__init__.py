@@ -94,6 +94,11 @@ def load():
     # C-ABI of the kernels (include/mhh.h)
     _declare(kern, "mhh_last_error", ctypes.c_char_p, [])
     _declare(kern, "mhh_launch_count", ctypes.c_longlong, [])
+    _declare(kern, "mhh_timing_enable", I, [I])
+    _declare(kern, "mhh_timing_reset", I, [])
+    _declare(kern, "mhh_timing_collect", I, [])
+    _declare(kern, "mhh_timing_count", I, [])
+    _declare(kern, "mhh_timing_get", I, [I, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_longlong), dp])
     _declare(kern, "mhh_ctx_create", I, [ctypes.POINTER(GridDesc), dp, I, ctypes.POINTER(Physics), ctypes.POINTER(P)])
     _declare(kern, "mhh_ctx_destroy", I, [P])
     _declare(kern, "mhh_ctx_get_grid", I, [P, ctypes.POINTER(Grid)])
@@ -129,6 +134,8 @@ def load():
     _declare(host, "mhh_model_destroy", I, [P])
     _declare(host, "mhh_model_set_field", I, [P, ctypes.c_char_p, dp])
     _declare(host, "mhh_model_get_field", I, [P, ctypes.c_char_p, dp])
+    _declare(host, "mhh_model_set_field_native", I, [P, ctypes.c_char_p, P])
+    _declare(host, "mhh_model_get_field_native", I, [P, ctypes.c_char_p, P])
     _declare(host, "mhh_model_run_steps", I, [P, I, I])
     _declare(host, "mhh_model_run_substeps", I, [P, I, I])
     for n in ("mhh_model_get_cfl", "mhh_model_get_dn", "mhh_model_get_div", "mhh_model_get_dt", "mhh_model_get_time"):
@@ -155,6 +162,32 @@ def check(rc, what="mhh"):
 def launch_count():
     kern, _ = load()
     return int(kern.mhh_launch_count())
+
+
+class Timing:
+    """Live per-kernel-group CUDA-event timing of the native library."""
+
+    @staticmethod
+    def enable(on=True):
+        kern, _ = load()
+        check(kern.mhh_timing_enable(1 if on else 0))
+
+    @staticmethod
+    def reset():
+        kern, _ = load()
+        check(kern.mhh_timing_reset())
+
+    @staticmethod
+    def collect():
+        """Returns {group: (launch groups, total ms)}."""
+        kern, _ = load()
+        check(kern.mhh_timing_collect())
+        out = {}
+        for q in range(kern.mhh_timing_count()):
+            name, cnt, ms = ctypes.c_char_p(), ctypes.c_longlong(), ctypes.c_double()
+            check(kern.mhh_timing_get(q, ctypes.byref(name), ctypes.byref(cnt), ctypes.byref(ms)))
+            out[name.value.decode()] = (cnt.value, ms.value)
+        return out
 
 
 def _dptr(a):
@@ -206,6 +239,13 @@ class Model:
         a = np.empty(self.shape, dtype=np.float64)
         check(self.host.mhh_model_get_field(self.h, name.encode(), _dptr(a)), f"get {name}")
         return a
+
+    def set_native(self, name, ptr):
+        """Copies a host buffer in the model's precision (address ``ptr``)."""
+        check(self.host.mhh_model_set_field_native(self.h, name.encode(), ctypes.c_void_p(ptr)), f"set {name}")
+
+    def get_native(self, name, ptr):
+        check(self.host.mhh_model_get_field_native(self.h, name.encode(), ctypes.c_void_p(ptr)), f"get {name}")
 
     def run_steps(self, n, fused=True):
         check(self.host.mhh_model_run_steps(self.h, n, 1 if fused else 0), "run_steps")

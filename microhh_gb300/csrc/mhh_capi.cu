@@ -14,6 +14,50 @@ namespace
 {
     thread_local std::string g_last_error;
     std::atomic<long long> g_launches{0};
+
+    // Live per-kernel timing: CUDA events recorded on the launching stream
+    // around each kernel group, collected after a synchronisation.
+    struct TimerEntry { std::string name; long long count = 0; double ms = 0.; };
+    struct PendingPair { int idx; cudaEvent_t a, b; };
+    bool g_timing = false;
+    std::vector<TimerEntry> g_timers;
+    std::vector<PendingPair> g_pending;
+    std::vector<cudaEvent_t> g_event_pool;
+
+    cudaEvent_t take_event()
+    {
+        if (!g_event_pool.empty()) { cudaEvent_t e = g_event_pool.back(); g_event_pool.pop_back(); return e; }
+        cudaEvent_t e;
+        cudaEventCreate(&e);
+        return e;
+    }
+
+    int timer_index(const char* name)
+    {
+        for (size_t q=0; q<g_timers.size(); ++q) if (g_timers[q].name == name) return (int)q;
+        g_timers.push_back(TimerEntry{name, 0, 0.});
+        return (int)g_timers.size() - 1;
+    }
+
+    struct Timed
+    {
+        PendingPair pp;
+        cudaStream_t s;
+        bool on;
+        Timed(const char* name, cudaStream_t st) : s(st), on(g_timing)
+        {
+            if (!on) return;
+            pp.idx = timer_index(name);
+            pp.a = take_event(); pp.b = take_event();
+            cudaEventRecord(pp.a, s);
+        }
+        ~Timed()
+        {
+            if (!on) return;
+            cudaEventRecord(pp.b, s);
+            g_pending.push_back(pp);
+        }
+    };
 }
 
 void mhh_set_last_error(const char* msg) { g_last_error = msg ? msg : ""; }
@@ -303,18 +347,24 @@ namespace
         const Dims& d = c->d;
         const Prof<TF>& pr = prof<TF>(c);
         FieldList<TF> fl;
-        fl.n = 1; fl.p[0] = T<TF>(f->ut); launch_cyclic(fl, d, MHH_EDGE_EW, s);
-        fl.p[0] = T<TF>(f->vt); launch_cyclic(fl, d, MHH_EDGE_NS, s);
         TF* pk = T<TF>(c->pw.pk);
-        launch_pres_in<TF>(d, pr, CT<TF>(f->u), CT<TF>(f->v), CT<TF>(f->w), CT<TF>(f->ut), CT<TF>(f->vt), CT<TF>(f->wt),
-                           pk, 1./sub_dt, s);
-        launch_fft_x<TF>(c->pw.px, pk, d.jtot*d.ktot, false, 1., s);
-        launch_fft_y<TF>(c->pw.py, pk, d.itot, d.jtot, d.ktot, false, 1., s);
-        launch_tdma<TF>(d, c->pw, pk, s);
-        launch_fft_y<TF>(c->pw.py, pk, d.itot, d.jtot, d.ktot, true, 1./d.jtot, s);
-        launch_fft_x<TF>(c->pw.px, pk, d.jtot*d.ktot, true, 1./d.itot, s);
-        launch_pres_scatter<TF>(d, pk, T<TF>(f->p), s);
-        fl.p[0] = T<TF>(f->p); launch_cyclic(fl, d, MHH_EDGE_BOTH, s);
+        {
+            Timed t("pres_in", s);
+            fl.n = 1; fl.p[0] = T<TF>(f->ut); launch_cyclic(fl, d, MHH_EDGE_EW, s);
+            fl.p[0] = T<TF>(f->vt); launch_cyclic(fl, d, MHH_EDGE_NS, s);
+            launch_pres_in<TF>(d, pr, CT<TF>(f->u), CT<TF>(f->v), CT<TF>(f->w), CT<TF>(f->ut), CT<TF>(f->vt), CT<TF>(f->wt),
+                               pk, 1./sub_dt, s);
+        }
+        { Timed t("fft_x", s); launch_fft_x<TF>(c->pw.px, pk, d.jtot*d.ktot, false, 1., s); }
+        { Timed t("fft_y", s); launch_fft_y<TF>(c->pw.py, pk, d.itot, d.jtot, d.ktot, false, 1., s); }
+        { Timed t("tdma", s); launch_tdma<TF>(d, c->pw, pk, s); }
+        { Timed t("fft_y", s); launch_fft_y<TF>(c->pw.py, pk, d.itot, d.jtot, d.ktot, true, 1./d.jtot, s); }
+        { Timed t("fft_x", s); launch_fft_x<TF>(c->pw.px, pk, d.jtot*d.ktot, true, 1./d.itot, s); }
+        {
+            Timed t("pres_scatter", s);
+            launch_pres_scatter<TF>(d, pk, T<TF>(f->p), s);
+            fl.p[0] = T<TF>(f->p); launch_cyclic(fl, d, MHH_EDGE_BOTH, s);
+        }
         if (with_out)
         {
             dim3 block(32, 8), grid((d.itot + 31)/32, (d.jtot + 7)/8, d.ktot);
@@ -330,6 +380,7 @@ namespace
         if (!f->evisc) return fail(MHH_ERR_ARG, "evisc is NULL");
         const bool surf = c->phys.surface != 0, thermo = c->phys.thermo != 0 && f->s;
         if (surf && !c->surf_ready) return fail(MHH_ERR_ARG, "surface layer not initialised");
+        Timed t("viscosity", s);
         launch_viscosity<TF>(c->d, prof<TF>(c), CT<TF>(f->u), CT<TF>(f->v), CT<TF>(f->w), CT<TF>(f->s), T<TF>(f->evisc),
                              c->sw.mlen2, c->sw.dudz, c->sw.dvdz, c->sw.dbdz, c->phys.cs, c->phys.tpr, c->phys.visc,
                              c->phys.swmason, surf, thermo, s);
@@ -341,6 +392,7 @@ namespace
     {
         if (!c->surf_ready) return fail(MHH_ERR_ARG, "surface layer not initialised");
         const int thermo = (c->phys.thermo && f->s) ? 1 : 0;
+        Timed t("surface", s);
         launch_surface<TF>(c->d, prof<TF>(c), c->sw, CT<TF>(f->u), CT<TF>(f->v), CT<TF>(f->s),
                            T<TF>(bc->u_bot), T<TF>(bc->v_bot), T<TF>(bc->u_fluxbot), T<TF>(bc->v_fluxbot),
                            T<TF>(bc->u_gradbot), T<TF>(bc->v_gradbot),
@@ -374,11 +426,14 @@ namespace
     template<typename TF>
     int substep_begin(mhh_ctx* c, const mhh_substep_config* cfg, const mhh_fields* f, const mhh_bcfields* bc, cudaStream_t s)
     {
-        FieldList<TF> fl{};
-        fl.p[fl.n++] = T<TF>(f->u); fl.p[fl.n++] = T<TF>(f->v); fl.p[fl.n++] = T<TF>(f->w);
-        if (f->s) fl.p[fl.n++] = T<TF>(f->s);
-        launch_cyclic(fl, c->d, MHH_EDGE_BOTH, s);
-        ghost_all<TF>(c, cfg, f, bc, true, s);
+        {
+            Timed t("boundaries", s);
+            FieldList<TF> fl{};
+            fl.p[fl.n++] = T<TF>(f->u); fl.p[fl.n++] = T<TF>(f->v); fl.p[fl.n++] = T<TF>(f->w);
+            if (f->s) fl.p[fl.n++] = T<TF>(f->s);
+            launch_cyclic(fl, c->d, MHH_EDGE_BOTH, s);
+            ghost_all<TF>(c, cfg, f, bc, true, s);
+        }
         if (cfg->diff == MHH_DIFF_SMAG2)
             return viscosity<TF>(c, f, s);
         return check_cuda("substep_begin");
@@ -395,6 +450,7 @@ namespace
         {
             int rc = surface_exec<TF>(c, f, bc, cfg->sbcbot, s);
             if (rc) return rc;
+            Timed t("boundaries", s);
             ghost_all<TF>(c, cfg, f, bc, false, s);
         }
         TendArgs<TF> a = tend_args<TF>(c, f, bc);
@@ -402,12 +458,18 @@ namespace
         a.fbody = TF(-1.*cfg->dpdx);
         const bool scal = f->s != nullptr;
         const bool buoy = scal && c->phys.thermo;
-        launch_tendency<TF>(d, pr, a, cfg->advec, cfg->diff, surf, scal, buoy, force, s);
+        {
+            Timed t("tendency", s);
+            launch_tendency<TF>(d, pr, a, cfg->advec, cfg->diff, surf, scal, buoy, force, s);
+        }
         const double cB[3] = {1./3., 15./16., 8./15.};
         int rc = pres_exec<TF>(c, f, cB[substep]*dt, false, s);
         if (rc) return rc;
-        launch_presout_rk3<TF>(d, pr, CT<TF>(f->p), T<TF>(f->u), T<TF>(f->v), T<TF>(f->w), T<TF>(f->s),
-                               T<TF>(f->ut), T<TF>(f->vt), T<TF>(f->wt), T<TF>(f->st), substep, dt, s);
+        {
+            Timed t("presout_rk3", s);
+            launch_presout_rk3<TF>(d, pr, CT<TF>(f->p), T<TF>(f->u), T<TF>(f->v), T<TF>(f->w), T<TF>(f->s),
+                                   T<TF>(f->ut), T<TF>(f->vt), T<TF>(f->wt), T<TF>(f->st), substep, dt, s);
+        }
         return check_cuda("substep_end");
     }
 }
@@ -417,6 +479,46 @@ namespace
 extern "C" {
 
 const char* mhh_last_error(void) { return g_last_error.c_str(); }
+
+int mhh_timing_enable(int on)
+{
+    g_timing = on != 0;
+    return MHH_OK;
+}
+
+int mhh_timing_reset(void)
+{
+    for (auto& p : g_pending) { g_event_pool.push_back(p.a); g_event_pool.push_back(p.b); }
+    g_pending.clear();
+    g_timers.clear();
+    return MHH_OK;
+}
+
+int mhh_timing_collect(void)
+{
+    for (auto& p : g_pending)
+    {
+        if (cudaEventSynchronize(p.b) != cudaSuccess) return fail(MHH_ERR_CUDA, "timing event");
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, p.a, p.b);
+        g_timers[p.idx].ms += ms;
+        g_timers[p.idx].count += 1;
+        g_event_pool.push_back(p.a); g_event_pool.push_back(p.b);
+    }
+    g_pending.clear();
+    return MHH_OK;
+}
+
+int mhh_timing_count(void) { return (int)g_timers.size(); }
+
+int mhh_timing_get(int idx, const char** name, long long* count, double* total_ms)
+{
+    if (idx < 0 || idx >= (int)g_timers.size() || !name || !count || !total_ms) return fail(MHH_ERR_ARG, "bad timer index");
+    *name = g_timers[idx].name.c_str();
+    *count = g_timers[idx].count;
+    *total_ms = g_timers[idx].ms;
+    return MHH_OK;
+}
 long long mhh_launch_count(void) { return mhh::launch_count(); }
 
 int mhh_ctx_create(const mhh_grid_desc* desc, const double* z, int precision, const mhh_physics* phys, mhh_ctx** out)

@@ -319,6 +319,22 @@ namespace mhh_host
         }
     }
 
+    template<typename TF>
+    void Fields<TF>::set_native(const std::string& name, const void* data, cudaStream_t s)
+    {
+        Field3d<TF>* f = by_name(name);
+        cuda_check(cudaMemcpyAsync(f->fld_g, data, sizeof(TF)*grid.get_grid_data().ncells, cudaMemcpyHostToDevice, s),
+                   "set field");
+    }
+
+    template<typename TF>
+    void Fields<TF>::get_native(const std::string& name, void* data, cudaStream_t s) const
+    {
+        Field3d<TF>* f = by_name(name);
+        cuda_check(cudaMemcpyAsync(data, f->fld_g, sizeof(TF)*grid.get_grid_data().ncells, cudaMemcpyDeviceToHost, s),
+                   "get field");
+    }
+
     // ---------------------------------------------------------------------
     // Boundary, src/boundary.cxx:185-262 (process_bcs), :615-700 (set_values)
     // and src/boundary_surface.cxx:755-790 (surface override).
@@ -855,6 +871,10 @@ int mhh_model_destroy(mhh_model* mm)
 
 int mhh_model_set_field(mhh_model* mm, const char* name, const double* data) { WITH_MODEL(mm, m.set_field(name, data)); }
 int mhh_model_get_field(mhh_model* mm, const char* name, double* data) { WITH_MODEL(mm, m.get_field(name, data)); }
+int mhh_model_set_field_native(mhh_model* mm, const char* name, const void* data)
+{ WITH_MODEL(mm, m.get_fields().set_native(name, data, m.stream)); }
+int mhh_model_get_field_native(mhh_model* mm, const char* name, void* data)
+{ WITH_MODEL(mm, m.get_fields().get_native(name, data, m.stream)); }
 int mhh_model_run_steps(mhh_model* mm, int n, int fused) { WITH_MODEL(mm, m.run_steps(n, fused != 0)); }
 int mhh_model_run_substeps(mhh_model* mm, int n, int fused) { WITH_MODEL(mm, m.run_substeps(n, fused != 0)); }
 int mhh_model_get_cfl(mhh_model* mm, double* out) { WITH_MODEL(mm, *out = m.get_cfl()); }

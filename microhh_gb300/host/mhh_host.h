@@ -83,6 +83,10 @@ namespace mhh_host
             mhh_bcfields bc() const;
             void set_from_host(const std::string& name, const double* data);
             void get_to_host(const std::string& name, double* data) const;
+            // Host buffers already in the model precision (TF), copied on the
+            // given stream (asynchronous for page-locked buffers).
+            void set_native(const std::string& name, const void* data, cudaStream_t s);
+            void get_native(const std::string& name, void* data, cudaStream_t s) const;
         private:
             Grid<TF>& grid;
             Field3d<TF>* by_name(const std::string& name) const;
