@@ -226,7 +226,7 @@ namespace
         if ((rc = fft_plan_init(&c->pw.py, d.jtot)) != MHH_OK) return fail(rc, "jtot has a prime factor above 7");
         const size_t tfb = c->prec == MHH_FP64 ? 8 : 4;
         if (cudaMalloc(&c->pw.pk, tfb*n) != cudaSuccess) return fail(MHH_ERR_CUDA, "cudaMalloc pressure");
-        if ((rc = dalloc(&c->pw.work, 2*(size_t)n, false))) return rc;
+        if ((rc = dalloc(&c->pw.work, (size_t)n, false))) return rc;
         if ((rc = dalloc(&c->pw.bmati, d.itot)) || (rc = dalloc(&c->pw.bmatj, d.jtot))) return rc;
         if ((rc = dalloc(&c->pw.a, d.ktot)) || (rc = dalloc(&c->pw.c, d.ktot))) return rc;
         if ((rc = dalloc(&c->pw.dz2, d.ktot)) || (rc = dalloc(&c->pw.dz2rho, d.ktot))) return rc;
@@ -251,6 +251,7 @@ namespace
         if ((rc = upload(c->pw.bmati, bi)) || (rc = upload(c->pw.bmatj, bj))) return rc;
         if ((rc = upload(c->pw.a, a)) || (rc = upload(c->pw.c, cc))) return rc;
         if ((rc = upload(c->pw.dz2, dz2)) || (rc = upload(c->pw.dz2rho, dz2r))) return rc;
+        if ((rc = tdma_table(c->pw, d.itot, d.jtot, d.ktot))) return fail(rc, "tridiagonal table");
         return MHH_OK;
     }
 
@@ -572,6 +573,11 @@ int mhh_ctx_create(const mhh_grid_desc* desc, const double* z, int precision, co
     if (!rc) rc = dalloc(&c->sw.dvdz, d.ijcells);
     if (!rc) rc = dalloc(&c->sw.dbdz, d.ijcells);
     if (!rc) rc = dalloc(&c->sw.dutot, d.ijcells);
+    if (!rc) rc = dalloc(&c->sw.fm, d.ijcells);
+    if (!rc) rc = dalloc(&c->sw.fh, d.ijcells);
+    if (!rc) rc = dalloc(&c->sw.phim, d.ijcells);
+    if (!rc) rc = dalloc(&c->sw.phih, d.ijcells);
+    c->sw.z0h = phys->z0h;
     if (!rc) rc = dalloc(&c->sw.nobuk, d.ijcells);
     if (!rc) rc = dalloc(&c->sw.zL, NZL_LUT);
     if (!rc) rc = dalloc(&c->sw.f, NZL_LUT);
@@ -602,8 +608,8 @@ int mhh_ctx_destroy(mhh_ctx* c)
     if (!c) return MHH_OK;
     for (auto& p : c->dprof) if (p) cudaFree(p);
     fft_plan_free(&c->pw.px); fft_plan_free(&c->pw.py);
-    void* ptrs[] = {c->pw.pk, c->pw.work, c->pw.bmati, c->pw.bmatj, c->pw.a, c->pw.c, c->pw.dz2, c->pw.dz2rho,
-                    c->red, c->sw.ustar, c->sw.obuk, c->sw.dudz, c->sw.dvdz, c->sw.dbdz, c->sw.dutot,
+    void* ptrs[] = {c->pw.pk, c->pw.work, c->pw.rtab, c->pw.bmati, c->pw.bmatj, c->pw.a, c->pw.c, c->pw.dz2, c->pw.dz2rho,
+                    c->red, c->sw.fm, c->sw.fh, c->sw.phim, c->sw.phih, c->sw.ustar, c->sw.obuk, c->sw.dudz, c->sw.dvdz, c->sw.dbdz, c->sw.dutot,
                     c->sw.nobuk, c->sw.zL, c->sw.f, c->sw.mlen2};
     for (void* p : ptrs) if (p) cudaFree(p);
     if (c->red_host) cudaFreeHost(c->red_host);

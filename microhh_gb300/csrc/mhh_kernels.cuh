@@ -79,8 +79,12 @@ namespace mhh
         double* c;            // ktot
         double* dz2;          // ktot: dz^2
         double* dz2rho;       // ktot: dz^2 * rhoref
-        double* work;         // itot*jtot*ktot doubles: Thomas coefficients
+        double* work;         // itot*jtot*ktot doubles: forward-swept right-hand side
+        double* rtab;         // (itot/2+1)*(jtot/2+1)*ktot: 1/den per column group and level
+        int niu, nju;
     };
+
+    int tdma_table(PresWork& pw, int itot, int jtot, int ktot);
 
     template<typename TF> void launch_pres_in(const Dims& d, const Prof<TF>& pr, const TF* u, const TF* v, const TF* w,
                                               const TF* ut, const TF* vt, const TF* wt, TF* pk, double dti, cudaStream_t s);
@@ -94,6 +98,8 @@ namespace mhh
     struct SurfWork
     {
         double *ustar, *obuk, *dudz, *dvdz, *dbdz, *dutot;
+        double *fm, *fh, *phim, *phih;   // per-cell Monin-Obukhov functions of the last stability call
+        double z0h;
         int* nobuk;
         float *zL, *f;
         double *mlen2;   // kcells: squared Smagorinsky mixing length per level

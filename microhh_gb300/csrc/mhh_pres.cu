@@ -126,6 +126,125 @@ namespace mhh
         return which;
     }
 
+
+    // ---- fixed-length transforms -----------------------------------------
+    // For the common lengths the radices are compile-time constants (8 first,
+    // then 4, 2, 3, 5), so all index arithmetic folds into shifts and
+    // multiplications and each stage is unrolled.
+    __host__ __device__ constexpr int fixed_radix(int n, int s)
+    {
+        int r = n;
+        for (int q=0; q<=s; ++q)
+        {
+            int f = 0;
+            const int cand[5] = {8, 4, 2, 3, 5};
+            for (int t=0; t<5 && !f; ++t) if (r % cand[t] == 0) f = cand[t];
+            if (q == s) return f;
+            r /= f;
+        }
+        return 0;
+    }
+
+    template<typename T2>
+    __device__ __forceinline__ T2 mul_mi(T2 a) { T2 r; r.x = a.y; r.y = -a.x; return r; }   // -i a
+
+    // Radix-8 DFT (forward, w = exp(-2 pi i/8)) of u[0..7] in place.
+    template<typename TF, typename T2>
+    __device__ __forceinline__ void dft8(T2* u)
+    {
+        const TF h = TF(0.70710678118654752440);
+        // Stage 1: pairs (q, q+4)
+        T2 a0 = cadd(u[0], u[4]), a4 = csub(u[0], u[4]);
+        T2 a1 = cadd(u[1], u[5]), a5 = csub(u[1], u[5]);
+        T2 a2 = cadd(u[2], u[6]), a6 = csub(u[2], u[6]);
+        T2 a3 = cadd(u[3], u[7]), a7 = csub(u[3], u[7]);
+        // twiddles w^q on the odd half: a5 *= w, a6 *= w^2 = -i, a7 *= w^3
+        T2 t5; t5.x = h*(a5.x + a5.y); t5.y = h*(a5.y - a5.x);
+        T2 t6 = mul_mi<T2>(a6);
+        T2 t7; t7.x = h*(a7.y - a7.x); t7.y = -h*(a7.x + a7.y);
+        // Stage 2: radix-4 on (a0,a1,a2,a3) and (a4,t5,t6,t7)
+        T2 b0 = cadd(a0, a2), b2 = csub(a0, a2), b1 = cadd(a1, a3), b3 = mul_mi<T2>(csub(a1, a3));
+        T2 c0 = cadd(a4, t6), c2 = csub(a4, t6), c1 = cadd(t5, t7), c3 = mul_mi<T2>(csub(t5, t7));
+        u[0] = cadd(b0, b1); u[4] = csub(b0, b1);
+        u[2] = cadd(b2, b3); u[6] = csub(b2, b3);
+        u[1] = cadd(c0, c1); u[5] = csub(c0, c1);
+        u[3] = cadd(c2, c3); u[7] = csub(c2, c3);
+    }
+
+    template<typename TF, int N, int P, int S, int PACC>
+    struct FixedStages
+    {
+        using T2 = typename C2<TF>::T;
+        static __device__ __forceinline__ void run(T2*& src, T2*& dst, const T2* __restrict__ tws)
+        {
+            constexpr int R = fixed_radix(N, S);
+            constexpr int T = N / R;
+            constexpr int step = N / (PACC*R);
+            constexpr int NITEM = P*T;
+            for (int it = threadIdx.x; it < NITEM; it += blockDim.x)
+            {
+                const int seq = it / T;
+                const int i = it - seq*T;
+                const int k = i % PACC;
+                const T2* x = src + seq*N;
+                T2* y = dst + seq*N;
+                const int j = (i - k)*R + k;
+                T2 u[R];
+                u[0] = x[i];
+                #pragma unroll
+                for (int q=1; q<R; ++q)
+                    u[q] = (PACC == 1) ? x[i + q*T] : cmul(x[i + q*T], tws[(q*k*step) % N]);
+                if (R == 8) dft8<TF, T2>(u);
+                else if (R == 4)
+                {
+                    const T2 a = cadd(u[0], u[2]), b = csub(u[0], u[2]);
+                    const T2 c = cadd(u[1], u[3]), e = mul_mi<T2>(csub(u[1], u[3]));
+                    u[0] = cadd(a, c); u[2] = csub(a, c); u[1] = cadd(b, e); u[3] = csub(b, e);
+                }
+                else if (R == 2)
+                {
+                    const T2 a = u[0];
+                    u[0] = cadd(a, u[1]); u[1] = csub(a, u[1]);
+                }
+                else if (R == 3)
+                {
+                    const TF s3 = TF(0.86602540378443864676);
+                    const T2 t1 = cadd(u[1], u[2]), t4 = csub(u[1], u[2]);
+                    T2 t2; t2.x = u[0].x - TF(0.5)*t1.x; t2.y = u[0].y - TF(0.5)*t1.y;
+                    u[0] = cadd(u[0], t1);
+                    u[1].x = t2.x + s3*t4.y; u[1].y = t2.y - s3*t4.x;
+                    u[2].x = t2.x - s3*t4.y; u[2].y = t2.y + s3*t4.x;
+                }
+                else
+                {
+                    T2 v[R];
+                    #pragma unroll
+                    for (int r=0; r<R; ++r)
+                    {
+                        T2 acc = u[0];
+                        #pragma unroll
+                        for (int q=1; q<R; ++q) acc = cadd(acc, cmul(u[q], tws[(q*r*T) % N]));
+                        v[r] = acc;
+                    }
+                    #pragma unroll
+                    for (int r=0; r<R; ++r) u[r] = v[r];
+                }
+                #pragma unroll
+                for (int r=0; r<R; ++r) y[j + r*PACC] = u[r];
+            }
+            __syncthreads();
+            T2* t = src; src = dst; dst = t;
+            FixedStages<TF, N, P, S+1, PACC*R>::run(src, dst, tws);
+        }
+    };
+
+    template<typename TF, int N, int P, int S>
+    struct FixedStages<TF, N, P, S, N>
+    {
+        using T2 = typename C2<TF>::T;
+        static __device__ __forceinline__ void run(T2*&, T2*&, const T2*) {}
+    };
+
     // Element j of real sequence s sits at base(s) + j*stride:
     //   rows (x):    base = s*n,                         stride = 1
     //   columns (y): base = (s / itot)*itot*n + s % itot, stride = itot
@@ -142,18 +261,30 @@ namespace mhh
         return (s / L.itot)*(long long)L.itot*n + (s % L.itot);
     }
 
-    // Shared-memory index of element j of local real sequence ls (2P x n, [ls][j]).
-    template<typename TF, bool INV>
+    // One block transforms 2P real sequences: load them into shared memory,
+    // pack pairs as complex, FFT, separate into halfcomplex (forward) or take
+    // real and imaginary parts (inverse), store.  NFIX > 0 selects the
+    // fixed-length path (NFIX = n, PFIX = P); NFIX = 0 the run-time plan.
+    template<typename TF, bool INV, int NFIX, int PFIX>
     __global__ void __launch_bounds__(256)
-    k_fft(FftPlan pl, TF* __restrict__ data, SeqLayout L, int P, TF scale)
+    k_fft(FftPlan pl, TF* __restrict__ data, SeqLayout L, int Prt, TF scale)
     {
         using T2 = typename C2<TF>::T;
         extern __shared__ __align__(16) unsigned char smem_raw[];
-        const int n = pl.n;
+        const int n = NFIX ? NFIX : pl.n;
+        const int P = NFIX ? PFIX : Prt;
         T2* buf0 = reinterpret_cast<T2*>(smem_raw);
         T2* buf1 = buf0 + (size_t)P*n;
-        const long long s0 = (long long)blockIdx.x*2*P;     // first real sequence of this block
+        T2* tws = buf1 + (size_t)P*n;      // twiddle table (fixed path)
+        const long long s0 = (long long)blockIdx.x*2*P;
         const int nloc = (int)min((long long)2*P, L.nseq - s0);
+
+        if (NFIX)
+        {
+            const TF* tt = twtab<TF>(pl);
+            for (int e = threadIdx.x; e < n; e += blockDim.x)
+            { T2 w; w.x = tt[2*e]; w.y = tt[2*e+1]; tws[e] = w; }
+        }
 
         // 1. Load 2P real sequences into buf1 viewed as real [2P][n].
         TF* r1 = reinterpret_cast<TF*>(buf1);
@@ -168,7 +299,6 @@ namespace mhh
         }
         else
         {
-            // Consecutive threads take consecutive columns of one row.
             for (int e = threadIdx.x; e < tot; e += blockDim.x)
             {
                 const int j = e / (2*P), ls = e - j*(2*P);
@@ -196,7 +326,6 @@ namespace mhh
                 const TF xr = hx[kk], yr = hy[kk];
                 const TF xi = real_only ? TF(0) : sg*hx[n - kk];
                 const TF yi = real_only ? TF(0) : sg*hy[n - kk];
-                // Z = (xr - yi) + i (xi + yr); store conj(Z).
                 z.x = xr - yi;
                 z.y = -(xi + yr);
             }
@@ -205,9 +334,22 @@ namespace mhh
         __syncthreads();
 
         // 3. FFT.
-        const int which = stockham<TF>(pl, buf0, buf1, P);
-        T2* res = which ? buf1 : buf0;
-        TF* rout = reinterpret_cast<TF*>(which ? buf0 : buf1);
+        T2* res;
+        T2* other;
+        if (NFIX)
+        {
+            T2* src = buf0;
+            T2* dst = buf1;
+            FixedStages<TF, (NFIX ? NFIX : 1), (PFIX ? PFIX : 1), 0, 1>::run(src, dst, tws);
+            res = src; other = dst;
+        }
+        else
+        {
+            const int which = stockham<TF>(pl, buf0, buf1, P);
+            res = which ? buf1 : buf0;
+            other = which ? buf0 : buf1;
+        }
+        TF* rout = reinterpret_cast<TF*>(other);
 
         // 4. Real outputs into the other buffer, [2P][n].
         for (int e = threadIdx.x; e < P*n; e += blockDim.x)
@@ -267,25 +409,60 @@ namespace mhh
         return P;
     }
 
+    template<typename TF, bool INV, int NF, int PF>
+    static void launch_fixed(const FftPlan& pl, TF* data, SeqLayout L, TF scale, cudaStream_t s)
+    {
+        const size_t smem = sizeof(typename C2<TF>::T)*((size_t)2*PF*NF + NF);
+        const long long nblk = (L.nseq + 2*PF - 1) / (2*PF);
+        cudaFuncSetAttribute(k_fft<TF, INV, NF, PF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_fft<TF, INV, NF, PF><<<(unsigned)nblk, 256, smem, s>>>(pl, data, L, PF, scale);
+    }
+
+    template<typename TF, bool INV, int NF>
+    static bool try_fixed_n(const FftPlan& pl, TF* data, SeqLayout L, TF scale, cudaStream_t s)
+    {
+        if (pl.n != NF) return false;
+        // Rows: 4 pairs per block; columns: 8 (float) or 4 (double) pairs so a
+        // warp reads at least 64 contiguous bytes per row.
+        constexpr int PR = (2*sizeof(typename C2<TF>::T)*4*NF <= 96*1024) ? 4 : 1;
+        constexpr int PC = (sizeof(TF) == 4 && 2*sizeof(typename C2<TF>::T)*8*NF <= 96*1024) ? 8 : PR;
+        if (L.rows) launch_fixed<TF, INV, NF, PR>(pl, data, L, scale, s);
+        else launch_fixed<TF, INV, NF, PC>(pl, data, L, scale, s);
+        return true;
+    }
+
+    template<typename TF, bool INV>
+    static bool launch_fixed_any(const FftPlan& pl, TF* data, SeqLayout L, TF scale, cudaStream_t s)
+    {
+        return try_fixed_n<TF, INV, 512>(pl, data, L, scale, s) || try_fixed_n<TF, INV, 256>(pl, data, L, scale, s)
+            || try_fixed_n<TF, INV, 128>(pl, data, L, scale, s) || try_fixed_n<TF, INV, 64>(pl, data, L, scale, s)
+            || try_fixed_n<TF, INV, 32>(pl, data, L, scale, s) || try_fixed_n<TF, INV, 1024>(pl, data, L, scale, s)
+            || try_fixed_n<TF, INV, 192>(pl, data, L, scale, s) || try_fixed_n<TF, INV, 96>(pl, data, L, scale, s)
+            || try_fixed_n<TF, INV, 48>(pl, data, L, scale, s) || try_fixed_n<TF, INV, 384>(pl, data, L, scale, s)
+            || try_fixed_n<TF, INV, 768>(pl, data, L, scale, s) || try_fixed_n<TF, INV, 16>(pl, data, L, scale, s);
+    }
+
     template<typename TF>
     static void launch_fft(const FftPlan& pl, TF* data, SeqLayout L, bool inverse, TF scale, cudaStream_t s)
     {
         const int n = pl.n;
         if (n == 1) return;
+        count_launch();
+        if (inverse ? launch_fixed_any<TF, true>(pl, data, L, scale, s) : launch_fixed_any<TF, false>(pl, data, L, scale, s))
+            return;
         const int P = pairs_per_block<TF>(n, L.rows != 0);
         const size_t smem = 2*sizeof(typename C2<TF>::T)*(size_t)P*n;
         const long long nblk = (L.nseq + 2*P - 1) / (2*P);
         if (inverse)
         {
-            cudaFuncSetAttribute(k_fft<TF, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            k_fft<TF, true><<<(unsigned)nblk, 256, smem, s>>>(pl, data, L, P, scale);
+            cudaFuncSetAttribute(k_fft<TF, true, 0, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            k_fft<TF, true, 0, 0><<<(unsigned)nblk, 256, smem, s>>>(pl, data, L, P, scale);
         }
         else
         {
-            cudaFuncSetAttribute(k_fft<TF, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            k_fft<TF, false><<<(unsigned)nblk, 256, smem, s>>>(pl, data, L, P, scale);
+            cudaFuncSetAttribute(k_fft<TF, false, 0, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            k_fft<TF, false, 0, 0><<<(unsigned)nblk, 256, smem, s>>>(pl, data, L, P, scale);
         }
-        count_launch();
     }
 
     template<typename TF>
@@ -374,58 +551,118 @@ namespace mhh
     // Tridiagonal solve per spectral column in double, src/pres_2.cxx:200-326:
     // b = dz^2 rho (bmati + bmatj) - (a + c), b[0] += a[0]; the top row gets
     // -c for the mean mode (p = 0 at the top) and +c otherwise (dp/dz = 0);
-    // right-hand side dz^2 p; Thomas algorithm.  The forward sweep keeps c/den
-    // and the swept right-hand side in `work` (two doubles per cell).
+    // right-hand side dz^2 p; Thomas algorithm.
+    //
+    // The elimination coefficients depend on the column only through
+    // lambda = bmati[i] + bmatj[j], and bmati, bmatj are mirror-symmetric
+    // (i and itot - i share a wave number), so the columns form groups of up
+    // to four with identical coefficients.  1/den_k of every group is computed
+    // once at set-up (k_tdma_table); the solve then needs three FP64 operations
+    // per cell, and one thread solves the four columns of a group together.
     // ---------------------------------------------------------------------
-    template<typename TF>
-    __global__ void __launch_bounds__(128)
-    k_tdma(int itot, int jtot, int ktot, const double* __restrict__ bmati, const double* __restrict__ bmatj,
-           const double* __restrict__ a, const double* __restrict__ c, const double* __restrict__ dz2,
-           const double* __restrict__ dz2rho, TF* __restrict__ pk, double* __restrict__ work)
+    __global__ void k_tdma_table(int niu, int nju, int ktot, const double* __restrict__ bmati,
+                                 const double* __restrict__ bmatj, const double* __restrict__ a,
+                                 const double* __restrict__ c, const double* __restrict__ dz2rho,
+                                 double* __restrict__ rtab)
     {
-        const int i = blockIdx.x*blockDim.x + threadIdx.x;
-        const int j = blockIdx.y;
-        if (i >= itot) return;
-        const long long ij = i + (long long)j*itot;
-        const long long kk = (long long)itot*jtot;
-        const double lam = bmati[i] + bmatj[j];
-        const bool mean_mode = (i == 0 && j == 0);
-        double* wc = work;
-        double* wp = work + kk*ktot;
-
+        const int iu = blockIdx.x*blockDim.x + threadIdx.x;
+        const int ju = blockIdx.y;
+        if (iu >= niu) return;
+        const long long stride = (long long)niu*nju;
+        const long long base = iu + (long long)ju*niu;
+        const double lam = bmati[iu] + bmatj[ju];
+        const bool mean_mode = (iu == 0 && ju == 0);
         double b = dz2rho[0]*lam - (a[0] + c[0]);
         b += a[0];
         if (ktot == 1) b += mean_mode ? -c[0] : c[0];
         double den = b;
-        double pprev = (dz2[0]*double(pk[ij])) / den;
-        wp[ij] = pprev;
+        rtab[base] = 1.0/den;
         for (int k=1; k<ktot; ++k)
         {
             double bk = dz2rho[k]*lam - (a[k] + c[k]);
             if (k == ktot-1) bk += mean_mode ? -c[k] : c[k];
-            const double w3 = c[k-1] / den;
+            const double w3 = c[k-1]/den;
             den = bk - a[k]*w3;
-            double pkk = dz2[k]*double(pk[ij + k*kk]);
-            pkk -= a[k]*pprev;
-            pkk /= den;
-            wc[ij + k*kk] = w3;
-            wp[ij + k*kk] = pkk;
-            pprev = pkk;
+            rtab[base + k*stride] = 1.0/den;
         }
-        double x = pprev;
-        pk[ij + (ktot-1)*kk] = TF(x);
+    }
+
+    template<typename TF>
+    __global__ void __launch_bounds__(128)
+    k_tdma(int itot, int jtot, int ktot, int niu, int nju, const double* __restrict__ rtab,
+           const double* __restrict__ a, const double* __restrict__ c, const double* __restrict__ dz2,
+           TF* __restrict__ pk, double* __restrict__ work)
+    {
+        const int iu = blockIdx.x*blockDim.x + threadIdx.x;
+        const int ju = blockIdx.y;
+        if (iu >= niu) return;
+        const long long stride = (long long)niu*nju;
+        const long long base = iu + (long long)ju*niu;
+        const long long kk = (long long)itot*jtot;
+        const int i1 = (iu == 0 || 2*iu == itot) ? -1 : itot - iu;
+        const int j1 = (ju == 0 || 2*ju == jtot) ? -1 : jtot - ju;
+        long long col[4];
+        int nc = 0;
+        col[nc++] = iu + (long long)ju*itot;
+        if (i1 >= 0) col[nc++] = i1 + (long long)ju*itot;
+        if (j1 >= 0) col[nc++] = iu + (long long)j1*itot;
+        if (i1 >= 0 && j1 >= 0) col[nc++] = i1 + (long long)j1*itot;
+
+        // Forward sweep: y_k = (dz2_k p_k - a_k y_{k-1}) / den_k.
+        double y[4] = {0., 0., 0., 0.};
+        for (int k=0; k<ktot; ++k)
+        {
+            const double r = __ldg(&rtab[base + k*stride]);
+            const double dr = dz2[k]*r;
+            const double ar = k ? a[k]*r : 0.;
+            #pragma unroll
+            for (int q=0; q<4; ++q)
+            {
+                if (q < nc)
+                {
+                    const long long idx = col[q] + k*kk;
+                    y[q] = double(pk[idx])*dr - ar*y[q];
+                    work[idx] = y[q];
+                }
+            }
+        }
+        // Back substitution: x_k = y_k - c_k/den_k x_{k+1}.
+        #pragma unroll
+        for (int q=0; q<4; ++q)
+            if (q < nc) pk[col[q] + (ktot-1)*kk] = TF(y[q]);
         for (int k=ktot-2; k>=0; --k)
         {
-            x = wp[ij + k*kk] - wc[ij + (k+1)*kk]*x;
-            pk[ij + k*kk] = TF(x);
+            const double w3 = c[k]*__ldg(&rtab[base + k*stride]);
+            #pragma unroll
+            for (int q=0; q<4; ++q)
+            {
+                if (q < nc)
+                {
+                    const long long idx = col[q] + k*kk;
+                    y[q] = work[idx] - w3*y[q];
+                    pk[idx] = TF(y[q]);
+                }
+            }
         }
+    }
+
+    int tdma_table(PresWork& pw, int itot, int jtot, int ktot)
+    {
+        pw.niu = itot/2 + 1;
+        pw.nju = jtot/2 + 1;
+        const size_t n = (size_t)pw.niu*pw.nju*ktot;
+        if (cudaMalloc(&pw.rtab, sizeof(double)*n) != cudaSuccess) return MHH_ERR_CUDA;
+        dim3 grid((pw.niu + 127)/128, pw.nju);
+        k_tdma_table<<<grid, 128>>>(pw.niu, pw.nju, ktot, pw.bmati, pw.bmatj, pw.a, pw.c, pw.dz2rho, pw.rtab);
+        count_launch();
+        return cudaDeviceSynchronize() == cudaSuccess ? MHH_OK : MHH_ERR_CUDA;
     }
 
     template<typename TF>
     void launch_tdma(const Dims& d, const PresWork& pw, TF* pk, cudaStream_t s)
     {
-        dim3 grid((d.itot + 127)/128, d.jtot);
-        k_tdma<TF><<<grid, 128, 0, s>>>(d.itot, d.jtot, d.ktot, pw.bmati, pw.bmatj, pw.a, pw.c, pw.dz2, pw.dz2rho, pk, pw.work);
+        dim3 grid((pw.niu + 127)/128, pw.nju);
+        k_tdma<TF><<<grid, 128, 0, s>>>(d.itot, d.jtot, d.ktot, pw.niu, pw.nju, pw.rtab, pw.a, pw.c, pw.dz2, pk, pw.work);
         count_launch();
     }
 

@@ -80,6 +80,36 @@ namespace mhh
         dutot[ij] = fmax(pow(du2, 0.5), 1.e-1);
     }
 
+    // The Monin-Obukhov functions of one cell, each evaluated once: the
+    // similarity function phi of the stability branch feeds both the
+    // integrated psi and the gradient (include/monin_obukhov.h:40-152).
+    struct MostCell { double fm, fh, phim, phih; };
+
+    __device__ __forceinline__ MostCell most_cell(double zsl, double z0m, double z0h, double L)
+    {
+        MostCell r;
+        const double zeta = zsl/L;
+        if (L <= 0.)
+        {
+            const double pm_s = phim_unstable(zeta), pm_0 = phim_unstable(z0m/L);
+            const double ph_s = phih_unstable(zeta), ph_0 = phih_unstable(z0h/L);
+            const double psim_s = 3.*log((1. + 1./pm_s)/2.), psim_0 = 3.*log((1. + 1./pm_0)/2.);
+            const double psih_s = 3.*log((1. + 1./ph_s)/2.), psih_0 = 3.*log((1. + 1./ph_0)/2.);
+            r.fm = KAPPA/(log(zsl/z0m) - psim_s + psim_0);
+            r.fh = KAPPA/(log(zsl/z0h) - psih_s + psih_0);
+            r.phim = zeta <= 0. ? pm_s : 1. + 5.*zeta;
+            r.phih = zeta <= 0. ? ph_s : (1. + 4.*zeta)*(1. + 4.*zeta);
+        }
+        else
+        {
+            r.fm = KAPPA/(log(zsl/z0m) - psim_stable(zeta) + psim_stable(z0m/L));
+            r.fh = KAPPA/(log(zsl/z0h) - psih_stable(zeta) + psih_stable(z0h/L));
+            r.phim = phim(zeta);
+            r.phih = phih(zeta);
+        }
+        return r;
+    }
+
     // Obukhov length and friction velocity, src/boundary_surface.cxx:55-160
     // (all cells; the neutral branch when there is no thermodynamics).
     template<typename TF>
@@ -108,8 +138,12 @@ namespace mhh
             const float Ri = (float)(KAPPA*db*zsl/(du*du));
             L = zsl/find_zL(sw.zL, sw.f, &sw.nobuk[n], Ri);
         }
+        // zsl/L and z0/L of a large |L| can reach zero; the branch choice
+        // follows the sign of L exactly as the separate functions do.
+        const MostCell mc = most_cell(zsl, z0m, sw.z0h, L);
         sw.obuk[n] = L;
-        sw.ustar[n] = du*most_fm(zsl, z0m, L);
+        sw.ustar[n] = du*mc.fm;
+        sw.fm[n] = mc.fm; sw.fh[n] = mc.fh; sw.phim[n] = mc.phim; sw.phih[n] = mc.phih;
     }
 
     // Momentum fluxes, src/boundary_surface.cxx:163-190 (interior).
@@ -124,9 +158,9 @@ namespace mhh
         const long long ii = 1, jj = d.icells;
         const long long ij = i + j*jj;
         const long long c = ij + (long long)d.kstart*d.ijcells;
-        const double fc = sw.ustar[ij]*most_fm(zsl, z0m, sw.obuk[ij]);
-        uflux[ij] = TF(-(double(u[c]) - double(ubot[ij]))*0.5*(sw.ustar[ij-ii]*most_fm(zsl, z0m, sw.obuk[ij-ii]) + fc));
-        vflux[ij] = TF(-(double(v[c]) - double(vbot[ij]))*0.5*(sw.ustar[ij-jj]*most_fm(zsl, z0m, sw.obuk[ij-jj]) + fc));
+        const double fc = sw.ustar[ij]*sw.fm[ij];
+        uflux[ij] = TF(-(double(u[c]) - double(ubot[ij]))*0.5*(sw.ustar[ij-ii]*sw.fm[ij-ii] + fc));
+        vflux[ij] = TF(-(double(v[c]) - double(vbot[ij]))*0.5*(sw.ustar[ij-jj]*sw.fm[ij-jj] + fc));
     }
 
     // Surface gradients of u and v and the scalar surface value, gradient or
@@ -148,12 +182,12 @@ namespace mhh
             const double th = double(s[c]);
             if (thermo_bc == MHH_BC_DIRICHLET)
             {
-                sflux[n] = TF(-(th - double(sbot[n]))*sw.ustar[n]*most_fh(zsl, z0h, sw.obuk[n]));
+                sflux[n] = TF(-(th - double(sbot[n]))*sw.ustar[n]*sw.fh[n]);
                 sgrad[n] = TF((th - double(sbot[n]))/zsl);
             }
             else
             {
-                const double bot = double(sflux[n])/(sw.ustar[n]*most_fh(zsl, z0h, sw.obuk[n])) + th;
+                const double bot = double(sflux[n])/(sw.ustar[n]*sw.fh[n]) + th;
                 sbot[n] = TF(bot);
                 sgrad[n] = TF((th - bot)/zsl);
             }
@@ -174,17 +208,17 @@ namespace mhh
         const long long c = ij + (long long)d.kstart*d.ijcells;
         const double du_c = 0.5*((double(u[c]) - double(ubot[ij])) + (double(u[c+ii]) - double(ubot[ij+ii])));
         const double dv_c = 0.5*((double(v[c]) - double(vbot[ij])) + (double(v[c+jj]) - double(vbot[ij+jj])));
-        const double us = sw.ustar[ij], L = sw.obuk[ij];
-        const double fmv = most_fm(zsl, z0m, L);
+        const double us = sw.ustar[ij];
+        const double fmv = sw.fm[ij];
         const double ufb = -du_c*us*fmv;
         const double vfb = -dv_c*us*fmv;
-        const double ph = phim(zsl/L);
+        const double ph = sw.phim[ij];
         sw.dudz[ij] = -ufb/(KAPPA*zsl*us)*ph;
         sw.dvdz[ij] = -vfb/(KAPPA*zsl*us)*ph;
         if (thermo)
         {
             const double bfb = GRAV/threfh_s*double(sflux[ij]);
-            sw.dbdz[ij] = -bfb/(KAPPA*zsl*us)*phih(zsl/L);
+            sw.dbdz[ij] = -bfb/(KAPPA*zsl*us)*sw.phih[ij];
         }
     }
 
