@@ -48,6 +48,8 @@ namespace mhh
                                                 double visc, int mason, bool surf, bool thermo, cudaStream_t s);
     template<typename TF> void launch_tendency(const Dims& d, const Prof<TF>& pr, const TendArgs<TF>& a, int adv, int dif,
                                                bool surf, bool scal, bool buoy, bool force, cudaStream_t s);
+    template<typename TF> void launch_tendency_les(const Dims& d, const Prof<TF>& pr, const TendArgs<TF>& a,
+                                                   bool surf, bool scal, bool buoy, cudaStream_t s);
     template<typename TF> void launch_rk3(TF* a, TF* at, const Dims& d, int substep, double dt, cudaStream_t s);
     template<typename TF> void launch_presout_rk3(const Dims& d, const Prof<TF>& pr, const TF* p, TF* u, TF* v, TF* w,
                                                   TF* s, TF* ut, TF* vt, TF* wt, TF* st, int substep, double dt,
