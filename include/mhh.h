@@ -118,6 +118,11 @@ const char* mhh_last_error(void);
 /* Kernels this library launched since load (for launch accounting). */
 long long mhh_launch_count(void);
 
+/* Process-wide kernel options (no counterpart in the reference; the
+   reference picks kernel variants through its Kernel Launcher wisdom files):
+   "tendency_kernel" 0 = one thread per cell, 1 = tiled planes marching in k. */
+int mhh_set_option(const char* name, int value);
+
 /* Live per-kernel-group timing with CUDA events recorded on the launching
    stream (no counterpart in the reference, which has no event timing):
    enable, run, then collect (waits for the recorded events) and read the

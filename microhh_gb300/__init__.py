@@ -94,6 +94,7 @@ def load():
     # C-ABI of the kernels (include/mhh.h)
     _declare(kern, "mhh_last_error", ctypes.c_char_p, [])
     _declare(kern, "mhh_launch_count", ctypes.c_longlong, [])
+    _declare(kern, "mhh_set_option", I, [ctypes.c_char_p, I])
     _declare(kern, "mhh_timing_enable", I, [I])
     _declare(kern, "mhh_timing_reset", I, [])
     _declare(kern, "mhh_timing_collect", I, [])
@@ -157,6 +158,12 @@ def check(rc, what="mhh"):
         kern, host = load()
         msg = host.mhh_model_last_error() or kern.mhh_last_error() or b""
         raise MhhError(f"{what} failed ({rc}): {msg.decode(errors='replace')}")
+
+
+def set_option(name, value):
+    """Process-wide kernel option of the native library (include/mhh.h)."""
+    kern, _ = load()
+    check(kern.mhh_set_option(name.encode(), int(value)), f"option {name}")
 
 
 def launch_count():

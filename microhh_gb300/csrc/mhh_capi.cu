@@ -65,6 +65,9 @@ void mhh_set_last_error(const char* msg) { g_last_error = msg ? msg : ""; }
 namespace mhh
 {
     void count_launch(int n) { g_launches += n; }
+    static int g_tend_variant = 0;
+    int tendency_variant() { return g_tend_variant; }
+    void set_tendency_variant(int v) { g_tend_variant = v; }
     long long launch_count() { return g_launches.load(); }
 
     template<typename TF>
@@ -480,6 +483,18 @@ namespace
 extern "C" {
 
 const char* mhh_last_error(void) { return g_last_error.c_str(); }
+
+int mhh_set_option(const char* name, int value)
+{
+    if (!name) return fail(MHH_ERR_ARG, "NULL option");
+    if (!std::strcmp(name, "tendency_kernel"))
+    {
+        if (value < 0 || value > 1) return fail(MHH_ERR_ARG, "tendency_kernel is 0 or 1");
+        set_tendency_variant(value);
+        return MHH_OK;
+    }
+    return fail(MHH_ERR_ARG, "unknown option");
+}
 
 int mhh_timing_enable(int on)
 {

@@ -7,6 +7,10 @@ namespace mhh
 {
     void count_launch(int n = 1);
     long long launch_count();
+    // Kernel variant of the LES tendencies: 0 = one thread per cell with
+    // cached global loads, 1 = tiled shared-memory planes marching in k.
+    int tendency_variant();
+    void set_tendency_variant(int v);
 
     template<typename TF>
     struct FieldList

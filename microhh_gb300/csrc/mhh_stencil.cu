@@ -364,8 +364,8 @@ namespace mhh
     void launch_tendency(const Dims& d, const Prof<TF>& pr, const TendArgs<TF>& a, int adv, int dif,
                          bool surf, bool scal, bool buoy, bool force, cudaStream_t s)
     {
-        // The LES combination runs in the tiled kernel (mhh_tend_tiled.cu).
-        if (adv == MHH_ADVEC_2I5 && dif == MHH_DIFF_SMAG2 && !force && d.igc >= 3 && d.jgc >= 3)
+        // The LES combination can run in the tiled kernel (mhh_tend_tiled.cu).
+        if (tendency_variant() == 1 && adv == MHH_ADVEC_2I5 && dif == MHH_DIFF_SMAG2 && !force && d.igc >= 3 && d.jgc >= 3)
         {
             launch_tendency_les<TF>(d, pr, a, surf, scal, buoy, s);
             return;
