@@ -120,7 +120,12 @@ long long mhh_launch_count(void);
 
 /* Process-wide kernel options (no counterpart in the reference; the
    reference picks kernel variants through its Kernel Launcher wisdom files):
-   "tendency_kernel" 0 = one thread per cell, 1 = tiled planes marching in k. */
+   "tendency_kernel" 0 = one thread per cell, 1 = tiled planes marching in k,
+   2 = flux form (each face flux computed once) marching in k, -1 = automatic
+   (2 for FP32 contexts, 0 for FP64 contexts; the default);
+   "tdma_kernel" 0 = the Thomas recurrence in the reference's operation order,
+   1 = the rescaled recurrence (two FP64 FMAs per cell), -1 = automatic
+   (0 for FP64 contexts, 1 for FP32 contexts; the default). */
 int mhh_set_option(const char* name, int value);
 
 /* Live per-kernel-group timing with CUDA events recorded on the launching

@@ -65,9 +65,12 @@ void mhh_set_last_error(const char* msg) { g_last_error = msg ? msg : ""; }
 namespace mhh
 {
     void count_launch(int n) { g_launches += n; }
-    static int g_tend_variant = 0;
+    static int g_tend_variant = -1;
     int tendency_variant() { return g_tend_variant; }
     void set_tendency_variant(int v) { g_tend_variant = v; }
+    static int g_tdma_variant = -1;
+    int tdma_variant() { return g_tdma_variant; }
+    void set_tdma_variant(int v) { g_tdma_variant = v; }
     long long launch_count() { return g_launches.load(); }
 
     template<typename TF>
@@ -80,8 +83,8 @@ namespace mhh
         if (i >= d.iend || j >= d.jend) return;
         const long long c = ijk(d, i, j, k);
         const TF pc = ld(p, c);
-        ut[c] -= (pc - ld(p, c-1))*TF(d.dxi);
-        vt[c] -= (pc - ld(p, c-d.icells))*TF(d.dyi);
+        ut[c] -= (pc - ld(p, c-1))*dxi_of<TF>(d);
+        vt[c] -= (pc - ld(p, c-d.icells))*dyi_of<TF>(d);
         wt[c] -= (pc - ld(p, c-d.ijcells))*ld(pr.dzhi, k);
     }
 }
@@ -96,8 +99,8 @@ struct mhh_ctx
     mhh_physics phys;
 
     // Host profiles (double), device profiles (one precision).
-    std::vector<double> h[10];
-    void* dprof[10];
+    std::vector<double> h[12];
+    void* dprof[12];
     Prof<double> pd;
     Prof<float> pf;
 
@@ -112,8 +115,9 @@ struct mhh_ctx
 
 namespace
 {
-    enum { P_Z, P_ZH, P_DZ, P_DZH, P_DZI, P_DZHI, P_RHO, P_RHOH, P_TH, P_THH };
-    const char* prof_names[10] = {"z", "zh", "dz", "dzh", "dzi", "dzhi", "rhoref", "rhorefh", "thref", "threfh"};
+    enum { P_Z, P_ZH, P_DZ, P_DZH, P_DZI, P_DZHI, P_RHO, P_RHOH, P_TH, P_THH, P_ZF, P_ZFH };
+    const char* prof_names[12] = {"z", "zh", "dz", "dzh", "dzi", "dzhi", "rhoref", "rhorefh", "thref", "threfh",
+                                  "zfac", "zfach"};
 
     int fail(int code, const char* msg) { mhh_set_last_error(msg); return code; }
 
@@ -158,6 +162,12 @@ namespace
             c->h[P_RHO][k] = 1.; c->h[P_RHOH][k] = 1.;
             c->h[P_TH][k] = c->phys.thref0; c->h[P_THH][k] = c->phys.thref0;
         }
+        // Vertical flux-divergence factors of the flux-form tendency kernel.
+        for (int k=0; k<kc; ++k)
+        {
+            c->h[P_ZF][k] = dzi[k]/c->h[P_RHO][k];
+            c->h[P_ZFH][k] = dzhi[k]/c->h[P_RHOH][k];
+        }
     }
 
     // Squared Smagorinsky mixing length per level: src/diff_smag2.cxx:176-180
@@ -188,7 +198,7 @@ namespace
     {
         const int kc = c->d.kcells;
         std::vector<TF> tmp(kc);
-        for (int q=0; q<10; ++q)
+        for (int q=0; q<12; ++q)
         {
             if (cudaMalloc(&c->dprof[q], sizeof(TF)*kc) != cudaSuccess) return fail(MHH_ERR_CUDA, "cudaMalloc profiles");
             for (int k=0; k<kc; ++k) tmp[k] = TF(c->h[q][k]);
@@ -200,6 +210,7 @@ namespace
         p.dzi = (const TF*)c->dprof[P_DZI]; p.dzhi = (const TF*)c->dprof[P_DZHI];
         p.rhoref = (const TF*)c->dprof[P_RHO]; p.rhorefh = (const TF*)c->dprof[P_RHOH];
         p.thref = (const TF*)c->dprof[P_TH]; p.threfh = (const TF*)c->dprof[P_THH];
+        p.zfac = (const TF*)c->dprof[P_ZF]; p.zfach = (const TF*)c->dprof[P_ZFH];
         if constexpr (sizeof(TF) == 8) c->pd = *reinterpret_cast<Prof<double>*>(&p);
         else c->pf = *reinterpret_cast<Prof<float>*>(&p);
         return MHH_OK;
@@ -336,6 +347,8 @@ namespace
         }
         a.visc = TF(c->phys.visc); a.svisc = TF(c->phys.svisc);
         a.tpri = TF(1)/TF(c->phys.tpr);
+        a.dxidxi_t = TF(1./(c->d.dx*c->d.dx));
+        a.dyidyi_t = TF(1./(c->d.dy*c->d.dy));
         a.fbody = TF(0);
         a.dxidxi = 1./(c->d.dx*c->d.dx);
         a.dyidyi = 1./(c->d.dy*c->d.dy);
@@ -385,8 +398,9 @@ namespace
         const bool surf = c->phys.surface != 0, thermo = c->phys.thermo != 0 && f->s;
         if (surf && !c->surf_ready) return fail(MHH_ERR_ARG, "surface layer not initialised");
         Timed t("viscosity", s);
+        const TF* ml2 = sizeof(TF) == 8 ? reinterpret_cast<const TF*>(c->sw.mlen2) : reinterpret_cast<const TF*>(c->sw.mlen2f);
         launch_viscosity<TF>(c->d, prof<TF>(c), CT<TF>(f->u), CT<TF>(f->v), CT<TF>(f->w), CT<TF>(f->s), T<TF>(f->evisc),
-                             c->sw.mlen2, c->sw.dudz, c->sw.dvdz, c->sw.dbdz, c->phys.cs, c->phys.tpr, c->phys.visc,
+                             ml2, c->sw.dudz, c->sw.dvdz, c->sw.dbdz, c->phys.cs, c->phys.tpr, c->phys.visc,
                              c->phys.swmason, surf, thermo, s);
         return check_cuda("viscosity");
     }
@@ -489,8 +503,14 @@ int mhh_set_option(const char* name, int value)
     if (!name) return fail(MHH_ERR_ARG, "NULL option");
     if (!std::strcmp(name, "tendency_kernel"))
     {
-        if (value < 0 || value > 1) return fail(MHH_ERR_ARG, "tendency_kernel is 0 or 1");
+        if (value < -1 || value > 2) return fail(MHH_ERR_ARG, "tendency_kernel is -1, 0, 1 or 2");
         set_tendency_variant(value);
+        return MHH_OK;
+    }
+    if (!std::strcmp(name, "tdma_kernel"))
+    {
+        if (value < -1 || value > 1) return fail(MHH_ERR_ARG, "tdma_kernel is -1, 0 or 1");
+        set_tdma_variant(value);
         return MHH_OK;
     }
     return fail(MHH_ERR_ARG, "unknown option");
@@ -549,6 +569,8 @@ int mhh_ctx_create(const mhh_grid_desc* desc, const double* z, int precision, co
         return fail(MHH_ERR_ARG, "the 5th-order scheme needs ktot >= 6");
     const double ncells = double(desc->itot + 2*desc->igc)*(desc->jtot + 2*desc->jgc)*(desc->ktot + 2);
     if (ncells > 4.0e9) return fail(MHH_ERR_ARG, "grid too large for 32-bit plane indexing");
+    if (double(desc->itot + 2*desc->igc)*(desc->jtot + 2*desc->jgc) > 2.0e9)
+        return fail(MHH_ERR_ARG, "horizontal plane too large for 32-bit indexing");
 
     mhh_ctx* c = new mhh_ctx();
     std::memset(c->dprof, 0, sizeof(c->dprof));
@@ -567,6 +589,7 @@ int mhh_ctx_create(const mhh_grid_desc* desc, const double* z, int precision, co
     d.kstart = d.kgc; d.kend = d.ktot + d.kgc;
     d.dx = desc->xsize / d.itot; d.dy = desc->ysize / d.jtot;
     d.dxi = 1./d.dx; d.dyi = 1./d.dy;
+    d.fdxi = float(d.dxi); d.fdyi = float(d.dyi); d.fzsize = float(desc->zsize);
     d.zsize = desc->zsize;
 
     mhh_grid& g = c->g;
@@ -598,6 +621,13 @@ int mhh_ctx_create(const mhh_grid_desc* desc, const double* z, int precision, co
     if (!rc) rc = dalloc(&c->sw.f, NZL_LUT);
     if (!rc) rc = dalloc(&c->sw.mlen2, d.kcells);
     if (!rc) rc = upload(c->sw.mlen2, mixing_length2(c));
+    if (!rc)
+    {
+        const std::vector<double> m2 = mixing_length2(c);
+        std::vector<float> m2f(m2.begin(), m2.end());
+        rc = dalloc(&c->sw.mlen2f, m2f.size());
+        if (!rc) cudaMemcpy(c->sw.mlen2f, m2f.data(), sizeof(float)*m2f.size(), cudaMemcpyHostToDevice);
+    }
     c->sw.zsl = c->h[P_Z][d.kstart];
     c->sw.thref_s = c->h[P_TH][d.kstart];
     c->sw.threfh_s = c->h[P_THH][d.kstart];
@@ -623,9 +653,9 @@ int mhh_ctx_destroy(mhh_ctx* c)
     if (!c) return MHH_OK;
     for (auto& p : c->dprof) if (p) cudaFree(p);
     fft_plan_free(&c->pw.px); fft_plan_free(&c->pw.py);
-    void* ptrs[] = {c->pw.pk, c->pw.work, c->pw.rtab, c->pw.bmati, c->pw.bmatj, c->pw.a, c->pw.c, c->pw.dz2, c->pw.dz2rho,
+    void* ptrs[] = {c->pw.pk, c->pw.work, c->pw.rtab, c->pw.gtab, c->pw.htab, c->pw.stab, c->pw.stabd, c->pw.bmati, c->pw.bmatj, c->pw.a, c->pw.c, c->pw.dz2, c->pw.dz2rho,
                     c->red, c->sw.fm, c->sw.fh, c->sw.phim, c->sw.phih, c->sw.ustar, c->sw.obuk, c->sw.dudz, c->sw.dvdz, c->sw.dbdz, c->sw.dutot,
-                    c->sw.nobuk, c->sw.zL, c->sw.f, c->sw.mlen2};
+                    c->sw.nobuk, c->sw.zL, c->sw.f, c->sw.mlen2, c->sw.mlen2f};
     for (void* p : ptrs) if (p) cudaFree(p);
     if (c->red_host) cudaFreeHost(c->red_host);
     delete c;

@@ -17,7 +17,19 @@ namespace mhh
         int istart, iend, jstart, jend, kstart, kend;
         long long ncells;
         double dx, dy, dxi, dyi, zsize;
+        float fdxi, fdyi, fzsize;   // the same in float, so float kernels convert nothing
     };
+
+    // 1/dx, 1/dy and zsize in the kernel's precision.
+    template<typename TF> __device__ __forceinline__ TF dxi_of(const Dims& d);
+    template<> __device__ __forceinline__ double dxi_of<double>(const Dims& d) { return d.dxi; }
+    template<> __device__ __forceinline__ float dxi_of<float>(const Dims& d) { return d.fdxi; }
+    template<typename TF> __device__ __forceinline__ TF dyi_of(const Dims& d);
+    template<> __device__ __forceinline__ double dyi_of<double>(const Dims& d) { return d.dyi; }
+    template<> __device__ __forceinline__ float dyi_of<float>(const Dims& d) { return d.fdyi; }
+    template<typename TF> __device__ __forceinline__ TF zsize_of(const Dims& d);
+    template<> __device__ __forceinline__ double zsize_of<double>(const Dims& d) { return d.zsize; }
+    template<> __device__ __forceinline__ float zsize_of<float>(const Dims& d) { return d.fzsize; }
 
     // Vertical profiles of one precision (device pointers, kcells each).
     template<typename TF>
@@ -26,6 +38,7 @@ namespace mhh
         const TF *z, *zh, *dz, *dzh, *dzi, *dzhi;
         const TF *rhoref, *rhorefh;
         const TF *thref, *threfh;
+        const TF *zfac, *zfach;     // dzi/rhoref and dzhi/rhorefh
     };
 
     __host__ __device__ inline long long ijk(const Dims& d, int i, int j, int k)

@@ -8,7 +8,9 @@ namespace mhh
     void count_launch(int n = 1);
     long long launch_count();
     // Kernel variant of the LES tendencies: 0 = one thread per cell with
-    // cached global loads, 1 = tiled shared-memory planes marching in k.
+    // cached global loads, 1 = tiled shared-memory planes marching in k,
+    // 2 = flux form (every face flux once) marching in k; -1 = automatic
+    // (2 for float fields, 0 for double fields; the default).
     int tendency_variant();
     void set_tendency_variant(int v);
 
@@ -39,6 +41,7 @@ namespace mhh
         const TF *u_fluxbot, *u_fluxtop, *v_fluxbot, *v_fluxtop, *s_fluxbot, *s_fluxtop;
         TF visc, svisc, tpri, fbody;
         double dxidxi, dyidyi;
+        TF dxidxi_t, dyidyi_t;
     };
 
     template<typename TF> void launch_cyclic(const FieldList<TF>& fl, const Dims& d, int edges, cudaStream_t s);
@@ -47,13 +50,15 @@ namespace mhh
                                              int sfg, const Dims& d, cudaStream_t s);
     template<typename TF> void launch_ghost(const GhostList<TF>& gl, const Dims& d, const TF* dzh, cudaStream_t s);
     template<typename TF> void launch_viscosity(const Dims& d, const Prof<TF>& pr, const TF* u, const TF* v, const TF* w,
-                                                const TF* th, TF* evisc, const double* mlen2, const double* dudz,
+                                                const TF* th, TF* evisc, const TF* mlen2, const double* dudz,
                                                 const double* dvdz, const double* dbdz, double cs, double tpr,
                                                 double visc, int mason, bool surf, bool thermo, cudaStream_t s);
     template<typename TF> void launch_tendency(const Dims& d, const Prof<TF>& pr, const TendArgs<TF>& a, int adv, int dif,
                                                bool surf, bool scal, bool buoy, bool force, cudaStream_t s);
     template<typename TF> void launch_tendency_les(const Dims& d, const Prof<TF>& pr, const TendArgs<TF>& a,
                                                    bool surf, bool scal, bool buoy, cudaStream_t s);
+    template<typename TF> void launch_tendency_flux(const Dims& d, const Prof<TF>& pr, const TendArgs<TF>& a,
+                                                    bool surf, bool scal, bool buoy, cudaStream_t s);
     template<typename TF> void launch_rk3(TF* a, TF* at, const Dims& d, int substep, double dt, cudaStream_t s);
     template<typename TF> void launch_presout_rk3(const Dims& d, const Prof<TF>& pr, const TF* p, TF* u, TF* v, TF* w,
                                                   TF* s, TF* ut, TF* vt, TF* wt, TF* st, int substep, double dt,
@@ -87,8 +92,18 @@ namespace mhh
         double* dz2rho;       // ktot: dz^2 * rhoref
         double* work;         // itot*jtot*ktot doubles: forward-swept right-hand side
         double* rtab;         // (itot/2+1)*(jtot/2+1)*ktot: 1/den per column group and level
+        double* gtab;         // same shape: forward coefficient of the rescaled recurrence
+        double* htab;         // same shape: backward coefficient of the rescaled recurrence
+        float* stab;          // same shape: output scale dz^2/den in float
+        double* stabd;        // same shape: output scale dz^2/den
         int niu, nju;
     };
+
+    // Tridiagonal kernel choice: 0 = the reference's operation order,
+    // 1 = the rescaled recurrence (two FP64 FMAs per cell); -1 = automatic
+    // (0 for double fields, 1 for float fields).
+    int tdma_variant();
+    void set_tdma_variant(int v);
 
     int tdma_table(PresWork& pw, int itot, int jtot, int ktot);
 
@@ -109,6 +124,7 @@ namespace mhh
         int* nobuk;
         float *zL, *f;
         double *mlen2;   // kcells: squared Smagorinsky mixing length per level
+        float *mlen2f;   // the same in float
         double zsl;      // height of the first full level
         double thref_s, threfh_s;  // reference potential temperature at kstart (full, half)
     };

@@ -531,8 +531,8 @@ namespace mhh
         const int kg = k + d.kgc;
         const TF rho = ld(pr.rhoref, kg);
         pk[i + (long long)j*d.itot + (long long)k*d.itot*d.jtot] =
-              rho*((ld(ut, c+ii) + ld(u, c+ii)*dti) - (ld(ut, c) + ld(u, c)*dti))*TF(d.dxi)
-            + rho*((ld(vt, c+jj) + ld(v, c+jj)*dti) - (ld(vt, c) + ld(v, c)*dti))*TF(d.dyi)
+              rho*((ld(ut, c+ii) + ld(u, c+ii)*dti) - (ld(ut, c) + ld(u, c)*dti))*dxi_of<TF>(d)
+            + rho*((ld(vt, c+jj) + ld(v, c+jj)*dti) - (ld(vt, c) + ld(v, c)*dti))*dyi_of<TF>(d)
             + (ld(pr.rhorefh, kg+1)*(ld(wt, c+kk) + ld(w, c+kk)*dti)
              - ld(pr.rhorefh, kg  )*(ld(wt, c   ) + ld(w, c   )*dti))*ld(pr.dzi, kg);
     }
@@ -563,7 +563,9 @@ namespace mhh
     __global__ void k_tdma_table(int niu, int nju, int ktot, const double* __restrict__ bmati,
                                  const double* __restrict__ bmatj, const double* __restrict__ a,
                                  const double* __restrict__ c, const double* __restrict__ dz2rho,
-                                 double* __restrict__ rtab)
+                                 const double* __restrict__ dz2, double* __restrict__ rtab,
+                                 double* __restrict__ gtab, double* __restrict__ htab,
+                                 float* __restrict__ stab, double* __restrict__ stabd)
     {
         const int iu = blockIdx.x*blockDim.x + threadIdx.x;
         const int ju = blockIdx.y;
@@ -585,7 +587,28 @@ namespace mhh
             den = bk - a[k]*w3;
             rtab[base + k*stride] = 1.0/den;
         }
+        // Rescaled recurrence: with s_k = dz2_k/den_k, y_k = s_k z_k and
+        // x_k = s_k xi_k the sweeps become
+        //   z_k = p_k - g_k z_{k-1},      g_k = a_k s_{k-1}/dz2_k,
+        //   xi_k = z_k - h_k xi_{k+1},    h_k = c_k s_{k+1}/dz2_k,
+        // and x_k = s_k xi_k: one FMA per cell and sweep.
+        for (int k=0; k<ktot; ++k)
+        {
+            const double sk = dz2[k]*rtab[base + k*stride];
+            stabd[base + k*stride] = sk;
+            stab[base + k*stride] = float(sk);
+            gtab[base + k*stride] = k ? a[k]*(dz2[k-1]*rtab[base + (k-1)*stride])/dz2[k] : 0.;
+            htab[base + k*stride] = k < ktot-1 ? c[k]*(dz2[k+1]*rtab[base + (k+1)*stride])/dz2[k] : 0.;
+        }
     }
+
+    // The k loops run in batches of levels (TDMA_KF forward, TDMA_KBK
+    // backward, where the batch holds doubles): the loads of a batch do not
+    // depend on the recurrence, so they are issued together and the few
+    // threads of this kernel (one per column group) keep enough bytes in
+    // flight to stream from HBM instead of waiting one level at a time.
+    constexpr int TDMA_KF = 8;
+    constexpr int TDMA_KBK = 4;
 
     template<typename TF>
     __global__ void __launch_bounds__(128)
@@ -601,46 +624,246 @@ namespace mhh
         const long long kk = (long long)itot*jtot;
         const int i1 = (iu == 0 || 2*iu == itot) ? -1 : itot - iu;
         const int j1 = (ju == 0 || 2*ju == jtot) ? -1 : jtot - ju;
-        long long col[4];
-        int nc = 0;
-        col[nc++] = iu + (long long)ju*itot;
-        if (i1 >= 0) col[nc++] = i1 + (long long)ju*itot;
-        if (j1 >= 0) col[nc++] = iu + (long long)j1*itot;
-        if (i1 >= 0 && j1 >= 0) col[nc++] = i1 + (long long)j1*itot;
+        // The group's columns (i, j), (itot-i, j), (i, jtot-j), (itot-i, jtot-j);
+        // a column that coincides with the first is masked out.  Column
+        // offsets within a level are 32-bit (itot*jtot < 2^31 is checked at
+        // set-up); level offsets are 64-bit pointers.
+        const bool use[4] = {true, i1 >= 0, j1 >= 0, i1 >= 0 && j1 >= 0};
+        const int ia = iu, ib = i1 >= 0 ? i1 : iu;
+        const int ja = ju*itot, jb = (j1 >= 0 ? j1 : ju)*itot;
+        const int col[4] = {ia + ja, ib + ja, ia + jb, ib + jb};
 
         // Forward sweep: y_k = (dz2_k p_k - a_k y_{k-1}) / den_k.
         double y[4] = {0., 0., 0., 0.};
-        for (int k=0; k<ktot; ++k)
+        for (int k0=0; k0<ktot; k0+=TDMA_KF)
         {
-            const double r = __ldg(&rtab[base + k*stride]);
-            const double dr = dz2[k]*r;
-            const double ar = k ? a[k]*r : 0.;
+            const int nk = min(TDMA_KF, ktot - k0);
+            double r[TDMA_KF];
+            TF pv[TDMA_KF][4];
             #pragma unroll
-            for (int q=0; q<4; ++q)
+            for (int b=0; b<TDMA_KF; ++b)
             {
-                if (q < nc)
+                if (b < nk)
                 {
-                    const long long idx = col[q] + k*kk;
-                    y[q] = double(pk[idx])*dr - ar*y[q];
-                    work[idx] = y[q];
+                    const long long k = k0 + b;
+                    r[b] = __ldg(&rtab[base + k*stride]);
+                    const TF* row = pk + k*kk;
+                    #pragma unroll
+                    for (int q=0; q<4; ++q)
+                        if (use[q]) pv[b][q] = row[col[q]];
+                }
+            }
+            #pragma unroll
+            for (int b=0; b<TDMA_KF; ++b)
+            {
+                if (b < nk)
+                {
+                    const int k = k0 + b;
+                    const double dr = dz2[k]*r[b];
+                    const double ar = k ? a[k]*r[b] : 0.;
+                    double* wrow = work + (long long)k*kk;
+                    #pragma unroll
+                    for (int q=0; q<4; ++q)
+                    {
+                        if (use[q])
+                        {
+                            y[q] = double(pv[b][q])*dr - ar*y[q];
+                            wrow[col[q]] = y[q];
+                        }
+                    }
                 }
             }
         }
         // Back substitution: x_k = y_k - c_k/den_k x_{k+1}.
-        #pragma unroll
-        for (int q=0; q<4; ++q)
-            if (q < nc) pk[col[q] + (ktot-1)*kk] = TF(y[q]);
-        for (int k=ktot-2; k>=0; --k)
         {
-            const double w3 = c[k]*__ldg(&rtab[base + k*stride]);
+            TF* row = pk + (long long)(ktot-1)*kk;
             #pragma unroll
             for (int q=0; q<4; ++q)
+                if (use[q]) row[col[q]] = TF(y[q]);
+        }
+        for (int k0=ktot-2; k0>=0; k0-=TDMA_KBK)
+        {
+            const int nk = min(TDMA_KBK, k0 + 1);
+            double r[TDMA_KBK];
+            double wv[TDMA_KBK][4];
+            #pragma unroll
+            for (int b=0; b<TDMA_KBK; ++b)
             {
-                if (q < nc)
+                if (b < nk)
                 {
-                    const long long idx = col[q] + k*kk;
-                    y[q] = work[idx] - w3*y[q];
-                    pk[idx] = TF(y[q]);
+                    const long long k = k0 - b;
+                    r[b] = __ldg(&rtab[base + k*stride]);
+                    const double* wrow = work + k*kk;
+                    #pragma unroll
+                    for (int q=0; q<4; ++q)
+                        if (use[q]) wv[b][q] = wrow[col[q]];
+                }
+            }
+            #pragma unroll
+            for (int b=0; b<TDMA_KBK; ++b)
+            {
+                if (b < nk)
+                {
+                    const int k = k0 - b;
+                    const double w3 = c[k]*r[b];
+                    TF* row = pk + (long long)k*kk;
+                    #pragma unroll
+                    for (int q=0; q<4; ++q)
+                    {
+                        if (use[q])
+                        {
+                            y[q] = wv[b][q] - w3*y[q];
+                            row[col[q]] = TF(y[q]);
+                        }
+                    }
+                }
+            }
+        }
+    }
+
+    // Exact float <-> double conversions on the integer pipe (IEEE 754
+    // binary32/binary64 layouts): the FP64 pipe of this GPU is narrow and
+    // its conversions would cost as much as the solve.  Zeros, subnormals,
+    // infinities, NaNs and results outside the normal float range take the
+    // hardware conversion.
+    __device__ __forceinline__ double f2d_exact(float f)
+    {
+        const unsigned u = __float_as_uint(f);
+        const unsigned e = (u >> 23) & 0xffu;
+        if (e == 0u || e == 0xffu)
+            return (u << 1) == 0u ? __hiloint2double(int(u & 0x80000000u), 0) : double(f);
+        const unsigned hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u >> 3) & 0xfffffu);
+        return __hiloint2double(int(hi), int(u << 29));
+    }
+
+    // Round to nearest, ties to even.
+    __device__ __forceinline__ float d2f_rn(double x)
+    {
+        const unsigned hi = unsigned(__double2hiint(x)), lo = unsigned(__double2loint(x));
+        const unsigned e = (hi >> 20) & 0x7ffu;
+        if (e < 897u || e > 1150u) return float(x);
+        const unsigned r = (((hi & 0x7fffffffu) << 3) | (lo >> 29)) - (896u << 23);
+        const unsigned rem = lo & 0x1fffffffu;
+        const unsigned up = (rem > 0x10000000u || (rem == 0x10000000u && (r & 1u))) ? 1u : 0u;
+        return __uint_as_float((hi & 0x80000000u) | (r + up));
+    }
+
+    template<typename TF> __device__ __forceinline__ double to_f64(TF v);
+    template<> __device__ __forceinline__ double to_f64<float>(float v) { return f2d_exact(v); }
+    template<> __device__ __forceinline__ double to_f64<double>(double v) { return v; }
+
+    // Output x_k = s_k xi_k in the field precision: in float the product of
+    // the rounded factors (the result is stored in float anyway).
+    template<typename TF> __device__ __forceinline__ TF scale_out(double xi, float s, double sd);
+    template<> __device__ __forceinline__ float scale_out<float>(double xi, float s, double) { return d2f_rn(xi)*s; }
+    template<> __device__ __forceinline__ double scale_out<double>(double xi, float, double sd) { return xi*sd; }
+
+    // The Thomas solve with the rescaled recurrence (coefficients from
+    // k_tdma_table): in the float form the whole solve costs two FP64 FMAs
+    // per cell, the elimination itself staying in double.
+    template<typename TF>
+    __global__ void __launch_bounds__(128)
+    k_tdma_scaled(int itot, int jtot, int ktot, int niu, int nju, const double* __restrict__ gtab,
+                  const double* __restrict__ htab, const float* __restrict__ stab, const double* __restrict__ stabd,
+                  TF* __restrict__ pk, double* __restrict__ work)
+    {
+        const int iu = blockIdx.x*blockDim.x + threadIdx.x;
+        const int ju = blockIdx.y;
+        if (iu >= niu) return;
+        const long long stride = (long long)niu*nju;
+        const long long base = iu + (long long)ju*niu;
+        const long long kk = (long long)itot*jtot;
+        const int i1 = (iu == 0 || 2*iu == itot) ? -1 : itot - iu;
+        const int j1 = (ju == 0 || 2*ju == jtot) ? -1 : jtot - ju;
+        const bool use[4] = {true, i1 >= 0, j1 >= 0, i1 >= 0 && j1 >= 0};
+        const int ia = iu, ib = i1 >= 0 ? i1 : iu;
+        const int ja = ju*itot, jb = (j1 >= 0 ? j1 : ju)*itot;
+        const int col[4] = {ia + ja, ib + ja, ia + jb, ib + jb};
+
+        // Forward: z_k = p_k - g_k z_{k-1}.
+        double z[4] = {0., 0., 0., 0.};
+        for (int k0=0; k0<ktot; k0+=TDMA_KF)
+        {
+            const int nk = min(TDMA_KF, ktot - k0);
+            double g[TDMA_KF];
+            TF pv[TDMA_KF][4];
+            #pragma unroll
+            for (int b=0; b<TDMA_KF; ++b)
+            {
+                if (b < nk)
+                {
+                    const long long k = k0 + b;
+                    g[b] = __ldg(&gtab[base + k*stride]);
+                    const TF* row = pk + k*kk;
+                    #pragma unroll
+                    for (int q=0; q<4; ++q)
+                        if (use[q]) pv[b][q] = row[col[q]];
+                }
+            }
+            #pragma unroll
+            for (int b=0; b<TDMA_KF; ++b)
+            {
+                if (b < nk)
+                {
+                    double* wrow = work + (long long)(k0 + b)*kk;
+                    #pragma unroll
+                    for (int q=0; q<4; ++q)
+                    {
+                        if (use[q])
+                        {
+                            z[q] = fma(-g[b], z[q], to_f64<TF>(pv[b][q]));
+                            wrow[col[q]] = z[q];
+                        }
+                    }
+                }
+            }
+        }
+        // Backward: xi_k = z_k - h_k xi_{k+1}; x_k = s_k xi_k.
+        {
+            const long long k = ktot - 1;
+            const float s = __ldg(&stab[base + k*stride]);
+            const double sd = sizeof(TF) == 8 ? __ldg(&stabd[base + k*stride]) : 0.;
+            TF* row = pk + k*kk;
+            #pragma unroll
+            for (int q=0; q<4; ++q)
+                if (use[q]) row[col[q]] = scale_out<TF>(z[q], s, sd);
+        }
+        for (int k0=ktot-2; k0>=0; k0-=TDMA_KBK)
+        {
+            const int nk = min(TDMA_KBK, k0 + 1);
+            double h[TDMA_KBK], sd[TDMA_KBK];
+            float s[TDMA_KBK];
+            double zv[TDMA_KBK][4];
+            #pragma unroll
+            for (int b=0; b<TDMA_KBK; ++b)
+            {
+                if (b < nk)
+                {
+                    const long long k = k0 - b;
+                    h[b] = __ldg(&htab[base + k*stride]);
+                    s[b] = __ldg(&stab[base + k*stride]);
+                    sd[b] = sizeof(TF) == 8 ? __ldg(&stabd[base + k*stride]) : 0.;
+                    const double* wrow = work + k*kk;
+                    #pragma unroll
+                    for (int q=0; q<4; ++q)
+                        if (use[q]) zv[b][q] = wrow[col[q]];
+                }
+            }
+            #pragma unroll
+            for (int b=0; b<TDMA_KBK; ++b)
+            {
+                if (b < nk)
+                {
+                    TF* row = pk + (long long)(k0 - b)*kk;
+                    #pragma unroll
+                    for (int q=0; q<4; ++q)
+                    {
+                        if (use[q])
+                        {
+                            z[q] = fma(-h[b], z[q], zv[b][q]);
+                            row[col[q]] = scale_out<TF>(z[q], s[b], sd[b]);
+                        }
+                    }
                 }
             }
         }
@@ -652,8 +875,13 @@ namespace mhh
         pw.nju = jtot/2 + 1;
         const size_t n = (size_t)pw.niu*pw.nju*ktot;
         if (cudaMalloc(&pw.rtab, sizeof(double)*n) != cudaSuccess) return MHH_ERR_CUDA;
+        if (cudaMalloc(&pw.gtab, sizeof(double)*n) != cudaSuccess) return MHH_ERR_CUDA;
+        if (cudaMalloc(&pw.htab, sizeof(double)*n) != cudaSuccess) return MHH_ERR_CUDA;
+        if (cudaMalloc(&pw.stab, sizeof(float)*n) != cudaSuccess) return MHH_ERR_CUDA;
+        if (cudaMalloc(&pw.stabd, sizeof(double)*n) != cudaSuccess) return MHH_ERR_CUDA;
         dim3 grid((pw.niu + 127)/128, pw.nju);
-        k_tdma_table<<<grid, 128>>>(pw.niu, pw.nju, ktot, pw.bmati, pw.bmatj, pw.a, pw.c, pw.dz2rho, pw.rtab);
+        k_tdma_table<<<grid, 128>>>(pw.niu, pw.nju, ktot, pw.bmati, pw.bmatj, pw.a, pw.c, pw.dz2rho, pw.dz2,
+                                    pw.rtab, pw.gtab, pw.htab, pw.stab, pw.stabd);
         count_launch();
         return cudaDeviceSynchronize() == cudaSuccess ? MHH_OK : MHH_ERR_CUDA;
     }
@@ -662,7 +890,12 @@ namespace mhh
     void launch_tdma(const Dims& d, const PresWork& pw, TF* pk, cudaStream_t s)
     {
         dim3 grid((pw.niu + 127)/128, pw.nju);
-        k_tdma<TF><<<grid, 128, 0, s>>>(d.itot, d.jtot, d.ktot, pw.niu, pw.nju, pw.rtab, pw.a, pw.c, pw.dz2, pk, pw.work);
+        const int v = tdma_variant() < 0 ? (sizeof(TF) == 4 ? 1 : 0) : tdma_variant();
+        if (v == 1)
+            k_tdma_scaled<TF><<<grid, 128, 0, s>>>(d.itot, d.jtot, d.ktot, pw.niu, pw.nju, pw.gtab, pw.htab,
+                                                   pw.stab, pw.stabd, pk, pw.work);
+        else
+            k_tdma<TF><<<grid, 128, 0, s>>>(d.itot, d.jtot, d.ktot, pw.niu, pw.nju, pw.rtab, pw.a, pw.c, pw.dz2, pk, pw.work);
         count_launch();
     }
 

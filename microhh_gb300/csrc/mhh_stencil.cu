@@ -2,6 +2,8 @@
 // wall ghost cells, Smagorinsky viscosity, the fused tendency kernel
 // (advection + diffusion + buoyancy + forcing), the pressure-gradient + RK3
 // update and the CFL / diffusion-number / divergence reductions.
+#include <type_traits>
+
 #include "mhh_kernels.cuh"
 #include "mhh_stencil.cuh"
 
@@ -154,7 +156,7 @@ namespace mhh
     template<typename TF, bool SURF, bool THERMO>
     __global__ void __launch_bounds__(256)
     k_viscosity(Dims d, Prof<TF> pr, const TF* __restrict__ u, const TF* __restrict__ v, const TF* __restrict__ w,
-                const TF* __restrict__ th, TF* __restrict__ evisc, const double* __restrict__ mlen2,
+                const TF* __restrict__ th, TF* __restrict__ evisc, const TF* __restrict__ mlen2,
                 const double* __restrict__ dudz, const double* __restrict__ dvdz, const double* __restrict__ dbdz,
                 TF cs, TF tpr, TF visc, int mason)
     {
@@ -165,7 +167,7 @@ namespace mhh
         const long long ii = 1, jj = d.icells, kk = d.ijcells;
         const long long c = ijk(d, i, j, k);
         const long long ij = i + (long long)j*jj;
-        const TF dxi = TF(d.dxi), dyi = TF(d.dyi);
+        const TF dxi = dxi_of<TF>(d), dyi = dyi_of<TF>(d);
 
         TF acc = sq((ld(u, c+ii)-ld(u, c))*dxi)
                + sq((ld(v, c+jj)-ld(v, c))*dyi)
@@ -203,7 +205,7 @@ namespace mhh
 
         // The squared mixing length is precomputed per level (and with the
         // Mason wall correction per level and column when z0m is uniform).
-        const TF ml2 = TF(mlen2[k]);
+        const TF ml2 = mlen2[k];
         TF ev;
         if (THERMO)
         {
@@ -228,7 +230,7 @@ namespace mhh
             const TF utt = pow(sq(visc*(ld(u, ct)-ld(u, ct-kk))*dzht) + sq(visc*(ld(v, ct)-ld(v, ct-kk))*dzht), TF(0.25));
             const TF zk = ld(pr.z, k);
             const TF fb = TF(1) - exp(-(zk*utb)/(TF(26)*visc));
-            const TF ft = TF(1) - exp(-((TF(d.zsize) - zk)*utt)/(TF(26)*visc));
+            const TF ft = TF(1) - exp(-((zsize_of<TF>(d) - zk)*utt)/(TF(26)*visc));
             const TF fac = fmin(fb, ft);
             ev = sq(fac)*ml2*sqrt(s2);
         }
@@ -249,7 +251,7 @@ namespace mhh
 
     template<typename TF>
     void launch_viscosity(const Dims& d, const Prof<TF>& pr, const TF* u, const TF* v, const TF* w, const TF* th,
-                          TF* evisc, const double* mlen2, const double* dudz, const double* dvdz, const double* dbdz,
+                          TF* evisc, const TF* mlen2, const double* dudz, const double* dvdz, const double* dbdz,
                           double cs, double tpr, double visc, int mason, bool surf, bool thermo, cudaStream_t s)
     {
         dim3 block(32, 8);
@@ -287,7 +289,7 @@ namespace mhh
         if (i >= d.iend || j >= d.jend) return;
         const long long c = ijk(d, i, j, k);
         const long long ij = i + (long long)j*d.icells;
-        const TF dxi = TF(d.dxi), dyi = TF(d.dyi);
+        const TF dxi = dxi_of<TF>(d), dyi = dyi_of<TF>(d);
         const TF* u = a.u; const TF* v = a.v; const TF* w = a.w;
 
         // u
@@ -296,7 +298,7 @@ namespace mhh
             if (ADV == MHH_ADVEC_2I5) t += advec_2i5_u(d, pr, u, v, w, c, k, dxi, dyi);
             else if (ADV == MHH_ADVEC_2) t += advec_2_u(d, pr, u, v, w, c, k, dxi, dyi);
             if (DIF == MHH_DIFF_SMAG2) t += diff_smag2_u(d, pr, u, v, w, a.evisc, a.u_fluxbot, a.u_fluxtop, SURF, c, ij, k, dxi, dyi, a.visc);
-            else if (DIF == MHH_DIFF_2) t += diff_2_c(d, pr, u, c, k, a.dxidxi, a.dyidyi, a.visc);
+            else if (DIF == MHH_DIFF_2) t += diff_2_c(d, pr, u, c, k, a.dxidxi_t, a.dyidyi_t, a.visc);
             if (FORCE) t += a.fbody;
             a.ut[c] += t;
         }
@@ -306,7 +308,7 @@ namespace mhh
             if (ADV == MHH_ADVEC_2I5) t += advec_2i5_v(d, pr, u, v, w, c, k, dxi, dyi);
             else if (ADV == MHH_ADVEC_2) t += advec_2_v(d, pr, u, v, w, c, k, dxi, dyi);
             if (DIF == MHH_DIFF_SMAG2) t += diff_smag2_v(d, pr, u, v, w, a.evisc, a.v_fluxbot, a.v_fluxtop, SURF, c, ij, k, dxi, dyi, a.visc);
-            else if (DIF == MHH_DIFF_2) t += diff_2_c(d, pr, v, c, k, a.dxidxi, a.dyidyi, a.visc);
+            else if (DIF == MHH_DIFF_2) t += diff_2_c(d, pr, v, c, k, a.dxidxi_t, a.dyidyi_t, a.visc);
             a.vt[c] += t;
         }
         // w (half levels above the wall)
@@ -317,7 +319,7 @@ namespace mhh
             if (ADV == MHH_ADVEC_2I5) t += advec_2i5_w(d, pr, u, v, w, c, k, dxi, dyi);
             else if (ADV == MHH_ADVEC_2) t += advec_2_w(d, pr, u, v, w, c, k, dxi, dyi);
             if (DIF == MHH_DIFF_SMAG2) t += diff_smag2_w(d, pr, u, v, w, a.evisc, c, k, dxi, dyi, a.visc);
-            else if (DIF == MHH_DIFF_2) t += diff_2_w(d, pr, w, c, k, a.dxidxi, a.dyidyi, a.visc);
+            else if (DIF == MHH_DIFF_2) t += diff_2_w(d, pr, w, c, k, a.dxidxi_t, a.dyidyi_t, a.visc);
             a.wt[c] += t;
         }
         // scalar
@@ -328,8 +330,8 @@ namespace mhh
             else if (ADV == MHH_ADVEC_2) t += advec_2_s(d, pr, a.s, u, v, w, c, k, dxi, dyi);
             if (DIF == MHH_DIFF_SMAG2)
                 t += diff_smag2_s(d, pr, a.s, a.evisc, a.s_fluxbot, a.s_fluxtop, SURF, c, ij, k,
-                                  TF(a.dxidxi), TF(a.dyidyi), a.tpri, a.svisc);
-            else if (DIF == MHH_DIFF_2) t += diff_2_c(d, pr, a.s, c, k, a.dxidxi, a.dyidyi, a.svisc);
+                                  a.dxidxi_t, a.dyidyi_t, a.tpri, a.svisc);
+            else if (DIF == MHH_DIFF_2) t += diff_2_c(d, pr, a.s, c, k, a.dxidxi_t, a.dyidyi_t, a.svisc);
             a.st[c] += t;
         }
     }
@@ -364,10 +366,15 @@ namespace mhh
     void launch_tendency(const Dims& d, const Prof<TF>& pr, const TendArgs<TF>& a, int adv, int dif,
                          bool surf, bool scal, bool buoy, bool force, cudaStream_t s)
     {
-        // The LES combination can run in the tiled kernel (mhh_tend_tiled.cu).
-        if (tendency_variant() == 1 && adv == MHH_ADVEC_2I5 && dif == MHH_DIFF_SMAG2 && !force && d.igc >= 3 && d.jgc >= 3)
+        // The LES combination can run in the tiled kernel (mhh_tend_tiled.cu)
+        // or in the flux-form kernel (mhh_tend_flux.cu).
+        // Automatic choice (-1): the flux form for float fields, the per-cell
+        // kernel (the reference's operation order) for double fields.
+        const int var = tendency_variant() < 0 ? (sizeof(TF) == 4 ? 2 : 0) : tendency_variant();
+        if (var >= 1 && adv == MHH_ADVEC_2I5 && dif == MHH_DIFF_SMAG2 && !force && d.igc >= 3 && d.jgc >= 3)
         {
-            launch_tendency_les<TF>(d, pr, a, surf, scal, buoy, s);
+            if (var == 2) launch_tendency_flux<TF>(d, pr, a, surf, scal, buoy, s);
+            else launch_tendency_les<TF>(d, pr, a, surf, scal, buoy, s);
             return;
         }
         // With scalar work requested but no scalar pointer, or buoyancy without
@@ -448,8 +455,8 @@ namespace mhh
         if (interior)
         {
             const TF pc = ld(p, c);
-            TF tu = ut[c] - (pc - ld(p, c-1))*TF(d.dxi);
-            TF tv = vt[c] - (pc - ld(p, c-d.icells))*TF(d.dyi);
+            TF tu = ut[c] - (pc - ld(p, c-1))*dxi_of<TF>(d);
+            TF tv = vt[c] - (pc - ld(p, c-d.icells))*dyi_of<TF>(d);
             TF tw = wt[c] - (pc - ld(p, c-d.ijcells))*ld(pr.dzhi, k);
             u[c] += cbdt*tu; v[c] += cbdt*tv; w[c] += cbdt*tw;
             ut[c] = last ? TF(0) : tu*ca;
@@ -486,24 +493,29 @@ namespace mhh
     }
 
     // ---------------------------------------------------------------------
-    // Max reductions in double: CFL of Advec_2i5 (src/advec_2i5.cxx:59-148)
-    // and Advec_2 (src/advec_2.cxx:50-80), diffusion number of Diff_smag2
+    // Max reductions: CFL of Advec_2i5 (src/advec_2i5.cxx:59-148) and
+    // Advec_2 (src/advec_2.cxx:50-80), diffusion number of Diff_smag2
     // (include/diff_kernels.h:486-511), divergence (src/pres_2.cxx:389-422).
-    // ---------------------------------------------------------------------
+    // The diffusion number and the divergence are computed per cell in
+    // double.  The CFL terms are evaluated in the field precision, as in the
+    // reference, and their maximum is taken in that precision before the one
+    // conversion per block: a maximum commutes with the exact float-to-double
+    // conversion, so the result is the same as a maximum over doubles.
     template<typename TF, int WHAT>
     __global__ void __launch_bounds__(256)
     k_reduce(Dims d, Prof<TF> pr, const TF* __restrict__ u, const TF* __restrict__ v, const TF* __restrict__ w,
              const TF* __restrict__ ev, double tprfi, unsigned long long* out)
     {
+        using RT = typename std::conditional<(WHAT <= 1), TF, double>::type;
         const int i = d.istart + blockIdx.x*blockDim.x + threadIdx.x;
         const int j = d.jstart + blockIdx.y*blockDim.y + threadIdx.y;
         const int k = d.kstart + blockIdx.z;
-        double val = 0.;
+        RT val = 0;
         if (i < d.iend && j < d.jend)
         {
             const long long ii = 1, jj = d.icells, kk = d.ijcells;
             const long long c = ijk(d, i, j, k);
-            if (WHAT == 0)
+            if constexpr (WHAT == 0)
             {
                 // CFL 2i5: w interpolated with 2nd/4th/6th order by level.
                 const int ord = face_order_w(d, k);
@@ -511,14 +523,14 @@ namespace mhh
                 if (ord == 2) wc = f2(w, c+kk, kk);
                 else if (ord == 4) wc = f4(w, c+kk, kk);
                 else wc = f6(w, c+kk, kk);
-                val = double(fabs(f6(u, c+ii, ii))*TF(d.dxi) + fabs(f6(v, c+jj, jj))*TF(d.dyi) + fabs(wc)*ld(pr.dzi, k));
+                val = fabs(f6(u, c+ii, ii))*dxi_of<TF>(d) + fabs(f6(v, c+jj, jj))*dyi_of<TF>(d) + fabs(wc)*ld(pr.dzi, k);
             }
-            else if (WHAT == 1)
+            else if constexpr (WHAT == 1)
             {
-                val = double(fabs(i2(ld(u, c), ld(u, c+ii)))*TF(d.dxi) + fabs(i2(ld(v, c), ld(v, c+jj)))*TF(d.dyi)
-                           + fabs(i2(ld(w, c), ld(w, c+kk)))*ld(pr.dzi, k));
+                val = fabs(i2(ld(u, c), ld(u, c+ii)))*dxi_of<TF>(d) + fabs(i2(ld(v, c), ld(v, c+jj)))*dyi_of<TF>(d)
+                    + fabs(i2(ld(w, c), ld(w, c+kk)))*ld(pr.dzi, k);
             }
-            else if (WHAT == 2)
+            else if constexpr (WHAT == 2)
             {
                 const double dzi = double(ld(pr.dzi, k));
                 val = fabs(double(ld(ev, c))*tprfi*(d.dxi*d.dxi + d.dyi*d.dyi + dzi*dzi));
@@ -533,17 +545,17 @@ namespace mhh
         // Block max, then one atomic per block.
         for (int o=16; o>0; o>>=1)
             val = fmax(val, __shfl_xor_sync(0xffffffffu, val, o));
-        __shared__ double sm[8];
+        __shared__ RT sm[8];
         const int lane = (threadIdx.x + threadIdx.y*blockDim.x) & 31;
         const int warp = (threadIdx.x + threadIdx.y*blockDim.x) >> 5;
         if (lane == 0) sm[warp] = val;
         __syncthreads();
         if (warp == 0)
         {
-            val = lane < (int)(blockDim.x*blockDim.y/32) ? sm[lane] : 0.;
+            val = lane < (int)(blockDim.x*blockDim.y/32) ? sm[lane] : RT(0);
             for (int o=16; o>0; o>>=1)
                 val = fmax(val, __shfl_xor_sync(0xffffffffu, val, o));
-            if (lane == 0) atomic_max_nonneg(out, val);
+            if (lane == 0) atomic_max_nonneg(out, double(val));
         }
     }
 
@@ -566,7 +578,7 @@ namespace mhh
     template void launch_set_bc<TF>(TF*, TF*, TF*, int, double, double, int, const Dims&, cudaStream_t); \
     template void launch_ghost<TF>(const GhostList<TF>&, const Dims&, const TF*, cudaStream_t); \
     template void launch_viscosity<TF>(const Dims&, const Prof<TF>&, const TF*, const TF*, const TF*, const TF*, TF*, \
-        const double*, const double*, const double*, const double*, double, double, double, int, bool, bool, cudaStream_t); \
+        const TF*, const double*, const double*, const double*, double, double, double, int, bool, bool, cudaStream_t); \
     template void launch_tendency<TF>(const Dims&, const Prof<TF>&, const TendArgs<TF>&, int, int, bool, bool, bool, bool, cudaStream_t); \
     template void launch_rk3<TF>(TF*, TF*, const Dims&, int, double, cudaStream_t); \
     template void launch_presout_rk3<TF>(const Dims&, const Prof<TF>&, const TF*, TF*, TF*, TF*, TF*, TF*, TF*, TF*, TF*, int, double, cudaStream_t); \

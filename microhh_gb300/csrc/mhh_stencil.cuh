@@ -264,27 +264,29 @@ namespace mhh
     }
 
     // ---- Diff_2, src/diff_2.cxx:38-86 ------------------------------------
-    // dxidxi and dyidyi are double in the reference even for float fields.
+    // (dxidxi and dyidyi are double in the reference even for float fields;
+    // here they take the kernel's precision so that float kernels stay off
+    // the FP64 pipe.)
 
     template<typename TF>
     __device__ __forceinline__ TF diff_2_c(const Dims& d, const Prof<TF>& pr, const TF* a, long long c, int k,
-                                           double dxidxi, double dyidyi, TF visc)
+                                           TF dxidxi, TF dyidyi, TF visc)
     {
         const long long ii = 1, jj = d.icells, kk = d.ijcells;
         const TF ac = ld(a, c);
-        return visc*(TF(((ld(a, c+ii)-ac) - (ac-ld(a, c-ii)))*dxidxi)
-                   + TF(((ld(a, c+jj)-ac) - (ac-ld(a, c-jj)))*dyidyi)
+        return visc*(((ld(a, c+ii)-ac) - (ac-ld(a, c-ii)))*dxidxi
+                   + ((ld(a, c+jj)-ac) - (ac-ld(a, c-jj)))*dyidyi
                    + ((ld(a, c+kk)-ac)*ld(pr.dzhi, k+1) - (ac-ld(a, c-kk))*ld(pr.dzhi, k))*ld(pr.dzi, k));
     }
 
     template<typename TF>
     __device__ __forceinline__ TF diff_2_w(const Dims& d, const Prof<TF>& pr, const TF* w, long long c, int k,
-                                           double dxidxi, double dyidyi, TF visc)
+                                           TF dxidxi, TF dyidyi, TF visc)
     {
         const long long ii = 1, jj = d.icells, kk = d.ijcells;
         const TF wc = ld(w, c);
-        return visc*(TF(((ld(w, c+ii)-wc) - (wc-ld(w, c-ii)))*dxidxi)
-                   + TF(((ld(w, c+jj)-wc) - (wc-ld(w, c-jj)))*dyidyi)
+        return visc*(((ld(w, c+ii)-wc) - (wc-ld(w, c-ii)))*dxidxi
+                   + ((ld(w, c+jj)-wc) - (wc-ld(w, c-jj)))*dyidyi
                    + ((ld(w, c+kk)-wc)*ld(pr.dzi, k) - (wc-ld(w, c-kk))*ld(pr.dzi, k-1))*ld(pr.dzhi, k));
     }
 }

@@ -1,40 +1,33 @@
 // mhh_surface.cu -- Monin-Obukhov surface layer on the GPU, after
 // src/boundary_surface.cxx:836-994 and include/boundary_surface_kernels.h
 // (lookup-table Obukhov-length solver with homogeneous z0m/z0h, noslip
-// momentum, flux or Dirichlet scalar).  All 2-D arithmetic is in double; the
-// z/L lookup table and the Richardson-number interpolation stay in float as in
-// the reference, with the float operations rounded one by one so that they
-// match the CPU bit for bit.
+// momentum, flux or Dirichlet scalar).  The 2-D fields are stored in double;
+// the Obukhov length and the similarity functions are computed in the field
+// precision (double for the FP64 path, float for the FP32 form, which keeps
+// the float form off the slow FP64 pipe).  The z/L lookup table and the
+// Richardson-number interpolation stay in float as in the reference, with the
+// float operations rounded one by one so that they match the CPU bit for bit.
 #include "mhh_kernels.cuh"
 
 namespace mhh
 {
-    __device__ __forceinline__ double phim_unstable(double z) { return pow(1. + 3.6*pow(fabs(z), 2./3.), -1./2.); }
-    __device__ __forceinline__ double phih_unstable(double z) { return pow(1. + 7.9*pow(fabs(z), 2./3.), -1./2.); }
-    __device__ __forceinline__ double phim(double z) { return z <= 0. ? phim_unstable(z) : 1. + 5.*z; }
-    __device__ __forceinline__ double phih(double z) { return z <= 0. ? phih_unstable(z) : (1. + 4.*z)*(1. + 4.*z); }
-    __device__ __forceinline__ double psim_unstable(double z) { return 3.*log((1. + 1./phim_unstable(z))/2.); }
-    __device__ __forceinline__ double psih_unstable(double z) { return 3.*log((1. + 1./phih_unstable(z))/2.); }
-    __device__ __forceinline__ double psim_stable(double z)
+    // Monin-Obukhov similarity functions, include/monin_obukhov.h:40-152, in
+    // the compute type CT (double for the FP64 path, float for the FP32 form).
+    template<typename CT> __device__ __forceinline__ CT phim_unstable(CT z)
+    { return pow(CT(1) + CT(3.6)*pow(fabs(z), CT(2./3.)), CT(-1./2.)); }
+    template<typename CT> __device__ __forceinline__ CT phih_unstable(CT z)
+    { return pow(CT(1) + CT(7.9)*pow(fabs(z), CT(2./3.)), CT(-1./2.)); }
+    template<typename CT> __device__ __forceinline__ CT phim(CT z) { return z <= CT(0) ? phim_unstable(z) : CT(1) + CT(5)*z; }
+    template<typename CT> __device__ __forceinline__ CT phih(CT z) { return z <= CT(0) ? phih_unstable(z) : (CT(1) + CT(4)*z)*(CT(1) + CT(4)*z); }
+    template<typename CT> __device__ __forceinline__ CT psim_stable(CT z)
     {
-        const double a = 1., b = 2./3., c = 5., d = 0.35;
+        const CT a = 1, b = CT(2)/CT(3), c = 5, d = CT(0.35);
         return -b*(z - (c/d))*exp(-d*z) - a*z - (b*c)/d;
     }
-    __device__ __forceinline__ double psih_stable(double z)
+    template<typename CT> __device__ __forceinline__ CT psih_stable(CT z)
     {
-        const double a = 1., b = 2./3., c = 5., d = 0.35;
-        return -b*(z - (c/d))*exp(-d*z) - pow(1. + b*a*z, 1.5) - (b*c)/d + 1.;
-    }
-    // include/monin_obukhov.h:137-152
-    __device__ __forceinline__ double most_fm(double zsl, double z0m, double L)
-    {
-        return L <= 0. ? KAPPA/(log(zsl/z0m) - psim_unstable(zsl/L) + psim_unstable(z0m/L))
-                       : KAPPA/(log(zsl/z0m) - psim_stable  (zsl/L) + psim_stable  (z0m/L));
-    }
-    __device__ __forceinline__ double most_fh(double zsl, double z0h, double L)
-    {
-        return L <= 0. ? KAPPA/(log(zsl/z0h) - psih_unstable(zsl/L) + psih_unstable(z0h/L))
-                       : KAPPA/(log(zsl/z0h) - psih_stable  (zsl/L) + psih_stable  (z0h/L));
+        const CT a = 1, b = CT(2)/CT(3), c = 5, d = CT(0.35);
+        return -b*(z - (c/d))*exp(-d*z) - pow(CT(1) + b*a*z, CT(1.5)) - (b*c)/d + CT(1);
     }
 
     // include/boundary_surface_kernels.h:282-298, with the search kept inside
@@ -83,27 +76,29 @@ namespace mhh
     // The Monin-Obukhov functions of one cell, each evaluated once: the
     // similarity function phi of the stability branch feeds both the
     // integrated psi and the gradient (include/monin_obukhov.h:40-152).
-    struct MostCell { double fm, fh, phim, phih; };
+    template<typename CT> struct MostCell { CT fm, fh, phim, phih; };
 
-    __device__ __forceinline__ MostCell most_cell(double zsl, double z0m, double z0h, double L)
+    template<typename CT>
+    __device__ __forceinline__ MostCell<CT> most_cell(CT zsl, CT z0m, CT z0h, CT L)
     {
-        MostCell r;
-        const double zeta = zsl/L;
-        if (L <= 0.)
+        MostCell<CT> r;
+        const CT kappa = CT(KAPPA);
+        const CT zeta = zsl/L;
+        if (L <= CT(0))
         {
-            const double pm_s = phim_unstable(zeta), pm_0 = phim_unstable(z0m/L);
-            const double ph_s = phih_unstable(zeta), ph_0 = phih_unstable(z0h/L);
-            const double psim_s = 3.*log((1. + 1./pm_s)/2.), psim_0 = 3.*log((1. + 1./pm_0)/2.);
-            const double psih_s = 3.*log((1. + 1./ph_s)/2.), psih_0 = 3.*log((1. + 1./ph_0)/2.);
-            r.fm = KAPPA/(log(zsl/z0m) - psim_s + psim_0);
-            r.fh = KAPPA/(log(zsl/z0h) - psih_s + psih_0);
-            r.phim = zeta <= 0. ? pm_s : 1. + 5.*zeta;
-            r.phih = zeta <= 0. ? ph_s : (1. + 4.*zeta)*(1. + 4.*zeta);
+            const CT pm_s = phim_unstable(zeta), pm_0 = phim_unstable(z0m/L);
+            const CT ph_s = phih_unstable(zeta), ph_0 = phih_unstable(z0h/L);
+            const CT psim_s = CT(3)*log((CT(1) + CT(1)/pm_s)/CT(2)), psim_0 = CT(3)*log((CT(1) + CT(1)/pm_0)/CT(2));
+            const CT psih_s = CT(3)*log((CT(1) + CT(1)/ph_s)/CT(2)), psih_0 = CT(3)*log((CT(1) + CT(1)/ph_0)/CT(2));
+            r.fm = kappa/(log(zsl/z0m) - psim_s + psim_0);
+            r.fh = kappa/(log(zsl/z0h) - psih_s + psih_0);
+            r.phim = zeta <= CT(0) ? pm_s : CT(1) + CT(5)*zeta;
+            r.phih = zeta <= CT(0) ? ph_s : (CT(1) + CT(4)*zeta)*(CT(1) + CT(4)*zeta);
         }
         else
         {
-            r.fm = KAPPA/(log(zsl/z0m) - psim_stable(zeta) + psim_stable(z0m/L));
-            r.fh = KAPPA/(log(zsl/z0h) - psih_stable(zeta) + psih_stable(z0h/L));
+            r.fm = kappa/(log(zsl/z0m) - psim_stable(zeta) + psim_stable(z0m/L));
+            r.fh = kappa/(log(zsl/z0h) - psih_stable(zeta) + psih_stable(z0h/L));
             r.phim = phim(zeta);
             r.phih = phih(zeta);
         }
@@ -119,28 +114,28 @@ namespace mhh
     {
         const int n = blockIdx.x*blockDim.x + threadIdx.x;
         if (n >= d.ijcells) return;
-        const double du = sw.dutot[n];
-        double L;
+        using CT = TF;
+        const CT du = CT(sw.dutot[n]);
+        const CT zs = CT(zsl);
+        CT L;
         if (!thermo)
-            L = -DBIG;
+            L = CT(-DBIG);
         else if (thermo_bc == MHH_BC_FLUX)
         {
-            const double bfluxbot = GRAV/threfh_s*double(s_flux[n]);
-            const float Ri = (float)(-KAPPA*bfluxbot*zsl/(du*du*du));
-            L = zsl/find_zL(sw.zL, sw.f, &sw.nobuk[n], Ri);
+            const CT bfluxbot = CT(GRAV)/CT(threfh_s)*CT(s_flux[n]);
+            const float Ri = (float)(CT(-KAPPA)*bfluxbot*zs/(du*du*du));
+            L = zs/CT(find_zL(sw.zL, sw.f, &sw.nobuk[n], Ri));
         }
         else
         {
-            const double b = GRAV/thref_s*(double(s[n + (long long)d.kstart*d.ijcells]) - thref_s);
-            const double bbot = GRAV/threfh_s*(double(s_bot[n]) - threfh_s);
-            const double db_ref = GRAV/thref_s*(thref_s - threfh_s);
-            const double db = b - bbot + db_ref;
-            const float Ri = (float)(KAPPA*db*zsl/(du*du));
-            L = zsl/find_zL(sw.zL, sw.f, &sw.nobuk[n], Ri);
+            const CT b = CT(GRAV)/CT(thref_s)*(CT(s[n + (long long)d.kstart*d.ijcells]) - CT(thref_s));
+            const CT bbot = CT(GRAV)/CT(threfh_s)*(CT(s_bot[n]) - CT(threfh_s));
+            const CT db_ref = CT(GRAV)/CT(thref_s)*(CT(thref_s) - CT(threfh_s));
+            const CT db = b - bbot + db_ref;
+            const float Ri = (float)(CT(KAPPA)*db*zs/(du*du));
+            L = zs/CT(find_zL(sw.zL, sw.f, &sw.nobuk[n], Ri));
         }
-        // zsl/L and z0/L of a large |L| can reach zero; the branch choice
-        // follows the sign of L exactly as the separate functions do.
-        const MostCell mc = most_cell(zsl, z0m, sw.z0h, L);
+        const MostCell<CT> mc = most_cell<CT>(zs, CT(z0m), CT(sw.z0h), L);
         sw.obuk[n] = L;
         sw.ustar[n] = du*mc.fm;
         sw.fm[n] = mc.fm; sw.fh[n] = mc.fh; sw.phim[n] = mc.phim; sw.phih[n] = mc.phih;

@@ -1,0 +1,400 @@
+// mhh_tend_flux.cu -- the LES tendency kernel in flux form (Advec_2i5 +
+// Smagorinsky diffusion + dry buoyancy, optionally with the Monin-Obukhov
+// wall fluxes).
+//
+// Every face flux is computed once.  A block owns a 32 x 8 tile of columns
+// and marches upward through a chunk of levels.  Its 33 x 9 face threads
+// compute, per level, the total (diffusive minus advective) flux through the
+// x- and y-faces of the u, v, w and s control volumes into shared memory; the
+// 32 x 8 cell threads add the flux differences, with the vertical faces of
+// their own column kept in registers (the top face of one level is the bottom
+// face of the next).  The shear stresses are shared between the fields whose
+// faces coincide: tau_xy at (i-1/2, j-1/2) is the y-flux of u and the x-flux
+// of v, tau_xz at (i-1/2, k+1/2) the x-flux of w and the z-flux of u, and
+// tau_yz likewise for w and v.
+//
+// Iteration m handles u, v, s at full level m and w at half level m+1, so the
+// horizontal faces of w and the vertical faces of u, v, s lie on the same
+// half level and share tau_xz and tau_yz.  The planes of each level (u, v, w,
+// s and the eddy viscosity with a 3-cell halo) are staged in shared memory
+// by cp.async one level ahead of their use; the 7-point vertical
+// neighbourhoods of the own column come from register queues.
+//
+// The arithmetic per face is that of the reference's kernels:
+// src/advec_2i5.cxx:150-728 (6th-order interpolation with 5th-order upwind
+// dissipation, lower orders next to the walls), include/diff_kernels.h:144-484
+// (Smagorinsky fluxes; wall fluxes from the surface model) and
+// src/thermo_dry.cxx:165-181 (buoyancy).  The sum of all fluxes is formed
+// before it is added to the tendency, so the result differs from the
+// reference's term-by-term accumulation by round-off only.
+#include "mhh_kernels.cuh"
+#include "mhh_stencil.cuh"
+
+namespace mhh
+{
+    namespace
+    {
+        constexpr int FTX = 32, FTY = 8, FH = 3;
+        constexpr int FPW = 40;                 // plane row (FTX + 2*FH, padded)
+        constexpr int FPH = FTY + 2*FH;         // plane rows
+        constexpr int FPS = FPW*FPH;            // plane size
+        constexpr int NFX = FTX + 1, NFY = FTY + 1;
+        constexpr int NFACE = NFX*NFY;          // 297 face threads
+        constexpr int NTHR = 320;
+        constexpr int FKCHUNK = 32;
+        // Plane slots: u 3, v 3, w 2, s 2, evisc 3; level l of a field lives in
+        // slot base + l % n.
+        constexpr int SU = 0, SV = 3, SW = 6, SS = 8, SE = 10, NSLOT = 13;
+        constexpr int NGX = FTY*NFX;            // x-faces per level and field
+        constexpr int NGY = NFY*FTX;            // y-faces per level and field
+        constexpr int NEL1 = FPS - NTHR;        // threads that copy a second element
+
+        template<typename TF> struct FluxOcc { static constexpr int v = sizeof(TF) == 4 ? 2 : 1; };
+
+        template<typename TF>
+        size_t flux_smem() { return sizeof(TF)*(size_t(NSLOT)*FPS + 2*4*(NGX + NGY)); }
+    }
+
+    // Asynchronous global -> shared copy of one element; a copy with
+    // valid == false writes zero and reads nothing.
+    template<typename TF>
+    __device__ __forceinline__ void cp_async_el(TF* dst, const TF* src, bool valid)
+    {
+        const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+        const int n = valid ? (int)sizeof(TF) : 0;
+        if constexpr (sizeof(TF) == 4)
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" :: "r"(s), "l"(src), "r"(n) : "memory");
+        else
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" :: "r"(s), "l"(src), "r"(n) : "memory");
+    }
+    __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+    __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+    // Upwind-biased advective flux vel * phi at a face from the six values
+    // around it (6th-order interpolation minus 5th-order dissipation).
+    template<typename TF>
+    __device__ __forceinline__ TF adv6(TF vel, TF a, TF b, TF c, TF d, TF e, TF f)
+    {
+        return vel*i6ws(a, b, c, d, e, f) - fabs(vel)*i5ws(a, b, c, d, e, f);
+    }
+
+    // Vertical advective flux through the face between queue entries 2 and 3
+    // (queue entry q holds level m-2+q of the own column).
+    template<typename TF>
+    __device__ __forceinline__ TF zadv(const TF (&q)[6], TF wf, int order)
+    {
+        if (order == 6) return adv6(wf, q[0], q[1], q[2], q[3], q[4], q[5]);
+        if (order == 4) return wf*i4ws(q[1], q[2], q[3], q[4]) - fabs(wf)*i3ws(q[1], q[2], q[3], q[4]);
+        if (order == 2) return wf*i2(q[2], q[3]);
+        return TF(0);
+    }
+
+    template<typename TF, bool SURF, bool SCAL, bool BUOY>
+    __global__ void __launch_bounds__(NTHR, FluxOcc<TF>::v)
+    k_tend_flux(Dims d, Prof<TF> pr, TendArgs<TF> a)
+    {
+        extern __shared__ __align__(16) unsigned char smem_raw[];
+        TF* sm = reinterpret_cast<TF*>(smem_raw);
+        TF* gbase = sm + NSLOT*FPS;     // [2 buffers][4 fields][NGX] then [2][4][NGY]
+
+        const int tid = threadIdx.x;
+        const int fx = tid % NFX, fy = tid / NFX;
+        const bool face = tid < NFACE;
+        const bool face_x = face && fy < FTY;
+        const bool face_y = face && fx < FTX;
+        const int i0 = d.istart + blockIdx.x*FTX;
+        const int j0 = d.jstart + blockIdx.y*FTY;
+        const int i = i0 + fx, j = j0 + fy;
+        const bool cell = fx < FTX && fy < FTY && i < d.iend && j < d.jend;
+        const int k0 = d.kstart + blockIdx.z*FKCHUNK;
+        const int k1 = min(k0 + FKCHUNK, d.kend);
+        const int pc = (min(fy, FTY) + FH)*FPW + (fx + FH);   // own (i, j) in a plane
+        const int gxi = fy*NFX + fx, gyi = fy*FTX + fx;
+
+        // The (at most) two plane elements this thread copies per plane.
+        const int e0 = tid, e1 = tid + NTHR;
+        int go0, go1;
+        bool v0, v1;
+        {
+            const int pj = e0 / FPW, pi = e0 - pj*FPW;
+            const int gi = i0 - FH + pi, gj = j0 - FH + pj;
+            v0 = gi < d.icells && gj < d.jcells;
+            go0 = v0 ? gi + gj*d.icells : 0;
+        }
+        {
+            const int pj = e1 / FPW, pi = e1 - pj*FPW;
+            const int gi = i0 - FH + pi, gj = j0 - FH + pj;
+            v1 = tid < NEL1 && gi < d.icells && gj < d.jcells;
+            go1 = v1 ? gi + gj*d.icells : 0;
+        }
+        auto plane = [&](int slot, const TF* f, int l)
+        {
+            TF* dst = sm + slot*FPS;
+            const TF* src = f + (long long)l*d.ijcells;
+            cp_async_el(dst + e0, v0 ? src + go0 : f, v0);
+            if (tid < NEL1) cp_async_el(dst + e1, v1 ? src + go1 : f, v1);
+        };
+
+        const TF* __restrict__ u = a.u;
+        const TF* __restrict__ v = a.v;
+        const TF* __restrict__ w = a.w;
+        const TF* __restrict__ s = a.s;
+        const TF* __restrict__ ev = a.evisc;
+        const long long col = cell ? (long long)i + (long long)j*d.icells : 0;
+        auto colval = [&](const TF* f, int l) -> TF
+        {
+            l = l < 0 ? 0 : (l > d.kcells-1 ? d.kcells-1 : l);
+            return __ldg(f + col + (long long)l*d.ijcells);
+        };
+
+        // Planes of the first iteration (m0) and of the next one.
+        const int m0 = k0 - 1;
+        plane(SU + m0%3, u, m0); plane(SU + (m0+1)%3, u, m0+1); plane(SU + (m0+2)%3, u, m0+2);
+        plane(SV + m0%3, v, m0); plane(SV + (m0+1)%3, v, m0+1); plane(SV + (m0+2)%3, v, m0+2);
+        plane(SW + (m0+1)%2, w, m0+1); plane(SW + (m0+2)%2, w, m0+2);
+        plane(SE + m0%3, ev, m0); plane(SE + (m0+1)%3, ev, m0+1); plane(SE + (m0+2)%3, ev, m0+2);
+        if (SCAL) { plane(SS + m0%2, s, m0); plane(SS + (m0+1)%2, s, m0+1); }
+        cp_async_commit();
+
+        // Register queues of the own column: u, v, s hold levels m-2 .. m+3,
+        // w holds m-1 .. m+4.
+        TF qu[6], qv[6], qw[6], qs[6];
+        if (cell)
+        {
+            #pragma unroll
+            for (int q=0; q<6; ++q)
+            {
+                qu[q] = colval(u, m0-2+q);
+                qv[q] = colval(v, m0-2+q);
+                qw[q] = colval(w, m0-1+q);
+                qs[q] = (SCAL || BUOY) ? colval(s, m0-2+q) : TF(0);
+            }
+        }
+        TF ufb = 0, uft = 0, vfb = 0, vft = 0, sfb = 0, sft = 0;
+        if (SURF && cell)
+        {
+            ufb = a.u_fluxbot[col]; uft = a.u_fluxtop[col];
+            vfb = a.v_fluxbot[col]; vft = a.v_fluxtop[col];
+            if (SCAL) { sfb = a.s_fluxbot[col]; sft = a.s_fluxtop[col]; }
+        }
+
+        const TF dxi = dxi_of<TF>(d), dyi = dyi_of<TF>(d);
+        const TF visc = a.visc, svisc = a.svisc, tpri = a.tpri;
+        TF gzu_b = 0, gzv_b = 0, gzw_b = 0, gzs_b = 0;
+
+        cp_async_wait_all();
+        __syncthreads();
+
+        for (int m = m0; m < k1; ++m)
+        {
+            const int buf = (m - m0) & 1;
+            TF* gx = gbase + buf*4*NGX;
+            TF* gy = gbase + 2*4*NGX + buf*4*NGY;
+            const TF* U0 = sm + (SU + m%3)*FPS + pc;
+            const TF* U1 = sm + (SU + (m+1)%3)*FPS + pc;
+            const TF* V0 = sm + (SV + m%3)*FPS + pc;
+            const TF* V1 = sm + (SV + (m+1)%3)*FPS + pc;
+            const TF* W1 = sm + (SW + (m+1)%2)*FPS + pc;
+            const TF* S0 = sm + (SS + m%2)*FPS + pc;
+            const TF* E0 = sm + (SE + m%3)*FPS + pc;
+            const TF* E1 = sm + (SE + (m+1)%3)*FPS + pc;
+            #define PL(P, dx, dy) (P)[(dy)*FPW + (dx)]
+
+            const bool write = cell && m >= k0;
+            const bool wlev = m+1 > d.kstart && m+1 < d.kend;
+            const long long c = col + (long long)m*d.ijcells;
+            // Early loads: the tendencies this iteration updates and the queue
+            // entries of the next iteration.
+            TF tu = 0, tv = 0, tw = 0, ts = 0;
+            if (write)
+            {
+                tu = a.ut[c]; tv = a.vt[c];
+                if (wlev) tw = a.wt[c + d.ijcells];
+                if (SCAL) ts = a.st[c];
+            }
+            TF nu = 0, nv = 0, nw = 0, ns = 0;
+            if (cell)
+            {
+                nu = colval(u, m+4); nv = colval(v, m+4); nw = colval(w, m+5);
+                if (SCAL || BUOY) ns = colval(s, m+4);
+            }
+
+            const TF dzhi1 = pr.dzhi[m+1];
+
+            // ---- faces: shear stresses and total fluxes ----
+            TF txz = 0, tyz = 0;
+            if (face)
+            {
+                const TF txy = (TF(0.25)*(PL(E0,-1,-1) + PL(E0,0,-1) + PL(E0,-1,0) + PL(E0,0,0)) + visc)
+                             * ((PL(U0,0,0) - PL(U0,0,-1))*dyi + (PL(V0,0,0) - PL(V0,-1,0))*dxi);
+                txz = (TF(0.25)*(PL(E0,-1,0) + PL(E0,0,0) + PL(E1,-1,0) + PL(E1,0,0)) + visc)
+                    * ((PL(U1,0,0) - PL(U0,0,0))*dzhi1 + (PL(W1,0,0) - PL(W1,-1,0))*dxi);
+                tyz = (TF(0.25)*(PL(E0,0,-1) + PL(E0,0,0) + PL(E1,0,-1) + PL(E1,0,0)) + visc)
+                    * ((PL(V1,0,0) - PL(V0,0,0))*dzhi1 + (PL(W1,0,0) - PL(W1,0,-1))*dyi);
+                if (face_x)
+                {
+                    // u at the cell centre i-1.
+                    {
+                        const TF uw = i2(PL(U0,-1,0), PL(U0,0,0));
+                        const TF A = adv6(uw, PL(U0,-3,0), PL(U0,-2,0), PL(U0,-1,0), PL(U0,0,0), PL(U0,1,0), PL(U0,2,0));
+                        const TF D = TF(2)*(PL(E0,-1,0) + visc)*(PL(U0,0,0) - PL(U0,-1,0))*dxi;
+                        gx[0*NGX + gxi] = D - A;
+                    }
+                    // v at (i-1/2, j-1/2).
+                    {
+                        const TF uw = i2(PL(U0,0,-1), PL(U0,0,0));
+                        const TF A = adv6(uw, PL(V0,-3,0), PL(V0,-2,0), PL(V0,-1,0), PL(V0,0,0), PL(V0,1,0), PL(V0,2,0));
+                        gx[1*NGX + gxi] = txy - A;
+                    }
+                    // w at (i-1/2, m+1/2).
+                    {
+                        const TF uw = i2(PL(U0,0,0), PL(U1,0,0));
+                        const TF A = adv6(uw, PL(W1,-3,0), PL(W1,-2,0), PL(W1,-1,0), PL(W1,0,0), PL(W1,1,0), PL(W1,2,0));
+                        gx[2*NGX + gxi] = txz - A;
+                    }
+                    if (SCAL)
+                    {
+                        const TF uw = PL(U0,0,0);
+                        const TF A = adv6(uw, PL(S0,-3,0), PL(S0,-2,0), PL(S0,-1,0), PL(S0,0,0), PL(S0,1,0), PL(S0,2,0));
+                        const TF D = (TF(0.5)*(PL(E0,-1,0) + PL(E0,0,0))*tpri + svisc)*(PL(S0,0,0) - PL(S0,-1,0))*dxi;
+                        gx[3*NGX + gxi] = D - A;
+                    }
+                }
+                if (face_y)
+                {
+                    // u at (i-1/2, j-1/2).
+                    {
+                        const TF vs = i2(PL(V0,-1,0), PL(V0,0,0));
+                        const TF A = adv6(vs, PL(U0,0,-3), PL(U0,0,-2), PL(U0,0,-1), PL(U0,0,0), PL(U0,0,1), PL(U0,0,2));
+                        gy[0*NGY + gyi] = txy - A;
+                    }
+                    // v at the cell centre j-1.
+                    {
+                        const TF vs = i2(PL(V0,0,-1), PL(V0,0,0));
+                        const TF A = adv6(vs, PL(V0,0,-3), PL(V0,0,-2), PL(V0,0,-1), PL(V0,0,0), PL(V0,0,1), PL(V0,0,2));
+                        const TF D = TF(2)*(PL(E0,0,-1) + visc)*(PL(V0,0,0) - PL(V0,0,-1))*dyi;
+                        gy[1*NGY + gyi] = D - A;
+                    }
+                    // w at (j-1/2, m+1/2).
+                    {
+                        const TF vs = i2(PL(V0,0,0), PL(V1,0,0));
+                        const TF A = adv6(vs, PL(W1,0,-3), PL(W1,0,-2), PL(W1,0,-1), PL(W1,0,0), PL(W1,0,1), PL(W1,0,2));
+                        gy[2*NGY + gyi] = tyz - A;
+                    }
+                    if (SCAL)
+                    {
+                        const TF vs = PL(V0,0,0);
+                        const TF A = adv6(vs, PL(S0,0,-3), PL(S0,0,-2), PL(S0,0,-1), PL(S0,0,0), PL(S0,0,1), PL(S0,0,2));
+                        const TF D = (TF(0.5)*(PL(E0,0,-1) + PL(E0,0,0))*tpri + svisc)*(PL(S0,0,0) - PL(S0,0,-1))*dyi;
+                        gy[3*NGY + gyi] = D - A;
+                    }
+                }
+            }
+
+            // ---- vertical faces of the own column ----
+            TF gzu_t = 0, gzv_t = 0, gzw_t = 0, gzs_t = 0, buoy = 0;
+            if (cell)
+            {
+                const int kf = m + 1;
+                const int ot = face_order_full(d, kf);
+                const TF rhoh1 = pr.rhorefh[kf];
+                // u and v: diffusive flux from the shear stress of the same
+                // face, or the surface model's flux at the walls.
+                const TF du = (SURF && kf == d.kstart) ? -ufb : ((SURF && kf == d.kend) ? -uft : txz);
+                const TF dv = (SURF && kf == d.kstart) ? -vfb : ((SURF && kf == d.kend) ? -vft : tyz);
+                gzu_t = rhoh1*(du - zadv(qu, i2(PL(W1,-1,0), PL(W1,0,0)), ot));
+                gzv_t = rhoh1*(dv - zadv(qv, i2(PL(W1,0,-1), PL(W1,0,0)), ot));
+                if (SCAL)
+                {
+                    const TF ds = (SURF && kf == d.kstart) ? -sfb : ((SURF && kf == d.kend) ? -sft
+                                : (TF(0.5)*(PL(E0,0,0) + PL(E1,0,0))*tpri + svisc)*(qs[3] - qs[2])*dzhi1);
+                    gzs_t = rhoh1*(ds - zadv(qs, qw[2], ot));
+                }
+                // w: the full level kf between w(kf) and w(kf+1).
+                if (kf < d.kend)
+                {
+                    const int ow = face_order_w(d, kf);
+                    const TF dw = TF(2)*(PL(E1,0,0) + visc)*(qw[3] - qw[2])*pr.dzi[kf];
+                    TF aw;
+                    if (ow == 6) aw = adv6(i2(qw[2], qw[3]), qw[0], qw[1], qw[2], qw[3], qw[4], qw[5]);
+                    else if (ow == 4) aw = i2(qw[2], qw[3])*i4ws(qw[1], qw[2], qw[3], qw[4])
+                                         - fabs(i2(qw[2], qw[3]))*i3ws(qw[1], qw[2], qw[3], qw[4]);
+                    else aw = i2(qw[2], qw[3])*i2(qw[2], qw[3]);
+                    gzw_t = pr.rhoref[kf]*(dw - aw);
+                }
+                if (BUOY && wlev)
+                    buoy = TF(GRAV)/pr.threfh[kf]*(i2(qs[2], qs[3]) - pr.threfh[kf]);
+            }
+            #undef PL
+
+            cp_async_wait_all();
+            __syncthreads();
+
+            // Planes of iteration m+2 into the slots that iteration m freed.
+            if (m + 2 < k1)
+            {
+                plane(SU + (m+3)%3, u, m+3);
+                plane(SV + (m+3)%3, v, m+3);
+                plane(SW + (m+3)%2, w, m+3);
+                plane(SE + (m+3)%3, ev, m+3);
+                if (SCAL) plane(SS + (m+2)%2, s, m+2);
+            }
+            cp_async_commit();
+
+            if (write)
+            {
+                const int gx0 = gxi, gy0 = gyi;
+                const TF zf = pr.zfac[m];
+                a.ut[c] = tu + (gx[0*NGX + gx0 + 1] - gx[0*NGX + gx0])*dxi
+                             + (gy[0*NGY + gy0 + FTX] - gy[0*NGY + gy0])*dyi + (gzu_t - gzu_b)*zf;
+                a.vt[c] = tv + (gx[1*NGX + gx0 + 1] - gx[1*NGX + gx0])*dxi
+                             + (gy[1*NGY + gy0 + FTX] - gy[1*NGY + gy0])*dyi + (gzv_t - gzv_b)*zf;
+                if (wlev)
+                    a.wt[c + d.ijcells] = tw + (gx[2*NGX + gx0 + 1] - gx[2*NGX + gx0])*dxi
+                                             + (gy[2*NGY + gy0 + FTX] - gy[2*NGY + gy0])*dyi
+                                             + (gzw_t - gzw_b)*pr.zfach[m+1] + buoy;
+                if (SCAL)
+                    a.st[c] = ts + (gx[3*NGX + gx0 + 1] - gx[3*NGX + gx0])*dxi
+                                 + (gy[3*NGY + gy0 + FTX] - gy[3*NGY + gy0])*dyi + (gzs_t - gzs_b)*zf;
+            }
+
+            gzu_b = gzu_t; gzv_b = gzv_t; gzw_b = gzw_t; gzs_b = gzs_t;
+            #pragma unroll
+            for (int q=0; q<5; ++q) { qu[q] = qu[q+1]; qv[q] = qv[q+1]; qw[q] = qw[q+1]; qs[q] = qs[q+1]; }
+            qu[5] = nu; qv[5] = nv; qw[5] = nw; qs[5] = ns;
+        }
+        cp_async_wait_all();
+    }
+
+    template<typename TF, bool SURF, bool SCAL, bool BUOY>
+    static void launch_flux_t(const Dims& d, const Prof<TF>& pr, const TendArgs<TF>& a, cudaStream_t s)
+    {
+        const size_t smem = flux_smem<TF>();
+        dim3 grid((d.itot + FTX - 1)/FTX, (d.jtot + FTY - 1)/FTY, (d.ktot + FKCHUNK - 1)/FKCHUNK);
+        cudaFuncSetAttribute(k_tend_flux<TF, SURF, SCAL, BUOY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        k_tend_flux<TF, SURF, SCAL, BUOY><<<grid, NTHR, smem, s>>>(d, pr, a);
+        count_launch();
+    }
+
+    // Advec_2i5 + Diff_smag2 (+ buoyancy) in flux form; igc, jgc >= 3.
+    template<typename TF>
+    void launch_tendency_flux(const Dims& d, const Prof<TF>& pr, const TendArgs<TF>& a, bool surf, bool scal,
+                              bool buoy, cudaStream_t s)
+    {
+        const int mask = (surf ? 4 : 0) | (scal ? 2 : 0) | (buoy ? 1 : 0);
+        switch (mask)
+        {
+            case 0: launch_flux_t<TF, false, false, false>(d, pr, a, s); break;
+            case 1: launch_flux_t<TF, false, false, true >(d, pr, a, s); break;
+            case 2: launch_flux_t<TF, false, true,  false>(d, pr, a, s); break;
+            case 3: launch_flux_t<TF, false, true,  true >(d, pr, a, s); break;
+            case 4: launch_flux_t<TF, true,  false, false>(d, pr, a, s); break;
+            case 5: launch_flux_t<TF, true,  false, true >(d, pr, a, s); break;
+            case 6: launch_flux_t<TF, true,  true,  false>(d, pr, a, s); break;
+            default: launch_flux_t<TF, true, true,  true >(d, pr, a, s); break;
+        }
+    }
+
+    template void launch_tendency_flux<double>(const Dims&, const Prof<double>&, const TendArgs<double>&, bool, bool, bool, cudaStream_t);
+    template void launch_tendency_flux<float>(const Dims&, const Prof<float>&, const TendArgs<float>&, bool, bool, bool, cudaStream_t);
+}

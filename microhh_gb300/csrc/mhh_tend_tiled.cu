@@ -113,8 +113,8 @@ namespace mhh
         load_plane(PE(0), ev, d, i0, j0, k0-1, tid);
         load_plane(PE(1), ev, d, i0, j0, k0, tid);
 
-        const TF dxi = TF(d.dxi), dyi = TF(d.dyi);
-        const TF dxidxi = TF(a.dxidxi), dyidyi = TF(a.dyidyi);
+        const TF dxi = dxi_of<TF>(d), dyi = dyi_of<TF>(d);
+        const TF dxidxi = a.dxidxi_t, dyidyi = a.dyidyi_t;
         const TF visc = a.visc, svisc = a.svisc, tpri = a.tpri;
         const long long ij = col;
         TF ufb = 0, uft = 0, vfb = 0, vft = 0, sfb = 0, sft = 0;

@@ -109,7 +109,69 @@ def test_against_oracle_fp64(mhh, oracle_lib, name, make):
             assert max_err(a, b) <= 10 * tol, (name, n, nsteps, max_err(a, b))
 
 
-def test_fp32_form_against_fp64_oracle(mhh, oracle_lib):
+@pytest.mark.parametrize("variant", [1, 2], ids=["tiled", "flux"])
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
+def test_tendency_variants_fp64(mhh, path, variant):
+    """The blocked LES tendency kernels (tiled planes; flux form) run on
+    double fields against the golden fixtures at the FP64 tolerance."""
+    name = os.path.basename(path)[:-4]
+    g = np.load(path)
+    case = golden_case(name)
+    mhh.set_option("tendency_kernel", variant)
+    try:
+        m = mhh.Model(case, precision=mhh.FP64)
+        for n in case.prognostic_names():
+            m.set(n, g["in_" + n])
+        m.run_substeps(3, fused=True)
+        for n in case.prognostic_names() + ["p"]:
+            err = rel_err(m.get(n), g["out_" + n])
+            assert err <= TOL64, (name, n, err)
+    finally:
+        mhh.set_option("tendency_kernel", -1)
+
+
+@pytest.mark.parametrize("variant", [0, 2], ids=["percell", "flux"])
+def test_tendency_chunks_and_partial_tiles_fp64(mhh, oracle_lib, variant):
+    """A grid whose x and y sizes are not multiples of the tile and whose
+    height spans three level chunks (the last one partial), against the
+    oracle."""
+    case = cases.drycbl(40, 20, 70, 4000., 2000., 2800., seed=24, noise_z=600.)
+    mhh.set_option("tendency_kernel", variant)
+    try:
+        m = mhh.Model(case, precision=mhh.FP64)
+        o = oracle_lib.model_from_case(case)
+        m.run_steps(1, fused=True)
+        o.run_substeps(3)
+        for n in case.prognostic_names() + ["p"]:
+            err = rel_err(m.get(n), o.get(n))
+            assert err <= TOL_LARGE, (n, err)
+    finally:
+        mhh.set_option("tendency_kernel", -1)
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
+def test_tdma_rescaled_recurrence_fp64(mhh, path):
+    """The rescaled Thomas recurrence of the float form (two FP64 FMAs per
+    cell), run on double fields, against the golden fixtures at the FP64
+    tolerance."""
+    name = os.path.basename(path)[:-4]
+    g = np.load(path)
+    case = golden_case(name)
+    mhh.set_option("tdma_kernel", 1)
+    try:
+        m = mhh.Model(case, precision=mhh.FP64)
+        for n in case.prognostic_names():
+            m.set(n, g["in_" + n])
+        m.run_substeps(3, fused=True)
+        for n in case.prognostic_names() + ["p"]:
+            err = rel_err(m.get(n), g["out_" + n])
+            assert err <= TOL64, (name, n, err)
+    finally:
+        mhh.set_option("tdma_kernel", -1)
+
+
+@pytest.mark.parametrize("variant", [0, 2], ids=["percell", "flux"])
+def test_fp32_form_against_fp64_oracle(mhh, oracle_lib, variant):
     """FP32 storage/stencils/FFTs with FP64 z-solve and reductions: one RK3
     step within 2e-3 of the FP64 oracle (relative to each field's maximum).
 
@@ -118,9 +180,13 @@ def test_fp32_form_against_fp64_oracle(mhh, oracle_lib):
     case = cases.drycbl(64, 48, 32, 6400., 4800., 3200., seed=31, noise_z=800.)
     # Start both from the same float-representable state.
     case.fields["th"] = case.fields["th"].astype(np.float32).astype(np.float64)
-    m = mhh.Model(case, precision=mhh.FP32)
+    mhh.set_option("tendency_kernel", variant)
+    try:
+        m = mhh.Model(case, precision=mhh.FP32)
+        m.run_steps(1, fused=True)
+    finally:
+        mhh.set_option("tendency_kernel", -1)
     o = oracle_lib.model_from_case(case)
-    m.run_steps(1, fused=True)
     o.run_substeps(3)
     for n in ("u", "v", "w"):
         err = rel_err(m.get(n), o.get(n))
