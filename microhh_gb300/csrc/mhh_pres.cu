@@ -273,9 +273,14 @@ namespace mhh
         extern __shared__ __align__(16) unsigned char smem_raw[];
         const int n = NFIX ? NFIX : pl.n;
         const int P = NFIX ? PFIX : Prt;
+        // Each buffer holds P complex sequences plus P elements of padding:
+        // viewed as 2P real sequences, the column (y) layout strides them by
+        // n + 1 so that a warp reading one element of 16+ sequences hits
+        // distinct banks.
         T2* buf0 = reinterpret_cast<T2*>(smem_raw);
-        T2* buf1 = buf0 + (size_t)P*n;
-        T2* tws = buf1 + (size_t)P*n;      // twiddle table (fixed path)
+        T2* buf1 = buf0 + (size_t)P*n + P;
+        T2* tws = buf1 + (size_t)P*n + P;  // twiddle table (fixed path)
+        const int ns = L.rows ? n : n + 1;  // real-sequence stride in shared memory
         const long long s0 = (long long)blockIdx.x*2*P;
         const int nloc = (int)min((long long)2*P, L.nseq - s0);
 
@@ -294,7 +299,7 @@ namespace mhh
             for (int e = threadIdx.x; e < tot; e += blockDim.x)
             {
                 const int ls = e / n, j = e - ls*n;
-                r1[e] = ls < nloc ? data[seq_base(L, s0 + ls, n) + j] : TF(0);
+                r1[ls*ns + j] = ls < nloc ? data[seq_base(L, s0 + ls, n) + j] : TF(0);
             }
         }
         else
@@ -302,7 +307,7 @@ namespace mhh
             for (int e = threadIdx.x; e < tot; e += blockDim.x)
             {
                 const int j = e / (2*P), ls = e - j*(2*P);
-                r1[ls*n + j] = ls < nloc ? data[seq_base(L, s0 + ls, n) + (long long)j*L.itot] : TF(0);
+                r1[ls*ns + j] = ls < nloc ? data[seq_base(L, s0 + ls, n) + (long long)j*L.itot] : TF(0);
             }
         }
         __syncthreads();
@@ -311,8 +316,8 @@ namespace mhh
         for (int e = threadIdx.x; e < P*n; e += blockDim.x)
         {
             const int q = e / n, k = e - q*n;
-            const TF* hx = r1 + (2*q)*n;
-            const TF* hy = r1 + (2*q+1)*n;
+            const TF* hx = r1 + (2*q)*ns;
+            const TF* hy = r1 + (2*q+1)*ns;
             T2 z;
             if (!INV)
             {
@@ -355,8 +360,8 @@ namespace mhh
         for (int e = threadIdx.x; e < P*n; e += blockDim.x)
         {
             const int q = e / n, k = e - q*n;
-            TF* ox = rout + (2*q)*n;
-            TF* oy = rout + (2*q+1)*n;
+            TF* ox = rout + (2*q)*ns;
+            TF* oy = rout + (2*q+1)*ns;
             if (!INV)
             {
                 if (k <= n/2)
@@ -383,7 +388,7 @@ namespace mhh
             for (int e = threadIdx.x; e < tot; e += blockDim.x)
             {
                 const int ls = e / n, j = e - ls*n;
-                if (ls < nloc) data[seq_base(L, s0 + ls, n) + j] = rout[e];
+                if (ls < nloc) data[seq_base(L, s0 + ls, n) + j] = rout[ls*ns + j];
             }
         }
         else
@@ -391,7 +396,7 @@ namespace mhh
             for (int e = threadIdx.x; e < tot; e += blockDim.x)
             {
                 const int j = e / (2*P), ls = e - j*(2*P);
-                if (ls < nloc) data[seq_base(L, s0 + ls, n) + (long long)j*L.itot] = rout[ls*n + j];
+                if (ls < nloc) data[seq_base(L, s0 + ls, n) + (long long)j*L.itot] = rout[ls*ns + j];
             }
         }
     }
@@ -412,7 +417,7 @@ namespace mhh
     template<typename TF, bool INV, int NF, int PF>
     static void launch_fixed(const FftPlan& pl, TF* data, SeqLayout L, TF scale, cudaStream_t s)
     {
-        const size_t smem = sizeof(typename C2<TF>::T)*((size_t)2*PF*NF + NF);
+        const size_t smem = sizeof(typename C2<TF>::T)*((size_t)2*(PF*NF + PF) + NF);
         const long long nblk = (L.nseq + 2*PF - 1) / (2*PF);
         cudaFuncSetAttribute(k_fft<TF, INV, NF, PF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         k_fft<TF, INV, NF, PF><<<(unsigned)nblk, 256, smem, s>>>(pl, data, L, PF, scale);
@@ -451,7 +456,7 @@ namespace mhh
         if (inverse ? launch_fixed_any<TF, true>(pl, data, L, scale, s) : launch_fixed_any<TF, false>(pl, data, L, scale, s))
             return;
         const int P = pairs_per_block<TF>(n, L.rows != 0);
-        const size_t smem = 2*sizeof(typename C2<TF>::T)*(size_t)P*n;
+        const size_t smem = 2*sizeof(typename C2<TF>::T)*((size_t)P*n + P);
         const long long nblk = (L.nseq + 2*P - 1) / (2*P);
         if (inverse)
         {
