@@ -222,6 +222,17 @@ int mhh_pres_2_exec(mhh_ctx* ctx, const mhh_fields* f, double sub_dt, cudaStream
 /* Pres_2<TF>::check_divergence (src/pres_2.cxx:97-105, :389-422): maximum
    absolute divergence, in double; synchronises. */
 int mhh_pres_2_get_divergence(mhh_ctx* ctx, const mhh_fields* f, double* div, cudaStream_t stream);
+
+/* The same maximum absolute divergence without any device allocation (no
+   counterpart in the reference).  For callers that must not allocate device
+   memory after set-up, e.g. a host that charges every device allocation
+   against a fixed HBM budget.  The scratch is a file-scope device array of
+   the library: jtot*ktot <= 262144 (2 MiB of row maxima), larger grids return
+   MHH_ERR_ARG.  The first call on each device looks up the array's address;
+   make it before any stream capture.  Calls on one device share the array,
+   so calls that overlap in time race and must be serialised by the caller.
+   Synchronises the stream. */
+int mhh_pres_2_get_divergence_noalloc(mhh_ctx* ctx, const mhh_fields* f, double* div, cudaStream_t stream);
 /* Halfcomplex x/y transforms of a packed itot*jtot*ktot array in place
    (FFT<TF>::exec_forward / exec_backward, src/fft.cxx:337-452). */
 int mhh_fft_forward(mhh_ctx* ctx, void* data, cudaStream_t stream);

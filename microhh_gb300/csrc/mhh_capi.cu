@@ -113,6 +113,14 @@ struct mhh_ctx
     double dnmul2;                // Diff_2 multiplier
 };
 
+namespace mhh
+{
+    const Dims& ctx_dims(const mhh_ctx* c) { return c->d; }
+    int ctx_precision(const mhh_ctx* c) { return c->prec; }
+    const Prof<double>& ctx_prof_double(const mhh_ctx* c) { return c->pd; }
+    const Prof<float>& ctx_prof_float(const mhh_ctx* c) { return c->pf; }
+}
+
 namespace
 {
     enum { P_Z, P_ZH, P_DZ, P_DZH, P_DZI, P_DZHI, P_RHO, P_RHOH, P_TH, P_THH, P_ZF, P_ZFH };

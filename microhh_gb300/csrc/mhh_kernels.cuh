@@ -7,6 +7,12 @@ namespace mhh
 {
     void count_launch(int n = 1);
     long long launch_count();
+
+    // Read-only view of a context for kernels in other translation units.
+    const Dims& ctx_dims(const mhh_ctx* c);
+    int ctx_precision(const mhh_ctx* c);
+    const Prof<double>& ctx_prof_double(const mhh_ctx* c);
+    const Prof<float>& ctx_prof_float(const mhh_ctx* c);
     // Kernel variant of the LES tendencies: 0 = one thread per cell with
     // cached global loads, 1 = tiled shared-memory planes marching in k,
     // 2 = flux form (every face flux once) marching in k; -1 = automatic
