@@ -123,6 +123,9 @@ long long mhh_launch_count(void);
    "tendency_kernel" 0 = one thread per cell, 1 = tiled planes marching in k,
    2 = flux form (each face flux computed once) marching in k, -1 = automatic
    (2 for FP32 contexts, 0 for FP64 contexts; the default);
+   "viscosity_kernel" 0 = one thread per cell, 1 = shared-memory planes
+   marching in k, -1 = automatic (1 for FP32 contexts, 0 for FP64; the
+   default; the neutral resolved-wall case always runs per cell);
    "tdma_kernel" 0 = the Thomas recurrence in the reference's operation order,
    1 = the rescaled recurrence (two FP64 FMAs per cell), -1 = automatic
    (0 for FP64 contexts, 1 for FP32 contexts; the default). */

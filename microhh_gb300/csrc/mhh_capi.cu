@@ -68,6 +68,9 @@ namespace mhh
     static int g_tend_variant = -1;
     int tendency_variant() { return g_tend_variant; }
     void set_tendency_variant(int v) { g_tend_variant = v; }
+    static int g_visc_variant = -1;
+    int viscosity_variant() { return g_visc_variant; }
+    void set_viscosity_variant(int v) { g_visc_variant = v; }
     static int g_tdma_variant = -1;
     int tdma_variant() { return g_tdma_variant; }
     void set_tdma_variant(int v) { g_tdma_variant = v; }
@@ -513,6 +516,12 @@ int mhh_set_option(const char* name, int value)
     {
         if (value < -1 || value > 2) return fail(MHH_ERR_ARG, "tendency_kernel is -1, 0, 1 or 2");
         set_tendency_variant(value);
+        return MHH_OK;
+    }
+    if (!std::strcmp(name, "viscosity_kernel"))
+    {
+        if (value < -1 || value > 1) return fail(MHH_ERR_ARG, "viscosity_kernel is -1, 0 or 1");
+        set_viscosity_variant(value);
         return MHH_OK;
     }
     if (!std::strcmp(name, "tdma_kernel"))

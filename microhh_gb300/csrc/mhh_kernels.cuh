@@ -59,6 +59,14 @@ namespace mhh
                                                 const TF* th, TF* evisc, const TF* mlen2, const double* dudz,
                                                 const double* dvdz, const double* dbdz, double cs, double tpr,
                                                 double visc, int mason, bool surf, bool thermo, cudaStream_t s);
+    template<typename TF> bool launch_viscosity_planes(const Dims& d, const Prof<TF>& pr, const TF* u, const TF* v,
+                                                       const TF* w, const TF* th, TF* evisc, const TF* mlen2,
+                                                       const double* dudz, const double* dvdz, const double* dbdz,
+                                                       double tpr, bool surf, bool thermo, cudaStream_t s);
+    // Viscosity kernel: 0 = per cell, 1 = shared-memory planes marching in k;
+    // -1 = automatic (1 for float fields, 0 for double fields).
+    int viscosity_variant();
+    void set_viscosity_variant(int v);
     template<typename TF> void launch_tendency(const Dims& d, const Prof<TF>& pr, const TendArgs<TF>& a, int adv, int dif,
                                                bool surf, bool scal, bool buoy, bool force, cudaStream_t s);
     template<typename TF> void launch_tendency_les(const Dims& d, const Prof<TF>& pr, const TendArgs<TF>& a,

@@ -256,15 +256,21 @@ namespace mhh
     {
         dim3 block(32, 8);
         dim3 grid((d.itot + 31)/32, (d.jtot + 7)/8, d.ktot);
-        if (surf && thermo)
-            k_viscosity<TF, true, true><<<grid, block, 0, s>>>(d, pr, u, v, w, th, evisc, mlen2, dudz, dvdz, dbdz, TF(cs), TF(tpr), TF(visc), mason);
-        else if (surf)
-            k_viscosity<TF, true, false><<<grid, block, 0, s>>>(d, pr, u, v, w, th, evisc, mlen2, dudz, dvdz, dbdz, TF(cs), TF(tpr), TF(visc), mason);
-        else if (thermo)
-            k_viscosity<TF, false, true><<<grid, block, 0, s>>>(d, pr, u, v, w, th, evisc, mlen2, dudz, dvdz, dbdz, TF(cs), TF(tpr), TF(visc), mason);
-        else
-            k_viscosity<TF, false, false><<<grid, block, 0, s>>>(d, pr, u, v, w, th, evisc, mlen2, dudz, dvdz, dbdz, TF(cs), TF(tpr), TF(visc), mason);
-        count_launch();
+        const int var = viscosity_variant() < 0 ? (sizeof(TF) == 4 ? 1 : 0) : viscosity_variant();
+        const bool planes = var == 1 && launch_viscosity_planes<TF>(d, pr, u, v, w, th, evisc, mlen2, dudz, dvdz, dbdz,
+                                                                    tpr, surf, thermo, s);
+        if (!planes)
+        {
+            if (surf && thermo)
+                k_viscosity<TF, true, true><<<grid, block, 0, s>>>(d, pr, u, v, w, th, evisc, mlen2, dudz, dvdz, dbdz, TF(cs), TF(tpr), TF(visc), mason);
+            else if (surf)
+                k_viscosity<TF, true, false><<<grid, block, 0, s>>>(d, pr, u, v, w, th, evisc, mlen2, dudz, dvdz, dbdz, TF(cs), TF(tpr), TF(visc), mason);
+            else if (thermo)
+                k_viscosity<TF, false, true><<<grid, block, 0, s>>>(d, pr, u, v, w, th, evisc, mlen2, dudz, dvdz, dbdz, TF(cs), TF(tpr), TF(visc), mason);
+            else
+                k_viscosity<TF, false, false><<<grid, block, 0, s>>>(d, pr, u, v, w, th, evisc, mlen2, dudz, dvdz, dbdz, TF(cs), TF(tpr), TF(visc), mason);
+            count_launch();
+        }
         if (!surf)
         {
             k_evisc_mirror<TF><<<(d.ijcells + 255)/256, 256, 0, s>>>(evisc, d);

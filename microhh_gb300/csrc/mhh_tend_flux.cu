@@ -17,7 +17,7 @@
 // horizontal faces of w and the vertical faces of u, v, s lie on the same
 // half level and share tau_xz and tau_yz.  The planes of each level (u, v, w,
 // s and the eddy viscosity with a 3-cell halo) are staged in shared memory
-// by cp.async one level ahead of their use; the 7-point vertical
+// by cp.async two levels ahead of their use; the 7-point vertical
 // neighbourhoods of the own column come from register queues.
 //
 // The arithmetic per face is that of the reference's kernels:
@@ -42,17 +42,20 @@ namespace mhh
         constexpr int NFACE = NFX*NFY;          // 297 face threads
         constexpr int NTHR = 320;
         constexpr int FKCHUNK = 32;
-        // Plane slots: u 3, v 3, w 2, s 2, evisc 3; level l of a field lives in
-        // slot base + l % n.
-        constexpr int SU = 0, SV = 3, SW = 6, SS = 8, SE = 10, NSLOT = 13;
+        // Plane slots: u 4, v 4, w 3, s 3, evisc 4; level l of a field lives
+        // in slot base + l % n.  Planes are prefetched two levels ahead.
+        constexpr int SU = 0, SV = 4, SW = 8, SS = 11, SE = 14, NSLOT = 18;
         constexpr int NGX = FTY*NFX;            // x-faces per level and field
         constexpr int NGY = NFY*FTX;            // y-faces per level and field
         constexpr int NEL1 = FPS - NTHR;        // threads that copy a second element
 
         template<typename TF> struct FluxOcc { static constexpr int v = sizeof(TF) == 4 ? 2 : 1; };
 
+        constexpr int NPROF = 8;                // per-level constants staged in shared memory
+        constexpr int PLEV = FKCHUNK + 2;       // levels m0 .. m0+FKCHUNK+1
+
         template<typename TF>
-        size_t flux_smem() { return sizeof(TF)*(size_t(NSLOT)*FPS + 2*4*(NGX + NGY)); }
+        size_t flux_smem() { return sizeof(TF)*(size_t(NSLOT)*FPS + 2*4*(NGX + NGY) + NPROF*PLEV); }
     }
 
     // Asynchronous global -> shared copy of one element; a copy with
@@ -96,10 +99,16 @@ namespace mhh
         extern __shared__ __align__(16) unsigned char smem_raw[];
         TF* sm = reinterpret_cast<TF*>(smem_raw);
         TF* gbase = sm + NSLOT*FPS;     // [2 buffers][4 fields][NGX] then [2][4][NGY]
+        TF* prof = gbase + 2*4*(NGX + NGY);   // [NPROF][PLEV]
 
+        // Warps 0-8 own the face rows fy = 0..8 (fx = lane); warp 9 owns the
+        // last face column fx = 32 of the rows fy = 0..7.  A warp thus reads
+        // one contiguous plane row.
         const int tid = threadIdx.x;
-        const int fx = tid % NFX, fy = tid / NFX;
-        const bool face = tid < NFACE;
+        const int warp = tid >> 5, lane = tid & 31;
+        const int fx = warp < NFY ? lane : FTX;
+        const int fy = warp < NFY ? warp : lane;
+        const bool face = warp < NFY || lane < FTY;
         const bool face_x = face && fy < FTY;
         const bool face_y = face && fx < FTX;
         const int i0 = d.istart + blockIdx.x*FTX;
@@ -129,6 +138,7 @@ namespace mhh
         }
         auto plane = [&](int slot, const TF* f, int l)
         {
+            if (l > d.kcells - 1) return;
             TF* dst = sm + slot*FPS;
             const TF* src = f + (long long)l*d.ijcells;
             cp_async_el(dst + e0, v0 ? src + go0 : f, v0);
@@ -147,13 +157,28 @@ namespace mhh
             return __ldg(f + col + (long long)l*d.ijcells);
         };
 
-        // Planes of the first iteration (m0) and of the next one.
+        // Per-level constants of the chunk: index l - m0 for level l.
         const int m0 = k0 - 1;
-        plane(SU + m0%3, u, m0); plane(SU + (m0+1)%3, u, m0+1); plane(SU + (m0+2)%3, u, m0+2);
-        plane(SV + m0%3, v, m0); plane(SV + (m0+1)%3, v, m0+1); plane(SV + (m0+2)%3, v, m0+2);
-        plane(SW + (m0+1)%2, w, m0+1); plane(SW + (m0+2)%2, w, m0+2);
-        plane(SE + m0%3, ev, m0); plane(SE + (m0+1)%3, ev, m0+1); plane(SE + (m0+2)%3, ev, m0+2);
-        if (SCAL) { plane(SS + m0%2, s, m0); plane(SS + (m0+1)%2, s, m0+1); }
+        for (int q = tid; q < PLEV; q += NTHR)
+        {
+            const int l = min(m0 + q, d.kcells - 1);
+            prof[0*PLEV + q] = pr.dzhi[l];
+            prof[1*PLEV + q] = pr.rhorefh[l];
+            prof[2*PLEV + q] = pr.rhoref[l];
+            prof[3*PLEV + q] = pr.dzi[l];
+            prof[4*PLEV + q] = TF(GRAV)/pr.threfh[l];
+            prof[7*PLEV + q] = pr.threfh[l];
+            prof[5*PLEV + q] = pr.zfac[l];
+            prof[6*PLEV + q] = pr.zfach[l];
+        }
+
+        // Planes of the first three iterations (m0 .. m0+2).
+        for (int l = m0; l <= m0+3; ++l)
+        {
+            plane(SU + l%4, u, l); plane(SV + l%4, v, l); plane(SE + l%4, ev, l);
+            if (l > m0) plane(SW + l%3, w, l);
+            if (SCAL && l < m0+3) plane(SS + l%3, s, l);
+        }
         cp_async_commit();
 
         // Register queues of the own column: u, v, s hold levels m-2 .. m+3,
@@ -190,14 +215,14 @@ namespace mhh
             const int buf = (m - m0) & 1;
             TF* gx = gbase + buf*4*NGX;
             TF* gy = gbase + 2*4*NGX + buf*4*NGY;
-            const TF* U0 = sm + (SU + m%3)*FPS + pc;
-            const TF* U1 = sm + (SU + (m+1)%3)*FPS + pc;
-            const TF* V0 = sm + (SV + m%3)*FPS + pc;
-            const TF* V1 = sm + (SV + (m+1)%3)*FPS + pc;
-            const TF* W1 = sm + (SW + (m+1)%2)*FPS + pc;
-            const TF* S0 = sm + (SS + m%2)*FPS + pc;
-            const TF* E0 = sm + (SE + m%3)*FPS + pc;
-            const TF* E1 = sm + (SE + (m+1)%3)*FPS + pc;
+            const TF* U0 = sm + (SU + m%4)*FPS + pc;
+            const TF* U1 = sm + (SU + (m+1)%4)*FPS + pc;
+            const TF* V0 = sm + (SV + m%4)*FPS + pc;
+            const TF* V1 = sm + (SV + (m+1)%4)*FPS + pc;
+            const TF* W1 = sm + (SW + (m+1)%3)*FPS + pc;
+            const TF* S0 = sm + (SS + m%3)*FPS + pc;
+            const TF* E0 = sm + (SE + m%4)*FPS + pc;
+            const TF* E1 = sm + (SE + (m+1)%4)*FPS + pc;
             #define PL(P, dx, dy) (P)[(dy)*FPW + (dx)]
 
             const bool write = cell && m >= k0;
@@ -219,7 +244,8 @@ namespace mhh
                 if (SCAL || BUOY) ns = colval(s, m+4);
             }
 
-            const TF dzhi1 = pr.dzhi[m+1];
+            const int lq = m + 1 - m0;      // index of level m+1 in prof
+            const TF dzhi1 = prof[0*PLEV + lq];
 
             // ---- faces: shear stresses and total fluxes ----
             TF txz = 0, tyz = 0;
@@ -297,7 +323,7 @@ namespace mhh
             {
                 const int kf = m + 1;
                 const int ot = face_order_full(d, kf);
-                const TF rhoh1 = pr.rhorefh[kf];
+                const TF rhoh1 = prof[1*PLEV + lq];
                 // u and v: diffusive flux from the shear stress of the same
                 // face, or the surface model's flux at the walls.
                 const TF du = (SURF && kf == d.kstart) ? -ufb : ((SURF && kf == d.kend) ? -uft : txz);
@@ -314,37 +340,40 @@ namespace mhh
                 if (kf < d.kend)
                 {
                     const int ow = face_order_w(d, kf);
-                    const TF dw = TF(2)*(PL(E1,0,0) + visc)*(qw[3] - qw[2])*pr.dzi[kf];
+                    const TF dw = TF(2)*(PL(E1,0,0) + visc)*(qw[3] - qw[2])*prof[3*PLEV + lq];
                     TF aw;
                     if (ow == 6) aw = adv6(i2(qw[2], qw[3]), qw[0], qw[1], qw[2], qw[3], qw[4], qw[5]);
                     else if (ow == 4) aw = i2(qw[2], qw[3])*i4ws(qw[1], qw[2], qw[3], qw[4])
                                          - fabs(i2(qw[2], qw[3]))*i3ws(qw[1], qw[2], qw[3], qw[4]);
                     else aw = i2(qw[2], qw[3])*i2(qw[2], qw[3]);
-                    gzw_t = pr.rhoref[kf]*(dw - aw);
+                    gzw_t = prof[2*PLEV + lq]*(dw - aw);
                 }
                 if (BUOY && wlev)
-                    buoy = TF(GRAV)/pr.threfh[kf]*(i2(qs[2], qs[3]) - pr.threfh[kf]);
+                    buoy = prof[4*PLEV + lq]*(i2(qs[2], qs[3]) - prof[7*PLEV + lq]);
             }
             #undef PL
 
-            cp_async_wait_all();
+            // The planes of iteration m+1 were issued two iterations ago; the
+            // last iteration's group may stay in flight.
+            asm volatile("cp.async.wait_group 1;\n" ::: "memory");
             __syncthreads();
 
-            // Planes of iteration m+2 into the slots that iteration m freed.
-            if (m + 2 < k1)
+            // Planes first used by iteration m+3 into the slots that
+            // iteration m freed.
+            if (m + 3 < k1)
             {
-                plane(SU + (m+3)%3, u, m+3);
-                plane(SV + (m+3)%3, v, m+3);
-                plane(SW + (m+3)%2, w, m+3);
-                plane(SE + (m+3)%3, ev, m+3);
-                if (SCAL) plane(SS + (m+2)%2, s, m+2);
+                plane(SU + (m+4)%4, u, m+4);
+                plane(SV + (m+4)%4, v, m+4);
+                plane(SW + (m+4)%3, w, m+4);
+                plane(SE + (m+4)%4, ev, m+4);
+                if (SCAL) plane(SS + (m+3)%3, s, m+3);
             }
             cp_async_commit();
 
             if (write)
             {
                 const int gx0 = gxi, gy0 = gyi;
-                const TF zf = pr.zfac[m];
+                const TF zf = prof[5*PLEV + lq - 1];
                 a.ut[c] = tu + (gx[0*NGX + gx0 + 1] - gx[0*NGX + gx0])*dxi
                              + (gy[0*NGY + gy0 + FTX] - gy[0*NGY + gy0])*dyi + (gzu_t - gzu_b)*zf;
                 a.vt[c] = tv + (gx[1*NGX + gx0 + 1] - gx[1*NGX + gx0])*dxi
@@ -352,7 +381,7 @@ namespace mhh
                 if (wlev)
                     a.wt[c + d.ijcells] = tw + (gx[2*NGX + gx0 + 1] - gx[2*NGX + gx0])*dxi
                                              + (gy[2*NGY + gy0 + FTX] - gy[2*NGY + gy0])*dyi
-                                             + (gzw_t - gzw_b)*pr.zfach[m+1] + buoy;
+                                             + (gzw_t - gzw_b)*prof[6*PLEV + lq] + buoy;
                 if (SCAL)
                     a.st[c] = ts + (gx[3*NGX + gx0 + 1] - gx[3*NGX + gx0])*dxi
                                  + (gy[3*NGY + gy0 + FTX] - gy[3*NGY + gy0])*dyi + (gzs_t - gzs_b)*zf;

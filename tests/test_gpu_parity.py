@@ -130,6 +130,28 @@ def test_tendency_variants_fp64(mhh, path, variant):
         mhh.set_option("tendency_kernel", -1)
 
 
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
+def test_viscosity_planes_fp64(mhh, path):
+    """The plane-staged eddy-viscosity kernel on double fields against the
+    golden fixtures (evisc at its own tolerance, the rest at FP64)."""
+    name = os.path.basename(path)[:-4]
+    g = np.load(path)
+    case = golden_case(name)
+    mhh.set_option("viscosity_kernel", 1)
+    try:
+        m = mhh.Model(case, precision=mhh.FP64)
+        for n in case.prognostic_names():
+            m.set(n, g["in_" + n])
+        m.run_substeps(3, fused=True)
+        for key in g.files:
+            if key.startswith("out_"):
+                n = key[4:]
+                err = rel_err(m.get(n), g[key])
+                assert err <= (TOL_EVISC if n == "evisc" else TOL64), (name, n, err)
+    finally:
+        mhh.set_option("viscosity_kernel", -1)
+
+
 @pytest.mark.parametrize("variant", [0, 2], ids=["percell", "flux"])
 def test_tendency_chunks_and_partial_tiles_fp64(mhh, oracle_lib, variant):
     """A grid whose x and y sizes are not multiples of the tile and whose
@@ -137,6 +159,7 @@ def test_tendency_chunks_and_partial_tiles_fp64(mhh, oracle_lib, variant):
     oracle."""
     case = cases.drycbl(40, 20, 70, 4000., 2000., 2800., seed=24, noise_z=600.)
     mhh.set_option("tendency_kernel", variant)
+    mhh.set_option("viscosity_kernel", 1 if variant == 2 else 0)
     try:
         m = mhh.Model(case, precision=mhh.FP64)
         o = oracle_lib.model_from_case(case)
@@ -147,6 +170,7 @@ def test_tendency_chunks_and_partial_tiles_fp64(mhh, oracle_lib, variant):
             assert err <= TOL_LARGE, (n, err)
     finally:
         mhh.set_option("tendency_kernel", -1)
+        mhh.set_option("viscosity_kernel", -1)
 
 
 @pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
