@@ -48,14 +48,16 @@ def peak_hbm():
 
 
 def ncu_traffic(kernel):
-    """Per-launch DRAM bytes of `kernel` from the committed ncu summary, or None."""
-    path = os.path.join(ROOT, "profiles", "ncu_traffic.md")
-    try:
-        for line in open(path):
-            if line.startswith("traffic_per_launch_bytes") and f" {kernel} " in line:
-                return float(line.split()[-1])
-    except OSError:
-        pass
+    """Per-launch DRAM bytes of kernel group `kernel` at the bench size, from
+    the committed ncu summaries (profiles/traffic_*.txt), or None."""
+    import glob
+    for path in sorted(glob.glob(os.path.join(ROOT, "profiles", "traffic_*.txt"))):
+        try:
+            for line in open(path):
+                if line.startswith("traffic_per_launch_bytes") and f" {kernel} " in line:
+                    return float(line.split()[-1])
+        except OSError:
+            pass
     return None
 
 

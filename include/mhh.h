@@ -16,7 +16,7 @@
  * reductions in double).
  *
  * Each entry point names the reference member function it replaces (paths
- * relative to the MicroHH source tree); see INTEGRATION.md for the bindings.
+ * relative to the MicroHH source tree).
  */
 #ifndef MHH_H
 #define MHH_H

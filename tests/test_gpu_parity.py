@@ -2,7 +2,7 @@
 
 All calls go through the C-ABI (libmhh_gb300.so) and the host layer
 (libmhh_host.so).  FP64: 1e-12 relative per field after one RK3 step (the
-tolerance of the spec parity requirement).  FP32 form: compared with the
+parity requirement of the FP64 path against the reference's FP64 CPU build).  FP32 form: compared with the
 FP64 oracle at the tolerance stated per test.
 """
 import glob
