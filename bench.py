@@ -330,16 +330,45 @@ def run_ours(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def run_form(args):
+    """The batching (64-member ensemble) and serving forms on one GPU."""
+    # Many concurrent streams: let each map to its own hardware queue (the
+    # default of 8 would serialise streams that share one).  Read when the
+    # CUDA context is created, so it is set before the first CUDA call.
+    os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+    import microhh_gb300 as mhh
+    from microhh_gb300 import forms
+    if args.form == "ensemble":
+        r = forms.ensemble_workload(mhh)
+        line = {"metric": "ensemble member-cell RK3 steps/s", "value": r["graphs"], "unit": "cell-steps/s",
+                "n_gpus": 1, "higher_is_better": True, "form": "ensemble", "dtype": "f32 (FP64 z-solve)",
+                "data": "synthetic (seeded dry CBL members)", "config": {"workload": r["workload"]},
+                "detail": r}
+    else:
+        r = forms.serve_workload(mhh)
+        line = {"metric": "served cell RK3 steps/s", "value": r["saturated"]["continuous"]["throughput"],
+                "unit": "cell-steps/s", "n_gpus": 1, "higher_is_better": True, "form": "serve",
+                "dtype": "f32 (FP64 z-solve)", "data": "synthetic (seeded dry CBL jobs)",
+                "config": {"workload": r["workload"]}, "detail": r}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=512)
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--form", default="step", choices=["step", "ensemble", "serve"],
+                    help="step: the time-step throughput (default); ensemble / serve: the batching and "
+                         "serving forms, one JSON line each")
     args = ap.parse_args()
+    if args.form != "step":
+        run_form(args)
+        return
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
     if args.impl == "reference":

@@ -117,6 +117,14 @@ int mhh_ctx_get_profile(const mhh_ctx* ctx, const char* name, double* out);
 const char* mhh_last_error(void);
 /* Kernels this library launched since load (for launch accounting). */
 long long mhh_launch_count(void);
+/* Adds n to that count: a driver that replays a captured CUDA graph adds the
+   graph's kernel nodes per replay (no counterpart in the reference). */
+int mhh_launch_count_add(long long n);
+/* Device memory the context allocated (measured at creation), and an upper
+   estimate of it from the grid alone, for admission by memory budget (no
+   counterpart in the reference). */
+int mhh_ctx_device_bytes(const mhh_ctx* ctx, size_t* bytes);
+int mhh_ctx_estimate_bytes(const mhh_grid_desc* desc, int precision, size_t* bytes);
 
 /* Process-wide kernel options (no counterpart in the reference; the
    reference picks kernel variants through its Kernel Launcher wisdom files):
@@ -130,6 +138,13 @@ long long mhh_launch_count(void);
    1 = the rescaled recurrence (two FP64 FMAs per cell), -1 = automatic
    (0 for FP64 contexts, 1 for FP32 contexts; the default). */
 int mhh_set_option(const char* name, int value);
+/* "tendency_kchunk" / "viscosity_kchunk": levels per block of the marching
+   kernels, 4, 8, 16, 32 or 64, or 0 (the default: 32, halved down to 8 while
+   the grid would give fewer than two blocks per SM). */
+/* The same options for one context, overriding the process-wide value;
+   -2 returns to it (no counterpart in the reference; used by the ensemble
+   autotuner to pick variants and level chunks per grid size). */
+int mhh_ctx_set_option(mhh_ctx* ctx, const char* name, int value);
 
 /* Live per-kernel-group timing with CUDA events recorded on the launching
    stream (no counterpart in the reference, which has no event timing):
@@ -240,6 +255,12 @@ int mhh_pres_2_get_divergence_noalloc(mhh_ctx* ctx, const mhh_fields* f, double*
    (FFT<TF>::exec_forward / exec_backward, src/fft.cxx:337-452). */
 int mhh_fft_forward(mhh_ctx* ctx, void* data, cudaStream_t stream);
 int mhh_fft_backward(mhh_ctx* ctx, void* data, cudaStream_t stream);
+
+/* Horizontal mean and variance (about the mean) of every level of a 3-D
+   field, kcells values each, in double (Field3d_operators<TF>::
+   calc_mean_profile, src/field3d_operators.cxx:46-67, with the variance of
+   the statistics' second moments); synchronises. */
+int mhh_stats_profile(mhh_ctx* ctx, const void* field, double* mean, double* var, cudaStream_t stream);
 
 /* ---------------------------------------------------------------------- */
 /* Time integration                                                        */

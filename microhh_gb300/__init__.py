@@ -149,6 +149,27 @@ def load():
     _declare(host, "mhh_model_synchronize", I, [P])
     _declare(host, "mhh_model_get_device_fields", I, [P, ctypes.POINTER(Fields), ctypes.POINTER(BcFields)])
     _declare(host, "mhh_model_get_ctx", P, [P])
+    # Ensembles and the server (include/mhh_batch.h)
+    _declare(host, "mhh_batch_last_error", ctypes.c_char_p, [])
+    _declare(host, "mhh_ensemble_create", I, [ctypes.POINTER(P)])
+    _declare(host, "mhh_ensemble_add", I, [P, P])
+    _declare(host, "mhh_ensemble_autotune", I, [P, ctypes.c_char_p, I])
+    _declare(host, "mhh_ensemble_run_steps", I, [P, I, I])
+    _declare(host, "mhh_ensemble_synchronize", I, [P])
+    _declare(host, "mhh_ensemble_destroy", I, [P])
+    _declare(host, "mhh_server_create", I, [D, I, ctypes.POINTER(P)])
+    _declare(host, "mhh_server_submit", I, [P, ctypes.c_char_p, dp, I, I, I, D, I, ctypes.POINTER(I)])
+    _declare(host, "mhh_server_set_initial", I, [P, I, ctypes.c_char_p, dp])
+    _declare(host, "mhh_server_run", I, [P, I])
+    _declare(host, "mhh_server_job_times", I, [P, I, dp, dp, dp])
+    _declare(host, "mhh_server_get_result", I, [P, I, ctypes.c_char_p, dp])
+    _declare(host, "mhh_server_peak_bytes", I, [P, dp])
+    _declare(host, "mhh_server_progress", I, [P, dp, dp, I, ctypes.POINTER(I)])
+    _declare(host, "mhh_server_destroy", I, [P])
+    _declare(kern, "mhh_ctx_set_option", I, [P, ctypes.c_char_p, I])
+    _declare(kern, "mhh_stats_profile", I, [P, P, dp, dp, S])
+    _declare(kern, "mhh_ctx_device_bytes", I, [P, ctypes.POINTER(ctypes.c_size_t)])
+    _declare(kern, "mhh_launch_count_add", I, [ctypes.c_longlong])
     _kern, _host = kern, host
     return kern, host
 
@@ -156,7 +177,7 @@ def load():
 def check(rc, what="mhh"):
     if rc != 0:
         kern, host = load()
-        msg = host.mhh_model_last_error() or kern.mhh_last_error() or b""
+        msg = host.mhh_batch_last_error() or host.mhh_model_last_error() or kern.mhh_last_error() or b""
         raise MhhError(f"{what} failed ({rc}): {msg.decode(errors='replace')}")
 
 
@@ -296,6 +317,17 @@ class Model:
     def synchronize(self):
         check(self.host.mhh_model_synchronize(self.h))
 
+    def profile_stats(self, name):
+        """Horizontal mean and variance of every level of field `name`
+        (kcells values each), computed on the device in double."""
+        self.synchronize()
+        f, _ = self.device_fields()
+        ptr = {"u": f.u, "v": f.v, "w": f.w, "th": f.s, "p": f.p, "evisc": f.evisc}[name]
+        mean = np.empty(self.grid.kcells)
+        var = np.empty(self.grid.kcells)
+        check(self.kern.mhh_stats_profile(self.ctx(), ptr, _dptr(mean), _dptr(var), None), "stats_profile")
+        return mean, var
+
     def device_fields(self):
         f, b = Fields(), BcFields()
         check(self.host.mhh_model_get_device_fields(self.h, ctypes.byref(f), ctypes.byref(b)))
@@ -303,3 +335,109 @@ class Model:
 
     def ctx(self):
         return self.host.mhh_model_get_ctx(self.h)
+
+
+ENS_SEQUENTIAL, ENS_STREAMS, ENS_GRAPHS = 0, 1, 2
+SERVE_FIFO, SERVE_CONTINUOUS = 0, 1
+
+
+class Ensemble:
+    """Models of uneven sizes advanced together (include/mhh_batch.h).  The
+    members stay owned by the caller and must outlive the ensemble."""
+
+    def __init__(self, members=()):
+        kern, host = load()
+        self.host = host
+        h = ctypes.c_void_p()
+        check(host.mhh_ensemble_create(ctypes.byref(h)), "ensemble_create")
+        self.h = h
+        self.members = []
+        for m in members:
+            self.add(m)
+
+    def add(self, model):
+        check(self.host.mhh_ensemble_add(self.h, model.h), "ensemble_add")
+        self.members.append(model)
+
+    def autotune(self):
+        buf = ctypes.create_string_buffer(4096)
+        check(self.host.mhh_ensemble_autotune(self.h, buf, len(buf)), "ensemble_autotune")
+        return buf.value.decode()
+
+    def run_steps(self, n, mode=ENS_GRAPHS):
+        check(self.host.mhh_ensemble_run_steps(self.h, n, mode), "ensemble_run_steps")
+
+    def synchronize(self):
+        check(self.host.mhh_ensemble_synchronize(self.h), "ensemble_synchronize")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.host.mhh_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Simulation jobs admitted by device-memory budget (include/mhh_batch.h)."""
+
+    def __init__(self, budget_bytes, max_active):
+        kern, host = load()
+        self.host = host
+        h = ctypes.c_void_p()
+        check(host.mhh_server_create(float(budget_bytes), int(max_active), ctypes.byref(h)), "server_create")
+        self.h = h
+        self.cells = []
+
+    def submit(self, case, nsteps, arrival=0.0, precision=FP32, keep=False):
+        z = np.ascontiguousarray(case.z, dtype=np.float64)
+        jid = ctypes.c_int()
+        check(self.host.mhh_server_submit(self.h, case.to_ini().encode(), _dptr(z), len(z), precision, int(nsteps),
+                                          float(arrival), 1 if keep else 0, ctypes.byref(jid)), "server_submit")
+        for n in case.prognostic_names():
+            a = np.ascontiguousarray(case.embed(case.fields[n]), dtype=np.float64)
+            check(self.host.mhh_server_set_initial(self.h, jid.value, n.encode(), _dptr(a)), "server_set_initial")
+        self.cells.append(case.itot * case.jtot * case.ktot * int(nsteps))
+        return jid.value
+
+    def run(self, mode=SERVE_CONTINUOUS):
+        check(self.host.mhh_server_run(self.h, mode), "server_run")
+
+    def times(self, job):
+        a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        check(self.host.mhh_server_job_times(self.h, job, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return a.value, b.value, c.value
+
+    def result(self, job, name, shape):
+        out = np.empty(shape, dtype=np.float64)
+        check(self.host.mhh_server_get_result(self.h, job, name.encode(), _dptr(out)), "server_get_result")
+        return out
+
+    def progress(self):
+        """(times, cells) of every completed step of the last run."""
+        n = ctypes.c_int()
+        check(self.host.mhh_server_progress(self.h, None, None, 0, ctypes.byref(n)))
+        t = np.empty(n.value)
+        c = np.empty(n.value)
+        check(self.host.mhh_server_progress(self.h, _dptr(t), _dptr(c), n.value, ctypes.byref(n)))
+        return t, c
+
+    def peak_bytes(self):
+        v = ctypes.c_double()
+        check(self.host.mhh_server_peak_bytes(self.h, ctypes.byref(v)))
+        return v.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.host.mhh_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -71,10 +71,26 @@ namespace mhh
     static int g_visc_variant = -1;
     int viscosity_variant() { return g_visc_variant; }
     void set_viscosity_variant(int v) { g_visc_variant = v; }
+    static int g_tend_kchunk = 0, g_visc_kchunk = 0;
     static int g_tdma_variant = -1;
     int tdma_variant() { return g_tdma_variant; }
     void set_tdma_variant(int v) { g_tdma_variant = v; }
     long long launch_count() { return g_launches.load(); }
+
+    int auto_kchunk(int requested, long long tiles, int ktot)
+    {
+        if (requested > 0) return requested;
+        static const int nsm = []
+        {
+            int dev = 0, n = 0;
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+            return n > 0 ? n : 152;
+        }();
+        int kc = 32;
+        while (kc > 8 && tiles*((ktot + kc - 1)/kc) < 2LL*nsm) kc /= 2;
+        return kc;
+    }
 
     template<typename TF>
     __global__ void k_pres_out(Dims d, Prof<TF> pr, const TF* __restrict__ p,
@@ -110,7 +126,12 @@ struct mhh_ctx
     PresWork pw;
     SurfWork sw;
     int surf_ready;
+    // Per-context kernel choices (-2 = follow the process-wide option).
+    int opt_tend, opt_visc, opt_tdma, opt_tend_kchunk, opt_visc_kchunk;
+    size_t dev_bytes;               // device memory allocated by this context
+    cudaStream_t setup;             // set-up and release stream (stream-ordered allocations)
 
+    double* statbuf;              // 2*kcells: mean and variance profiles
     unsigned long long* red;      // device reduction word
     unsigned long long* red_host; // pinned host copy
     double dnmul2;                // Diff_2 multiplier
@@ -211,9 +232,11 @@ namespace
         std::vector<TF> tmp(kc);
         for (int q=0; q<12; ++q)
         {
-            if (cudaMalloc(&c->dprof[q], sizeof(TF)*kc) != cudaSuccess) return fail(MHH_ERR_CUDA, "cudaMalloc profiles");
+            if (cudaMallocAsync(&c->dprof[q], sizeof(TF)*kc, c->setup) != cudaSuccess)
+                return fail(MHH_ERR_CUDA, "cudaMallocAsync profiles");
             for (int k=0; k<kc; ++k) tmp[k] = TF(c->h[q][k]);
-            cudaMemcpy(c->dprof[q], tmp.data(), sizeof(TF)*kc, cudaMemcpyHostToDevice);
+            cudaMemcpyAsync(c->dprof[q], tmp.data(), sizeof(TF)*kc, cudaMemcpyHostToDevice, c->setup);
+            if (cudaStreamSynchronize(c->setup) != cudaSuccess) return fail(MHH_ERR_CUDA, "profiles");
         }
         Prof<TF> p;
         p.z = (const TF*)c->dprof[P_Z]; p.zh = (const TF*)c->dprof[P_ZH];
@@ -227,18 +250,36 @@ namespace
         return MHH_OK;
     }
 
+    // The kernel choices of a call on context c.
+    KernelOpts opts_of(const mhh_ctx* c)
+    {
+        KernelOpts o;
+        o.tend = c->opt_tend != -2 ? c->opt_tend : tendency_variant();
+        o.visc = c->opt_visc != -2 ? c->opt_visc : viscosity_variant();
+        o.tdma = c->opt_tdma != -2 ? c->opt_tdma : tdma_variant();
+        o.tend_kchunk = c->opt_tend_kchunk != -2 ? c->opt_tend_kchunk : g_tend_kchunk;
+        o.visc_kchunk = c->opt_visc_kchunk != -2 ? c->opt_visc_kchunk : g_visc_kchunk;
+        return o;
+    }
+
+    // Set-up allocations and copies go to the context's own stream with
+    // stream-ordered allocation, so creating or destroying a context does not
+    // synchronise the work of other contexts on the device.
+    thread_local cudaStream_t g_setup = nullptr;
+
     template<typename T>
     int dalloc(T** p, size_t n, bool zero = true)
     {
-        if (cudaMalloc((void**)p, sizeof(T)*(n ? n : 1)) != cudaSuccess) return fail(MHH_ERR_CUDA, "cudaMalloc scratch");
-        if (zero) cudaMemset(*p, 0, sizeof(T)*(n ? n : 1));
+        if (cudaMallocAsync((void**)p, sizeof(T)*(n ? n : 1), g_setup) != cudaSuccess)
+            return fail(MHH_ERR_CUDA, "cudaMallocAsync scratch");
+        if (zero) cudaMemsetAsync(*p, 0, sizeof(T)*(n ? n : 1), g_setup);
         return MHH_OK;
     }
 
     int upload(double* dst, const std::vector<double>& v)
     {
-        return cudaMemcpy(dst, v.data(), sizeof(double)*v.size(), cudaMemcpyHostToDevice) == cudaSuccess
-            ? MHH_OK : fail(MHH_ERR_CUDA, "cudaMemcpy");
+        cudaMemcpyAsync(dst, v.data(), sizeof(double)*v.size(), cudaMemcpyHostToDevice, g_setup);
+        return cudaStreamSynchronize(g_setup) == cudaSuccess ? MHH_OK : fail(MHH_ERR_CUDA, "upload");
     }
 
     // Pressure-solver constants, src/pres_2.cxx:124-153.
@@ -247,10 +288,10 @@ namespace
         const Dims& d = c->d;
         const long long n = (long long)d.itot*d.jtot*d.ktot;
         int rc;
-        if ((rc = fft_plan_init(&c->pw.px, d.itot)) != MHH_OK) return fail(rc, "itot has a prime factor above 7");
-        if ((rc = fft_plan_init(&c->pw.py, d.jtot)) != MHH_OK) return fail(rc, "jtot has a prime factor above 7");
+        if ((rc = fft_plan_init(&c->pw.px, d.itot, c->setup)) != MHH_OK) return fail(rc, "itot has a prime factor above 7");
+        if ((rc = fft_plan_init(&c->pw.py, d.jtot, c->setup)) != MHH_OK) return fail(rc, "jtot has a prime factor above 7");
         const size_t tfb = c->prec == MHH_FP64 ? 8 : 4;
-        if (cudaMalloc(&c->pw.pk, tfb*n) != cudaSuccess) return fail(MHH_ERR_CUDA, "cudaMalloc pressure");
+        if (cudaMallocAsync(&c->pw.pk, tfb*n, c->setup) != cudaSuccess) return fail(MHH_ERR_CUDA, "cudaMallocAsync pressure");
         if ((rc = dalloc(&c->pw.work, (size_t)n, false))) return rc;
         if ((rc = dalloc(&c->pw.bmati, d.itot)) || (rc = dalloc(&c->pw.bmatj, d.jtot))) return rc;
         if ((rc = dalloc(&c->pw.a, d.ktot)) || (rc = dalloc(&c->pw.c, d.ktot))) return rc;
@@ -276,7 +317,7 @@ namespace
         if ((rc = upload(c->pw.bmati, bi)) || (rc = upload(c->pw.bmatj, bj))) return rc;
         if ((rc = upload(c->pw.a, a)) || (rc = upload(c->pw.c, cc))) return rc;
         if ((rc = upload(c->pw.dz2, dz2)) || (rc = upload(c->pw.dz2rho, dz2r))) return rc;
-        if ((rc = tdma_table(c->pw, d.itot, d.jtot, d.ktot))) return fail(rc, "tridiagonal table");
+        if ((rc = tdma_table(c->pw, d.itot, d.jtot, d.ktot, c->setup))) return fail(rc, "tridiagonal table");
         return MHH_OK;
     }
 
@@ -385,7 +426,7 @@ namespace
         }
         { Timed t("fft_x", s); launch_fft_x<TF>(c->pw.px, pk, d.jtot*d.ktot, false, 1., s); }
         { Timed t("fft_y", s); launch_fft_y<TF>(c->pw.py, pk, d.itot, d.jtot, d.ktot, false, 1., s); }
-        { Timed t("tdma", s); launch_tdma<TF>(d, c->pw, pk, s); }
+        { Timed t("tdma", s); launch_tdma<TF>(d, c->pw, pk, opts_of(c), s); }
         { Timed t("fft_y", s); launch_fft_y<TF>(c->pw.py, pk, d.itot, d.jtot, d.ktot, true, 1./d.jtot, s); }
         { Timed t("fft_x", s); launch_fft_x<TF>(c->pw.px, pk, d.jtot*d.ktot, true, 1./d.itot, s); }
         {
@@ -412,7 +453,7 @@ namespace
         const TF* ml2 = sizeof(TF) == 8 ? reinterpret_cast<const TF*>(c->sw.mlen2) : reinterpret_cast<const TF*>(c->sw.mlen2f);
         launch_viscosity<TF>(c->d, prof<TF>(c), CT<TF>(f->u), CT<TF>(f->v), CT<TF>(f->w), CT<TF>(f->s), T<TF>(f->evisc),
                              ml2, c->sw.dudz, c->sw.dvdz, c->sw.dbdz, c->phys.cs, c->phys.tpr, c->phys.visc,
-                             c->phys.swmason, surf, thermo, s);
+                             c->phys.swmason, surf, thermo, opts_of(c), s);
         return check_cuda("viscosity");
     }
 
@@ -489,7 +530,7 @@ namespace
         const bool buoy = scal && c->phys.thermo;
         {
             Timed t("tendency", s);
-            launch_tendency<TF>(d, pr, a, cfg->advec, cfg->diff, surf, scal, buoy, force, s);
+            launch_tendency<TF>(d, pr, a, cfg->advec, cfg->diff, surf, scal, buoy, force, opts_of(c), s);
         }
         const double cB[3] = {1./3., 15./16., 8./15.};
         int rc = pres_exec<TF>(c, f, cB[substep]*dt, false, s);
@@ -530,7 +571,50 @@ int mhh_set_option(const char* name, int value)
         set_tdma_variant(value);
         return MHH_OK;
     }
+    if (!std::strcmp(name, "tendency_kchunk") || !std::strcmp(name, "viscosity_kchunk"))
+    {
+        if (value != 0 && value != 4 && value != 8 && value != 16 && value != 32 && value != 64)
+            return fail(MHH_ERR_ARG, "kchunk is 0 (default), 4, 8, 16, 32 or 64");
+        (name[0] == 't' ? g_tend_kchunk : g_visc_kchunk) = value;
+        return MHH_OK;
+    }
     return fail(MHH_ERR_ARG, "unknown option");
+}
+
+int mhh_ctx_set_option(mhh_ctx* c, const char* name, int value)
+{
+    if (!c || !name) return fail(MHH_ERR_ARG, "NULL argument");
+    const bool reset = value == -2;
+    if (!std::strcmp(name, "tendency_kernel"))
+    {
+        if (!reset && (value < -1 || value > 2)) return fail(MHH_ERR_ARG, "tendency_kernel is -2, -1, 0, 1 or 2");
+        c->opt_tend = value;
+    }
+    else if (!std::strcmp(name, "viscosity_kernel"))
+    {
+        if (!reset && (value < -1 || value > 1)) return fail(MHH_ERR_ARG, "viscosity_kernel is -2, -1, 0 or 1");
+        c->opt_visc = value;
+    }
+    else if (!std::strcmp(name, "tdma_kernel"))
+    {
+        if (!reset && (value < -1 || value > 1)) return fail(MHH_ERR_ARG, "tdma_kernel is -2, -1, 0 or 1");
+        c->opt_tdma = value;
+    }
+    else if (!std::strcmp(name, "tendency_kchunk") || !std::strcmp(name, "viscosity_kchunk"))
+    {
+        if (!reset && value != 0 && value != 4 && value != 8 && value != 16 && value != 32 && value != 64)
+            return fail(MHH_ERR_ARG, "kchunk is -2, 0 (default), 4, 8, 16, 32 or 64");
+        (name[0] == 't' ? c->opt_tend_kchunk : c->opt_visc_kchunk) = value;
+    }
+    else
+        return fail(MHH_ERR_ARG, "unknown option");
+    return MHH_OK;
+}
+
+int mhh_launch_count_add(long long n)
+{
+    mhh::count_launch((int)n);
+    return MHH_OK;
 }
 
 int mhh_timing_enable(int on)
@@ -589,7 +673,18 @@ int mhh_ctx_create(const mhh_grid_desc* desc, const double* z, int precision, co
     if (double(desc->itot + 2*desc->igc)*(desc->jtot + 2*desc->jgc) > 2.0e9)
         return fail(MHH_ERR_ARG, "horizontal plane too large for 32-bit indexing");
 
+    size_t free0 = 0, total0 = 0;
+    cudaMemGetInfo(&free0, &total0);
     mhh_ctx* c = new mhh_ctx();
+    c->statbuf = nullptr;
+    c->opt_tend = c->opt_visc = c->opt_tdma = c->opt_tend_kchunk = c->opt_visc_kchunk = -2;
+    c->dev_bytes = 0;
+    if (cudaStreamCreateWithFlags(&c->setup, cudaStreamNonBlocking) != cudaSuccess)
+    {
+        delete c;
+        return fail(MHH_ERR_CUDA, "cudaStreamCreate");
+    }
+    g_setup = c->setup;
     std::memset(c->dprof, 0, sizeof(c->dprof));
     std::memset(&c->pw, 0, sizeof(c->pw));
     std::memset(&c->sw, 0, sizeof(c->sw));
@@ -619,6 +714,7 @@ int mhh_ctx_create(const mhh_grid_desc* desc, const double* z, int precision, co
     int rc = precision == MHH_FP64 ? upload_profiles<double>(c) : upload_profiles<float>(c);
     if (!rc) rc = setup_pres(c);
     if (!rc) rc = dalloc(&c->red, 1);
+    if (!rc) rc = dalloc(&c->statbuf, 2*(size_t)d.kcells);
     if (!rc && cudaMallocHost((void**)&c->red_host, sizeof(unsigned long long)) != cudaSuccess)
         rc = fail(MHH_ERR_CUDA, "cudaMallocHost");
     // Surface and viscosity arrays (always allocated; small).
@@ -643,7 +739,11 @@ int mhh_ctx_create(const mhh_grid_desc* desc, const double* z, int precision, co
         const std::vector<double> m2 = mixing_length2(c);
         std::vector<float> m2f(m2.begin(), m2.end());
         rc = dalloc(&c->sw.mlen2f, m2f.size());
-        if (!rc) cudaMemcpy(c->sw.mlen2f, m2f.data(), sizeof(float)*m2f.size(), cudaMemcpyHostToDevice);
+        if (!rc)
+        {
+            cudaMemcpyAsync(c->sw.mlen2f, m2f.data(), sizeof(float)*m2f.size(), cudaMemcpyHostToDevice, c->setup);
+            if (cudaStreamSynchronize(c->setup) != cudaSuccess) rc = fail(MHH_ERR_CUDA, "mixing length");
+        }
     }
     c->sw.zsl = c->h[P_Z][d.kstart];
     c->sw.thref_s = c->h[P_TH][d.kstart];
@@ -659,22 +759,59 @@ int mhh_ctx_create(const mhh_grid_desc* desc, const double* z, int precision, co
         }
         c->dnmul2 = dn;
     }
+    g_setup = nullptr;
     if (rc) { mhh_ctx_destroy(c); return rc; }
-    if (cudaDeviceSynchronize() != cudaSuccess) { mhh_ctx_destroy(c); return fail(MHH_ERR_CUDA, "set-up failed"); }
+    if (cudaStreamSynchronize(c->setup) != cudaSuccess) { mhh_ctx_destroy(c); return fail(MHH_ERR_CUDA, "set-up failed"); }
+    size_t free1 = 0, total1 = 0;
+    cudaMemGetInfo(&free1, &total1);
+    c->dev_bytes = free0 > free1 ? free0 - free1 : 0;
     *out = c;
+    return MHH_OK;
+}
+
+int mhh_ctx_device_bytes(const mhh_ctx* c, size_t* bytes)
+{
+    if (!c || !bytes) return fail(MHH_ERR_ARG, "NULL argument");
+    *bytes = c->dev_bytes;
+    return MHH_OK;
+}
+
+int mhh_ctx_estimate_bytes(const mhh_grid_desc* g, int precision, size_t* bytes)
+{
+    if (!g || !bytes) return fail(MHH_ERR_ARG, "NULL argument");
+    if (precision != MHH_FP64 && precision != MHH_FP32) return fail(MHH_ERR_ARG, "precision must be 64 or 32");
+    const double tf = precision == MHH_FP64 ? 8. : 4.;
+    const double icells = g->itot + 2*g->igc, jcells = g->jtot + 2*g->jgc, kcells = g->ktot + 2*g->kgc;
+    const double ij = icells*jcells;
+    const double n = double(g->itot)*g->jtot*g->ktot;
+    const double groups = double(g->itot/2 + 1)*(g->jtot/2 + 1)*g->ktot;
+    double b = 0.;
+    b += 12.*kcells*tf;                         // profiles
+    b += n*tf + n*8.;                           // packed pressure + work
+    b += groups*(8. + 8. + 8. + 4. + 8.);      // elimination tables
+    b += 2.*(g->itot + g->jtot)*(16. + 8.);    // twiddles
+    b += 12.*ij*8. + ij*4. + 2.*10000*4.;      // surface layer
+    b += 2.*kcells*8.;                          // mixing length
+    // cudaMalloc granularity: about 40 allocations of up to 2 MiB each.
+    b += 40.*2.*1024*1024;
+    *bytes = (size_t)b;
     return MHH_OK;
 }
 
 int mhh_ctx_destroy(mhh_ctx* c)
 {
     if (!c) return MHH_OK;
-    for (auto& p : c->dprof) if (p) cudaFree(p);
-    fft_plan_free(&c->pw.px); fft_plan_free(&c->pw.py);
+    // Stream-ordered release: the memory returns to the pool once the set-up
+    // stream reaches it; the caller has finished its own work on the fields.
+    for (auto& p : c->dprof) if (p) cudaFreeAsync(p, c->setup);
+    fft_plan_free(&c->pw.px, c->setup); fft_plan_free(&c->pw.py, c->setup);
     void* ptrs[] = {c->pw.pk, c->pw.work, c->pw.rtab, c->pw.gtab, c->pw.htab, c->pw.stab, c->pw.stabd, c->pw.bmati, c->pw.bmatj, c->pw.a, c->pw.c, c->pw.dz2, c->pw.dz2rho,
-                    c->red, c->sw.fm, c->sw.fh, c->sw.phim, c->sw.phih, c->sw.ustar, c->sw.obuk, c->sw.dudz, c->sw.dvdz, c->sw.dbdz, c->sw.dutot,
+                    c->red, c->statbuf, c->sw.fm, c->sw.fh, c->sw.phim, c->sw.phih, c->sw.ustar, c->sw.obuk, c->sw.dudz, c->sw.dvdz, c->sw.dbdz, c->sw.dutot,
                     c->sw.nobuk, c->sw.zL, c->sw.f, c->sw.mlen2, c->sw.mlen2f};
-    for (void* p : ptrs) if (p) cudaFree(p);
+    for (void* p : ptrs) if (p) cudaFreeAsync(p, c->setup);
     if (c->red_host) cudaFreeHost(c->red_host);
+    cudaStreamSynchronize(c->setup);
+    cudaStreamDestroy(c->setup);
     delete c;
     return MHH_OK;
 }
@@ -743,16 +880,18 @@ int mhh_boundary_surface_init(mhh_ctx* c, int thermo_bc)
         return fail(MHH_ERR_ARG, "surface model needs a flux or Dirichlet scalar BC");
     std::vector<float> zL, f;
     prepare_lut(zL, f, c->sw.zsl, c->phys.z0m, c->phys.z0h, thermo_bc);
-    cudaMemcpy(c->sw.zL, zL.data(), sizeof(float)*zL.size(), cudaMemcpyHostToDevice);
-    cudaMemcpy(c->sw.f, f.data(), sizeof(float)*f.size(), cudaMemcpyHostToDevice);
+    cudaStream_t s = c->setup;
+    cudaMemcpyAsync(c->sw.zL, zL.data(), sizeof(float)*zL.size(), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(c->sw.f, f.data(), sizeof(float)*f.size(), cudaMemcpyHostToDevice, s);
     const int n = c->d.ijcells;
     std::vector<double> obuk(n, DSMALL), ustar(n, 1e-2);
-    cudaMemcpy(c->sw.obuk, obuk.data(), sizeof(double)*n, cudaMemcpyHostToDevice);
-    cudaMemcpy(c->sw.ustar, ustar.data(), sizeof(double)*n, cudaMemcpyHostToDevice);
-    cudaMemset(c->sw.nobuk, 0, sizeof(int)*n);
-    cudaMemset(c->sw.dudz, 0, sizeof(double)*n);
-    cudaMemset(c->sw.dvdz, 0, sizeof(double)*n);
-    cudaMemset(c->sw.dbdz, 0, sizeof(double)*n);
+    cudaMemcpyAsync(c->sw.obuk, obuk.data(), sizeof(double)*n, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(c->sw.ustar, ustar.data(), sizeof(double)*n, cudaMemcpyHostToDevice, s);
+    cudaMemsetAsync(c->sw.nobuk, 0, sizeof(int)*n, s);
+    cudaMemsetAsync(c->sw.dudz, 0, sizeof(double)*n, s);
+    cudaMemsetAsync(c->sw.dvdz, 0, sizeof(double)*n, s);
+    cudaMemsetAsync(c->sw.dbdz, 0, sizeof(double)*n, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return fail(MHH_ERR_CUDA, "surface_init");
     c->surf_ready = 1;
     return check_cuda("surface_init");
 }
@@ -791,12 +930,12 @@ static int tend_only(mhh_ctx* c, const mhh_fields* f, const mhh_bcfields* bc, in
     if (c->prec == MHH_FP64)
     {
         TendArgs<double> a = tend_args<double>(c, f, bc); a.fbody = fbody;
-        launch_tendency<double>(c->d, c->pd, a, adv, dif, surf, scal && !buoy, buoy, force, s);
+        launch_tendency<double>(c->d, c->pd, a, adv, dif, surf, scal && !buoy, buoy, force, opts_of(c), s);
     }
     else
     {
         TendArgs<float> a = tend_args<float>(c, f, bc); a.fbody = float(fbody);
-        launch_tendency<float>(c->d, c->pf, a, adv, dif, surf, scal && !buoy, buoy, force, s);
+        launch_tendency<float>(c->d, c->pf, a, adv, dif, surf, scal && !buoy, buoy, force, opts_of(c), s);
     }
     return check_cuda("tendency");
 }
@@ -883,6 +1022,69 @@ int mhh_diff_2_get_dn(mhh_ctx* c, double dt, double* dn)
 {
     if (!c || !dn) return fail(MHH_ERR_ARG, "NULL argument");
     *dn = c->dnmul2*dt;
+    return MHH_OK;
+}
+
+}
+
+namespace mhh
+{
+    // Horizontal mean and variance of one level per block, in double (two
+    // passes over the level: the mean, then the mean squared deviation).
+    template<typename TF>
+    __global__ void __launch_bounds__(256)
+    k_profile(Dims d, const TF* __restrict__ a, double* __restrict__ mean, double* __restrict__ var)
+    {
+        const int k = blockIdx.x;
+        const int n = d.itot*d.jtot;
+        __shared__ double sm[8];
+        __shared__ double m_sh;
+        auto block_sum = [&](double v) -> double
+        {
+            for (int o=16; o>0; o>>=1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
+            __syncthreads();
+            double t = 0.;
+            if (threadIdx.x == 0) { for (int q=0; q<8; ++q) t += sm[q]; }
+            __syncthreads();
+            return t;
+        };
+        double s = 0.;
+        for (int q = threadIdx.x; q < n; q += blockDim.x)
+        {
+            const int j = q / d.itot, i = q - j*d.itot;
+            s += double(a[ijk(d, i + d.istart, j + d.jstart, k)]);
+        }
+        s = block_sum(s);
+        if (threadIdx.x == 0) m_sh = s/n;
+        __syncthreads();
+        const double m = m_sh;
+        double v = 0.;
+        for (int q = threadIdx.x; q < n; q += blockDim.x)
+        {
+            const int j = q / d.itot, i = q - j*d.itot;
+            const double x = double(a[ijk(d, i + d.istart, j + d.jstart, k)]) - m;
+            v += x*x;
+        }
+        v = block_sum(v);
+        if (threadIdx.x == 0) { mean[k] = m; var[k] = v/n; }
+    }
+}
+
+extern "C" {
+
+int mhh_stats_profile(mhh_ctx* c, const void* field, double* mean, double* var, cudaStream_t s)
+{
+    if (!c || !field || !mean || !var) return fail(MHH_ERR_ARG, "NULL argument");
+    const Dims& d = c->d;
+    if (c->prec == MHH_FP64) k_profile<double><<<d.kcells, 256, 0, s>>>(d, (const double*)field, c->statbuf, c->statbuf + d.kcells);
+    else k_profile<float><<<d.kcells, 256, 0, s>>>(d, (const float*)field, c->statbuf, c->statbuf + d.kcells);
+    count_launch();
+    int rc = check_cuda("stats_profile");
+    if (rc) return rc;
+    cudaMemcpyAsync(mean, c->statbuf, sizeof(double)*d.kcells, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(var, c->statbuf + d.kcells, sizeof(double)*d.kcells, cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return fail(MHH_ERR_CUDA, "stats_profile");
     return MHH_OK;
 }
 

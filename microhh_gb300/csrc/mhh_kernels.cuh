@@ -8,6 +8,19 @@ namespace mhh
     void count_launch(int n = 1);
     long long launch_count();
 
+    // Kernel choices of one call: variant switches (-1 = automatic) and the
+    // level-chunk height of the marching kernels (0 = default 32).
+    struct KernelOpts
+    {
+        int tend, visc, tdma;
+        int tend_kchunk, visc_kchunk;
+    };
+
+    // Level-chunk height of a marching kernel with `tiles` blocks per chunk
+    // row: the requested height, or for 0 the largest of 32, 16, 8 that still
+    // gives two blocks per SM (small grids get more, shorter chunks).
+    int auto_kchunk(int requested, long long tiles, int ktot);
+
     // Read-only view of a context for kernels in other translation units.
     const Dims& ctx_dims(const mhh_ctx* c);
     int ctx_precision(const mhh_ctx* c);
@@ -58,21 +71,23 @@ namespace mhh
     template<typename TF> void launch_viscosity(const Dims& d, const Prof<TF>& pr, const TF* u, const TF* v, const TF* w,
                                                 const TF* th, TF* evisc, const TF* mlen2, const double* dudz,
                                                 const double* dvdz, const double* dbdz, double cs, double tpr,
-                                                double visc, int mason, bool surf, bool thermo, cudaStream_t s);
+                                                double visc, int mason, bool surf, bool thermo, const KernelOpts& o,
+                                                cudaStream_t s);
     template<typename TF> bool launch_viscosity_planes(const Dims& d, const Prof<TF>& pr, const TF* u, const TF* v,
                                                        const TF* w, const TF* th, TF* evisc, const TF* mlen2,
                                                        const double* dudz, const double* dvdz, const double* dbdz,
-                                                       double tpr, bool surf, bool thermo, cudaStream_t s);
+                                                       double tpr, bool surf, bool thermo, int kchunk, cudaStream_t s);
     // Viscosity kernel: 0 = per cell, 1 = shared-memory planes marching in k;
     // -1 = automatic (1 for float fields, 0 for double fields).
     int viscosity_variant();
     void set_viscosity_variant(int v);
     template<typename TF> void launch_tendency(const Dims& d, const Prof<TF>& pr, const TendArgs<TF>& a, int adv, int dif,
-                                               bool surf, bool scal, bool buoy, bool force, cudaStream_t s);
+                                               bool surf, bool scal, bool buoy, bool force, const KernelOpts& o,
+                                               cudaStream_t s);
     template<typename TF> void launch_tendency_les(const Dims& d, const Prof<TF>& pr, const TendArgs<TF>& a,
                                                    bool surf, bool scal, bool buoy, cudaStream_t s);
     template<typename TF> void launch_tendency_flux(const Dims& d, const Prof<TF>& pr, const TendArgs<TF>& a,
-                                                    bool surf, bool scal, bool buoy, cudaStream_t s);
+                                                    bool surf, bool scal, bool buoy, int kchunk, cudaStream_t s);
     template<typename TF> void launch_rk3(TF* a, TF* at, const Dims& d, int substep, double dt, cudaStream_t s);
     template<typename TF> void launch_presout_rk3(const Dims& d, const Prof<TF>& pr, const TF* p, TF* u, TF* v, TF* w,
                                                   TF* s, TF* ut, TF* vt, TF* wt, TF* st, int substep, double dt,
@@ -91,8 +106,10 @@ namespace mhh
         float* tw_f;      // the same in float
     };
 
-    int fft_plan_init(FftPlan* pl, int n);
-    void fft_plan_free(FftPlan* pl);
+    // Set-up and release on a stream: allocations are stream-ordered
+    // (cudaMallocAsync / cudaFreeAsync), so neither synchronises the device.
+    int fft_plan_init(FftPlan* pl, int n, cudaStream_t s);
+    void fft_plan_free(FftPlan* pl, cudaStream_t s);
 
     struct PresWork
     {
@@ -119,14 +136,14 @@ namespace mhh
     int tdma_variant();
     void set_tdma_variant(int v);
 
-    int tdma_table(PresWork& pw, int itot, int jtot, int ktot);
+    int tdma_table(PresWork& pw, int itot, int jtot, int ktot, cudaStream_t s);
 
     template<typename TF> void launch_pres_in(const Dims& d, const Prof<TF>& pr, const TF* u, const TF* v, const TF* w,
                                               const TF* ut, const TF* vt, const TF* wt, TF* pk, double dti, cudaStream_t s);
     template<typename TF> void launch_fft_x(const FftPlan& pl, TF* data, int nrows, bool inverse, double scale, cudaStream_t s);
     template<typename TF> void launch_fft_y(const FftPlan& pl, TF* data, int itot, int jtot, int ktot, bool inverse,
                                             double scale, cudaStream_t s);
-    template<typename TF> void launch_tdma(const Dims& d, const PresWork& pw, TF* pk, cudaStream_t s);
+    template<typename TF> void launch_tdma(const Dims& d, const PresWork& pw, TF* pk, const KernelOpts& o, cudaStream_t s);
     template<typename TF> void launch_pres_scatter(const Dims& d, const TF* pk, TF* p, cudaStream_t s);
 
     // ---- surface layer (mhh_surface.cu) ----

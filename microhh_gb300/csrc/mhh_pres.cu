@@ -401,6 +401,10 @@ namespace mhh
         }
     }
 
+    // Dynamic shared-memory limit of the run-time-plan FFT (two buffers of at
+    // most 96 KB of sequences, plus padding).
+    constexpr int FFT_GENERIC_SMEM = 100*1024;
+
     template<typename TF>
     static int pairs_per_block(int n, bool rows)
     {
@@ -419,7 +423,9 @@ namespace mhh
     {
         const size_t smem = sizeof(typename C2<TF>::T)*((size_t)2*(PF*NF + PF) + NF);
         const long long nblk = (L.nseq + 2*PF - 1) / (2*PF);
-        cudaFuncSetAttribute(k_fft<TF, INV, NF, PF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        static const bool attr = cudaFuncSetAttribute(k_fft<TF, INV, NF, PF>,
+            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess;
+        (void)attr;
         k_fft<TF, INV, NF, PF><<<(unsigned)nblk, 256, smem, s>>>(pl, data, L, PF, scale);
     }
 
@@ -460,12 +466,16 @@ namespace mhh
         const long long nblk = (L.nseq + 2*P - 1) / (2*P);
         if (inverse)
         {
-            cudaFuncSetAttribute(k_fft<TF, true, 0, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            static const bool attr = cudaFuncSetAttribute(k_fft<TF, true, 0, 0>,
+                cudaFuncAttributeMaxDynamicSharedMemorySize, FFT_GENERIC_SMEM) == cudaSuccess;
+            (void)attr;
             k_fft<TF, true, 0, 0><<<(unsigned)nblk, 256, smem, s>>>(pl, data, L, P, scale);
         }
         else
         {
-            cudaFuncSetAttribute(k_fft<TF, false, 0, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            static const bool attr = cudaFuncSetAttribute(k_fft<TF, false, 0, 0>,
+                cudaFuncAttributeMaxDynamicSharedMemorySize, FFT_GENERIC_SMEM) == cudaSuccess;
+            (void)attr;
             k_fft<TF, false, 0, 0><<<(unsigned)nblk, 256, smem, s>>>(pl, data, L, P, scale);
         }
     }
@@ -485,7 +495,7 @@ namespace mhh
         (void)jtot;
     }
 
-    int fft_plan_init(FftPlan* pl, int n)
+    int fft_plan_init(FftPlan* pl, int n, cudaStream_t s)
     {
         std::memset(pl, 0, sizeof(*pl));
         pl->n = n;
@@ -503,17 +513,17 @@ namespace mhh
             td[2*k] = (double)cosl(ang); td[2*k+1] = (double)sinl(ang);
             tf[2*k] = (float)td[2*k]; tf[2*k+1] = (float)td[2*k+1];
         }
-        if (cudaMalloc(&pl->tw_d, sizeof(double)*2*n) != cudaSuccess) return MHH_ERR_CUDA;
-        if (cudaMalloc(&pl->tw_f, sizeof(float)*2*n) != cudaSuccess) return MHH_ERR_CUDA;
-        cudaMemcpy(pl->tw_d, td.data(), sizeof(double)*2*n, cudaMemcpyHostToDevice);
-        cudaMemcpy(pl->tw_f, tf.data(), sizeof(float)*2*n, cudaMemcpyHostToDevice);
-        return MHH_OK;
+        if (cudaMallocAsync((void**)&pl->tw_d, sizeof(double)*2*n, s) != cudaSuccess) return MHH_ERR_CUDA;
+        if (cudaMallocAsync((void**)&pl->tw_f, sizeof(float)*2*n, s) != cudaSuccess) return MHH_ERR_CUDA;
+        cudaMemcpyAsync(pl->tw_d, td.data(), sizeof(double)*2*n, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(pl->tw_f, tf.data(), sizeof(float)*2*n, cudaMemcpyHostToDevice, s);
+        return cudaStreamSynchronize(s) == cudaSuccess ? MHH_OK : MHH_ERR_CUDA;
     }
 
-    void fft_plan_free(FftPlan* pl)
+    void fft_plan_free(FftPlan* pl, cudaStream_t s)
     {
-        if (pl->tw_d) cudaFree(pl->tw_d);
-        if (pl->tw_f) cudaFree(pl->tw_f);
+        if (pl->tw_d) cudaFreeAsync(pl->tw_d, s);
+        if (pl->tw_f) cudaFreeAsync(pl->tw_f, s);
         pl->tw_d = nullptr; pl->tw_f = nullptr;
     }
 
@@ -874,28 +884,28 @@ namespace mhh
         }
     }
 
-    int tdma_table(PresWork& pw, int itot, int jtot, int ktot)
+    int tdma_table(PresWork& pw, int itot, int jtot, int ktot, cudaStream_t s)
     {
         pw.niu = itot/2 + 1;
         pw.nju = jtot/2 + 1;
         const size_t n = (size_t)pw.niu*pw.nju*ktot;
-        if (cudaMalloc(&pw.rtab, sizeof(double)*n) != cudaSuccess) return MHH_ERR_CUDA;
-        if (cudaMalloc(&pw.gtab, sizeof(double)*n) != cudaSuccess) return MHH_ERR_CUDA;
-        if (cudaMalloc(&pw.htab, sizeof(double)*n) != cudaSuccess) return MHH_ERR_CUDA;
-        if (cudaMalloc(&pw.stab, sizeof(float)*n) != cudaSuccess) return MHH_ERR_CUDA;
-        if (cudaMalloc(&pw.stabd, sizeof(double)*n) != cudaSuccess) return MHH_ERR_CUDA;
+        if (cudaMallocAsync((void**)&pw.rtab, sizeof(double)*n, s) != cudaSuccess) return MHH_ERR_CUDA;
+        if (cudaMallocAsync((void**)&pw.gtab, sizeof(double)*n, s) != cudaSuccess) return MHH_ERR_CUDA;
+        if (cudaMallocAsync((void**)&pw.htab, sizeof(double)*n, s) != cudaSuccess) return MHH_ERR_CUDA;
+        if (cudaMallocAsync((void**)&pw.stab, sizeof(float)*n, s) != cudaSuccess) return MHH_ERR_CUDA;
+        if (cudaMallocAsync((void**)&pw.stabd, sizeof(double)*n, s) != cudaSuccess) return MHH_ERR_CUDA;
         dim3 grid((pw.niu + 127)/128, pw.nju);
-        k_tdma_table<<<grid, 128>>>(pw.niu, pw.nju, ktot, pw.bmati, pw.bmatj, pw.a, pw.c, pw.dz2rho, pw.dz2,
+        k_tdma_table<<<grid, 128, 0, s>>>(pw.niu, pw.nju, ktot, pw.bmati, pw.bmatj, pw.a, pw.c, pw.dz2rho, pw.dz2,
                                     pw.rtab, pw.gtab, pw.htab, pw.stab, pw.stabd);
         count_launch();
-        return cudaDeviceSynchronize() == cudaSuccess ? MHH_OK : MHH_ERR_CUDA;
+        return cudaStreamSynchronize(s) == cudaSuccess ? MHH_OK : MHH_ERR_CUDA;
     }
 
     template<typename TF>
-    void launch_tdma(const Dims& d, const PresWork& pw, TF* pk, cudaStream_t s)
+    void launch_tdma(const Dims& d, const PresWork& pw, TF* pk, const KernelOpts& o, cudaStream_t s)
     {
         dim3 grid((pw.niu + 127)/128, pw.nju);
-        const int v = tdma_variant() < 0 ? (sizeof(TF) == 4 ? 1 : 0) : tdma_variant();
+        const int v = o.tdma < 0 ? (sizeof(TF) == 4 ? 1 : 0) : o.tdma;
         if (v == 1)
             k_tdma_scaled<TF><<<grid, 128, 0, s>>>(d.itot, d.jtot, d.ktot, pw.niu, pw.nju, pw.gtab, pw.htab,
                                                    pw.stab, pw.stabd, pk, pw.work);
@@ -933,7 +943,7 @@ namespace mhh
     template void launch_pres_in<TF>(const Dims&, const Prof<TF>&, const TF*, const TF*, const TF*, const TF*, const TF*, const TF*, TF*, double, cudaStream_t); \
     template void launch_fft_x<TF>(const FftPlan&, TF*, int, bool, double, cudaStream_t); \
     template void launch_fft_y<TF>(const FftPlan&, TF*, int, int, int, bool, double, cudaStream_t); \
-    template void launch_tdma<TF>(const Dims&, const PresWork&, TF*, cudaStream_t); \
+    template void launch_tdma<TF>(const Dims&, const PresWork&, TF*, const KernelOpts&, cudaStream_t); \
     template void launch_pres_scatter<TF>(const Dims&, const TF*, TF*, cudaStream_t);
 
     MHH_PRES_INST(double)

@@ -252,13 +252,14 @@ namespace mhh
     template<typename TF>
     void launch_viscosity(const Dims& d, const Prof<TF>& pr, const TF* u, const TF* v, const TF* w, const TF* th,
                           TF* evisc, const TF* mlen2, const double* dudz, const double* dvdz, const double* dbdz,
-                          double cs, double tpr, double visc, int mason, bool surf, bool thermo, cudaStream_t s)
+                          double cs, double tpr, double visc, int mason, bool surf, bool thermo, const KernelOpts& o,
+                          cudaStream_t s)
     {
         dim3 block(32, 8);
         dim3 grid((d.itot + 31)/32, (d.jtot + 7)/8, d.ktot);
-        const int var = viscosity_variant() < 0 ? (sizeof(TF) == 4 ? 1 : 0) : viscosity_variant();
+        const int var = o.visc < 0 ? (sizeof(TF) == 4 ? 1 : 0) : o.visc;
         const bool planes = var == 1 && launch_viscosity_planes<TF>(d, pr, u, v, w, th, evisc, mlen2, dudz, dvdz, dbdz,
-                                                                    tpr, surf, thermo, s);
+                                                                    tpr, surf, thermo, o.visc_kchunk, s);
         if (!planes)
         {
             if (surf && thermo)
@@ -370,16 +371,16 @@ namespace mhh
 
     template<typename TF>
     void launch_tendency(const Dims& d, const Prof<TF>& pr, const TendArgs<TF>& a, int adv, int dif,
-                         bool surf, bool scal, bool buoy, bool force, cudaStream_t s)
+                         bool surf, bool scal, bool buoy, bool force, const KernelOpts& o, cudaStream_t s)
     {
         // The LES combination can run in the tiled kernel (mhh_tend_tiled.cu)
         // or in the flux-form kernel (mhh_tend_flux.cu).
         // Automatic choice (-1): the flux form for float fields, the per-cell
         // kernel (the reference's operation order) for double fields.
-        const int var = tendency_variant() < 0 ? (sizeof(TF) == 4 ? 2 : 0) : tendency_variant();
+        const int var = o.tend < 0 ? (sizeof(TF) == 4 ? 2 : 0) : o.tend;
         if (var >= 1 && adv == MHH_ADVEC_2I5 && dif == MHH_DIFF_SMAG2 && !force && d.igc >= 3 && d.jgc >= 3)
         {
-            if (var == 2) launch_tendency_flux<TF>(d, pr, a, surf, scal, buoy, s);
+            if (var == 2) launch_tendency_flux<TF>(d, pr, a, surf, scal, buoy, o.tend_kchunk, s);
             else launch_tendency_les<TF>(d, pr, a, surf, scal, buoy, s);
             return;
         }
@@ -584,8 +585,8 @@ namespace mhh
     template void launch_set_bc<TF>(TF*, TF*, TF*, int, double, double, int, const Dims&, cudaStream_t); \
     template void launch_ghost<TF>(const GhostList<TF>&, const Dims&, const TF*, cudaStream_t); \
     template void launch_viscosity<TF>(const Dims&, const Prof<TF>&, const TF*, const TF*, const TF*, const TF*, TF*, \
-        const TF*, const double*, const double*, const double*, double, double, double, int, bool, bool, cudaStream_t); \
-    template void launch_tendency<TF>(const Dims&, const Prof<TF>&, const TendArgs<TF>&, int, int, bool, bool, bool, bool, cudaStream_t); \
+        const TF*, const double*, const double*, const double*, double, double, double, int, bool, bool, const KernelOpts&, cudaStream_t); \
+    template void launch_tendency<TF>(const Dims&, const Prof<TF>&, const TendArgs<TF>&, int, int, bool, bool, bool, bool, const KernelOpts&, cudaStream_t); \
     template void launch_rk3<TF>(TF*, TF*, const Dims&, int, double, cudaStream_t); \
     template void launch_presout_rk3<TF>(const Dims&, const Prof<TF>&, const TF*, TF*, TF*, TF*, TF*, TF*, TF*, TF*, TF*, int, double, cudaStream_t); \
     template void launch_reduce<TF>(int, const Dims&, const Prof<TF>&, const TF*, const TF*, const TF*, const TF*, double, unsigned long long*, cudaStream_t);

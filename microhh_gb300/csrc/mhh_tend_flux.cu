@@ -39,9 +39,8 @@ namespace mhh
         constexpr int FPH = FTY + 2*FH;         // plane rows
         constexpr int FPS = FPW*FPH;            // plane size
         constexpr int NFX = FTX + 1, NFY = FTY + 1;
-        constexpr int NFACE = NFX*NFY;          // 297 face threads
         constexpr int NTHR = 320;
-        constexpr int FKCHUNK = 32;
+        constexpr int FKCHUNK_MAX = 64;
         // Plane slots: u 4, v 4, w 3, s 3, evisc 4; level l of a field lives
         // in slot base + l % n.  Planes are prefetched two levels ahead.
         constexpr int SU = 0, SV = 4, SW = 8, SS = 11, SE = 14, NSLOT = 18;
@@ -52,7 +51,7 @@ namespace mhh
         template<typename TF> struct FluxOcc { static constexpr int v = sizeof(TF) == 4 ? 2 : 1; };
 
         constexpr int NPROF = 8;                // per-level constants staged in shared memory
-        constexpr int PLEV = FKCHUNK + 2;       // levels m0 .. m0+FKCHUNK+1
+        constexpr int PLEV = FKCHUNK_MAX + 2;   // levels m0 .. m0+kchunk+1
 
         template<typename TF>
         size_t flux_smem() { return sizeof(TF)*(size_t(NSLOT)*FPS + 2*4*(NGX + NGY) + NPROF*PLEV); }
@@ -94,7 +93,7 @@ namespace mhh
 
     template<typename TF, bool SURF, bool SCAL, bool BUOY>
     __global__ void __launch_bounds__(NTHR, FluxOcc<TF>::v)
-    k_tend_flux(Dims d, Prof<TF> pr, TendArgs<TF> a)
+    k_tend_flux(Dims d, Prof<TF> pr, TendArgs<TF> a, int kchunk)
     {
         extern __shared__ __align__(16) unsigned char smem_raw[];
         TF* sm = reinterpret_cast<TF*>(smem_raw);
@@ -115,8 +114,8 @@ namespace mhh
         const int j0 = d.jstart + blockIdx.y*FTY;
         const int i = i0 + fx, j = j0 + fy;
         const bool cell = fx < FTX && fy < FTY && i < d.iend && j < d.jend;
-        const int k0 = d.kstart + blockIdx.z*FKCHUNK;
-        const int k1 = min(k0 + FKCHUNK, d.kend);
+        const int k0 = d.kstart + blockIdx.z*kchunk;
+        const int k1 = min(k0 + kchunk, d.kend);
         const int pc = (min(fy, FTY) + FH)*FPW + (fx + FH);   // own (i, j) in a plane
         const int gxi = fy*NFX + fx, gyi = fy*FTX + fx;
 
@@ -159,7 +158,7 @@ namespace mhh
 
         // Per-level constants of the chunk: index l - m0 for level l.
         const int m0 = k0 - 1;
-        for (int q = tid; q < PLEV; q += NTHR)
+        for (int q = tid; q < kchunk + 2; q += NTHR)
         {
             const int l = min(m0 + q, d.kcells - 1);
             prof[0*PLEV + q] = pr.dzhi[l];
@@ -396,34 +395,40 @@ namespace mhh
     }
 
     template<typename TF, bool SURF, bool SCAL, bool BUOY>
-    static void launch_flux_t(const Dims& d, const Prof<TF>& pr, const TendArgs<TF>& a, cudaStream_t s)
+    static void launch_flux_t(const Dims& d, const Prof<TF>& pr, const TendArgs<TF>& a, int kchunk, cudaStream_t s)
     {
         const size_t smem = flux_smem<TF>();
-        dim3 grid((d.itot + FTX - 1)/FTX, (d.jtot + FTY - 1)/FTY, (d.ktot + FKCHUNK - 1)/FKCHUNK);
-        cudaFuncSetAttribute(k_tend_flux<TF, SURF, SCAL, BUOY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_tend_flux<TF, SURF, SCAL, BUOY><<<grid, NTHR, smem, s>>>(d, pr, a);
+        // The shared-memory limit is set once per kernel, outside any stream
+        // capture that a later call may be part of.
+        static const bool attr = cudaFuncSetAttribute(k_tend_flux<TF, SURF, SCAL, BUOY>,
+            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess;
+        (void)attr;
+        kchunk = min(auto_kchunk(kchunk, (long long)((d.itot + FTX - 1)/FTX)*((d.jtot + FTY - 1)/FTY), d.ktot),
+                     FKCHUNK_MAX);
+        dim3 grid((d.itot + FTX - 1)/FTX, (d.jtot + FTY - 1)/FTY, (d.ktot + kchunk - 1)/kchunk);
+        k_tend_flux<TF, SURF, SCAL, BUOY><<<grid, NTHR, smem, s>>>(d, pr, a, kchunk);
         count_launch();
     }
 
     // Advec_2i5 + Diff_smag2 (+ buoyancy) in flux form; igc, jgc >= 3.
     template<typename TF>
     void launch_tendency_flux(const Dims& d, const Prof<TF>& pr, const TendArgs<TF>& a, bool surf, bool scal,
-                              bool buoy, cudaStream_t s)
+                              bool buoy, int kchunk, cudaStream_t s)
     {
         const int mask = (surf ? 4 : 0) | (scal ? 2 : 0) | (buoy ? 1 : 0);
         switch (mask)
         {
-            case 0: launch_flux_t<TF, false, false, false>(d, pr, a, s); break;
-            case 1: launch_flux_t<TF, false, false, true >(d, pr, a, s); break;
-            case 2: launch_flux_t<TF, false, true,  false>(d, pr, a, s); break;
-            case 3: launch_flux_t<TF, false, true,  true >(d, pr, a, s); break;
-            case 4: launch_flux_t<TF, true,  false, false>(d, pr, a, s); break;
-            case 5: launch_flux_t<TF, true,  false, true >(d, pr, a, s); break;
-            case 6: launch_flux_t<TF, true,  true,  false>(d, pr, a, s); break;
-            default: launch_flux_t<TF, true, true,  true >(d, pr, a, s); break;
+            case 0: launch_flux_t<TF, false, false, false>(d, pr, a, kchunk, s); break;
+            case 1: launch_flux_t<TF, false, false, true >(d, pr, a, kchunk, s); break;
+            case 2: launch_flux_t<TF, false, true,  false>(d, pr, a, kchunk, s); break;
+            case 3: launch_flux_t<TF, false, true,  true >(d, pr, a, kchunk, s); break;
+            case 4: launch_flux_t<TF, true,  false, false>(d, pr, a, kchunk, s); break;
+            case 5: launch_flux_t<TF, true,  false, true >(d, pr, a, kchunk, s); break;
+            case 6: launch_flux_t<TF, true,  true,  false>(d, pr, a, kchunk, s); break;
+            default: launch_flux_t<TF, true, true,  true >(d, pr, a, kchunk, s); break;
         }
     }
 
-    template void launch_tendency_flux<double>(const Dims&, const Prof<double>&, const TendArgs<double>&, bool, bool, bool, cudaStream_t);
-    template void launch_tendency_flux<float>(const Dims&, const Prof<float>&, const TendArgs<float>&, bool, bool, bool, cudaStream_t);
+    template void launch_tendency_flux<double>(const Dims&, const Prof<double>&, const TendArgs<double>&, bool, bool, bool, int, cudaStream_t);
+    template void launch_tendency_flux<float>(const Dims&, const Prof<float>&, const TendArgs<float>&, bool, bool, bool, int, cudaStream_t);
 }

@@ -299,7 +299,9 @@ namespace mhh
         const size_t smem = sizeof(TF)*NPLANE*PS;
         dim3 block(TX, TY);
         dim3 grid((d.itot + TX - 1)/TX, (d.jtot + TY - 1)/TY, (d.ktot + KCHUNK - 1)/KCHUNK);
-        cudaFuncSetAttribute(k_tend_les<TF, SURF, SCAL, BUOY>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        static const bool attr = cudaFuncSetAttribute(k_tend_les<TF, SURF, SCAL, BUOY>,
+            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess;
+        (void)attr;
         k_tend_les<TF, SURF, SCAL, BUOY><<<grid, block, smem, s>>>(d, pr, a);
         count_launch();
     }

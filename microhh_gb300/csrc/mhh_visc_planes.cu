@@ -30,7 +30,7 @@ namespace mhh
         constexpr int VPS = VPW*VPH;            // 340
         constexpr int VNX = VTX + 1, VNY = VTY + 1;
         constexpr int VNT = 320;
-        constexpr int VKCHUNK = 32;
+        constexpr int VKCHUNK_MAX = 64;
         // Plane slots: u, v, w 4 each; level l of a field in slot base + l % 4.
         constexpr int VSU = 0, VSV = 4, VSW = 8, VNSLOT = 12;
         constexpr int VNEL1 = VPS - VNT;        // threads that copy a second element
@@ -40,7 +40,7 @@ namespace mhh
         // level while the next one writes the following half level).
         constexpr int NXY = VNY*VNX, NXZ = VTY*VNX, NYZ = VNY*VTX;
 
-        constexpr int VPLEV = VKCHUNK + 2;      // per-level constants of levels m0 .. m0+VKCHUNK+1
+        constexpr int VPLEV = VKCHUNK_MAX + 2;  // per-level constants of levels m0 .. m0+kchunk+1
 
         template<typename TF>
         size_t visc_smem() { return sizeof(TF)*(size_t(VNSLOT)*VPS + 2*NXY + 3*(NXZ + NYZ) + 5*VPLEV); }
@@ -83,7 +83,7 @@ namespace mhh
     k_visc_planes(Dims d, Prof<TF> pr, const TF* __restrict__ u, const TF* __restrict__ v, const TF* __restrict__ w,
                   const TF* __restrict__ th, TF* __restrict__ evisc, const TF* __restrict__ mlen2,
                   const double* __restrict__ dudz, const double* __restrict__ dvdz, const double* __restrict__ dbdz,
-                  TF tpr)
+                  TF tpr, int kchunk)
     {
         extern __shared__ __align__(16) unsigned char smem_raw[];
         TF* sm = reinterpret_cast<TF*>(smem_raw);
@@ -102,8 +102,8 @@ namespace mhh
         const int i0 = d.istart + blockIdx.x*VTX, j0 = d.jstart + blockIdx.y*VTY;
         const int i = i0 + ex, j = j0 + ey;
         const bool cell = ex < VTX && ey < VTY && i < d.iend && j < d.jend;
-        const int k0 = d.kstart + blockIdx.z*VKCHUNK;
-        const int k1 = min(k0 + VKCHUNK, d.kend);
+        const int k0 = d.kstart + blockIdx.z*kchunk;
+        const int k1 = min(k0 + kchunk, d.kend);
         const int pc = (min(ey, VTY) + VH)*VPW + (ex + VH);
 
         const int e0 = tid, e1 = tid + VNT;
@@ -133,7 +133,7 @@ namespace mhh
         // Iteration m uses the planes of m and m+1; the loop starts one level
         // below the chunk to produce the edges of the chunk's bottom half level.
         const int m0 = k0 - 1;
-        for (int q = tid; q < VPLEV; q += VNT)
+        for (int q = tid; q < kchunk + 2; q += VNT)
         {
             const int l = min(m0 + q, d.kcells - 1);
             lev[0*VPLEV + q] = pr.dzhi[l];
@@ -262,12 +262,17 @@ namespace mhh
     template<typename TF, bool SURF, bool THERMO>
     static void launch_vp_t(const Dims& d, const Prof<TF>& pr, const TF* u, const TF* v, const TF* w, const TF* th,
                             TF* evisc, const TF* mlen2, const double* dudz, const double* dvdz, const double* dbdz,
-                            double tpr, cudaStream_t s)
+                            double tpr, int kchunk, cudaStream_t s)
     {
         const size_t smem = visc_smem<TF>();
-        dim3 grid((d.itot + VTX - 1)/VTX, (d.jtot + VTY - 1)/VTY, (d.ktot + VKCHUNK - 1)/VKCHUNK);
-        cudaFuncSetAttribute(k_visc_planes<TF, SURF, THERMO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        k_visc_planes<TF, SURF, THERMO><<<grid, VNT, smem, s>>>(d, pr, u, v, w, th, evisc, mlen2, dudz, dvdz, dbdz, TF(tpr));
+        static const bool attr = cudaFuncSetAttribute(k_visc_planes<TF, SURF, THERMO>,
+            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess;
+        (void)attr;
+        kchunk = min(auto_kchunk(kchunk, (long long)((d.itot + VTX - 1)/VTX)*((d.jtot + VTY - 1)/VTY), d.ktot),
+                     VKCHUNK_MAX);
+        dim3 grid((d.itot + VTX - 1)/VTX, (d.jtot + VTY - 1)/VTY, (d.ktot + kchunk - 1)/kchunk);
+        k_visc_planes<TF, SURF, THERMO><<<grid, VNT, smem, s>>>(d, pr, u, v, w, th, evisc, mlen2, dudz, dvdz, dbdz,
+                                                                TF(tpr), kchunk);
         count_launch();
     }
 
@@ -277,19 +282,19 @@ namespace mhh
     template<typename TF>
     bool launch_viscosity_planes(const Dims& d, const Prof<TF>& pr, const TF* u, const TF* v, const TF* w,
                                  const TF* th, TF* evisc, const TF* mlen2, const double* dudz, const double* dvdz,
-                                 const double* dbdz, double tpr, bool surf, bool thermo, cudaStream_t s)
+                                 const double* dbdz, double tpr, bool surf, bool thermo, int kchunk, cudaStream_t s)
     {
-        if (surf && thermo) launch_vp_t<TF, true, true>(d, pr, u, v, w, th, evisc, mlen2, dudz, dvdz, dbdz, tpr, s);
-        else if (surf) launch_vp_t<TF, true, false>(d, pr, u, v, w, th, evisc, mlen2, dudz, dvdz, dbdz, tpr, s);
-        else if (thermo) launch_vp_t<TF, false, true>(d, pr, u, v, w, th, evisc, mlen2, dudz, dvdz, dbdz, tpr, s);
+        if (surf && thermo) launch_vp_t<TF, true, true>(d, pr, u, v, w, th, evisc, mlen2, dudz, dvdz, dbdz, tpr, kchunk, s);
+        else if (surf) launch_vp_t<TF, true, false>(d, pr, u, v, w, th, evisc, mlen2, dudz, dvdz, dbdz, tpr, kchunk, s);
+        else if (thermo) launch_vp_t<TF, false, true>(d, pr, u, v, w, th, evisc, mlen2, dudz, dvdz, dbdz, tpr, kchunk, s);
         else return false;
         return true;
     }
 
     template bool launch_viscosity_planes<double>(const Dims&, const Prof<double>&, const double*, const double*,
         const double*, const double*, double*, const double*, const double*, const double*, const double*, double,
-        bool, bool, cudaStream_t);
+        bool, bool, int, cudaStream_t);
     template bool launch_viscosity_planes<float>(const Dims&, const Prof<float>&, const float*, const float*,
         const float*, const float*, float*, const float*, const double*, const double*, const double*, double,
-        bool, bool, cudaStream_t);
+        bool, bool, int, cudaStream_t);
 }

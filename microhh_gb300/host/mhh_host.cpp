@@ -209,16 +209,18 @@ namespace mhh_host
     // ---------------------------------------------------------------------
     // Fields
     // ---------------------------------------------------------------------
+    // Stream-ordered allocation on the model's set-up stream: creating and
+    // destroying a model does not synchronise the work of other models.
     template<typename TF>
-    Field3d<TF>::Field3d(const std::string& n, long long ncells, int ijcells) : name(n)
+    Field3d<TF>::Field3d(const std::string& n, long long ncells, int ijcells, cudaStream_t s) : name(n), alloc_stream(s)
     {
-        cuda_check(cudaMalloc(&fld_g, sizeof(TF)*ncells), "cudaMalloc field");
-        cuda_check(cudaMemset(fld_g, 0, sizeof(TF)*ncells), "cudaMemset field");
+        cuda_check(cudaMallocAsync((void**)&fld_g, sizeof(TF)*ncells, s), "cudaMallocAsync field");
+        cuda_check(cudaMemsetAsync(fld_g, 0, sizeof(TF)*ncells, s), "cudaMemsetAsync field");
         TF** two_d[] = {&fld_bot_g, &fld_top_g, &grad_bot_g, &grad_top_g, &flux_bot_g, &flux_top_g};
         for (TF** p : two_d)
         {
-            cuda_check(cudaMalloc(p, sizeof(TF)*ijcells), "cudaMalloc boundary array");
-            cuda_check(cudaMemset(*p, 0, sizeof(TF)*ijcells), "cudaMemset boundary array");
+            cuda_check(cudaMallocAsync((void**)p, sizeof(TF)*ijcells, s), "cudaMallocAsync boundary array");
+            cuda_check(cudaMemsetAsync(*p, 0, sizeof(TF)*ijcells, s), "cudaMemsetAsync boundary array");
         }
     }
 
@@ -226,7 +228,7 @@ namespace mhh_host
     Field3d<TF>::~Field3d()
     {
         TF* ps[] = {fld_g, fld_bot_g, fld_top_g, grad_bot_g, grad_top_g, flux_bot_g, flux_top_g};
-        for (TF* p : ps) if (p) cudaFree(p);
+        for (TF* p : ps) if (p) cudaFreeAsync(p, alloc_stream);
     }
 
     template<typename TF>
@@ -235,12 +237,24 @@ namespace mhh_host
         const auto& gd = g.get_grid_data();
         visc = g.phys.visc;
         svisc = g.phys.svisc;
-        auto make = [&](const std::string& n) { return std::make_shared<Field3d<TF>>(n, gd.ncells, gd.ijcells); };
+        cuda_check(cudaStreamCreateWithFlags(&setup, cudaStreamNonBlocking), "stream");
+        auto make = [&](const std::string& n) { return std::make_shared<Field3d<TF>>(n, gd.ncells, gd.ijcells, setup); };
         for (const char* n : {"u", "v", "w"}) { mp[n] = make(n); mt[n] = make(std::string(n) + "t"); mp[n]->visc = visc; }
         if (with_scalar) { sp["th"] = make("th"); st["th"] = make("tht"); sp["th"]->visc = svisc; }
         sd["p"] = make("p");
         if (with_evisc) sd["evisc"] = make("evisc");
         (void)in;
+    }
+
+    template<typename TF>
+    Fields<TF>::~Fields()
+    {
+        mp.clear(); mt.clear(); sp.clear(); st.clear(); sd.clear();
+        if (setup)
+        {
+            cudaStreamSynchronize(setup);
+            cudaStreamDestroy(setup);
+        }
     }
 
     template<typename TF>
@@ -388,7 +402,10 @@ namespace mhh_host
             check(mhh_boundary_set_bc(c, v.fld_bot_g, v.grad_bot_g, v.flux_bot_g, MHH_BC_DIRICHLET, vbot, fields.visc, 0, 0), "set_bc");
             check(mhh_boundary_surface_init(c, fields.sp.count("th") ? sbcbot : MHH_BC_FLUX), "surface_init");
         }
-        cuda_check(cudaDeviceSynchronize(), "set_values");
+        // The BC kernels ran on the legacy stream and the fields were
+        // allocated on the fields' set-up stream; wait for both only.
+        cuda_check(cudaStreamSynchronize(0), "set_values");
+        cuda_check(cudaStreamSynchronize(fields.setup), "set_values");
     }
 
     template<typename TF>
@@ -680,7 +697,7 @@ namespace mhh_host
     // Model
     // ---------------------------------------------------------------------
     template<typename TF>
-    Model<TF>::Model(const std::string& ini_text)
+    Model<TF>::Model(const std::string& ini) : ini_text(ini)
     {
         input = std::make_unique<Input>(ini_text);
         const std::string swadvec = input->get_item<std::string>("advec", "swadvec", "", "2");
@@ -690,7 +707,9 @@ namespace mhh_host
     template<typename TF>
     void Model<TF>::init(const std::vector<double>& z)
     {
+        z_full = z;
         grid->create(z);
+        adaptive_ = input->get_item<bool>("time", "adaptivestep", "", true);
         const std::string swdiff = input->get_item<std::string>("diff", "swdiff", "", "2");
         fields = std::make_unique<Fields<TF>>(*grid, *input, grid->phys.thermo != 0, swdiff == "smag2");
         boundary = std::make_unique<Boundary<TF>>(*grid, *fields, *input);
@@ -713,7 +732,8 @@ namespace mhh_host
     template<typename TF>
     Model<TF>::~Model()
     {
-        cudaDeviceSynchronize();
+        cudaStreamSynchronize(stream);
+        cudaStreamSynchronize(0);
         pres.reset(); diff.reset(); advec.reset(); force.reset(); thermo.reset(); boundary.reset();
         fields.reset(); timeloop.reset(); grid.reset();
     }
@@ -767,9 +787,16 @@ namespace mhh_host
         check(mhh_substep_begin(grid->ctx(), &cfg, &f, &b, stream), "substep_begin");
         // The limits only matter with an adaptive time step; with a fixed
         // step they would cost a synchronisation and change nothing.
-        if (!timeloop->in_substep() && input->get_item<bool>("time", "adaptivestep", "", true))
+        if (!timeloop->in_substep() && adaptive_)
             set_time_step();
         check(mhh_substep_end(grid->ctx(), &cfg, &f, &b, timeloop->get_substep(), timeloop->get_dt(), stream), "substep_end");
+        timeloop->advance_substep();
+        timeloop->step_time();
+    }
+
+    template<typename TF>
+    void Model<TF>::advance_substep_host()
+    {
         timeloop->advance_substep();
         timeloop->step_time();
     }
@@ -806,6 +833,28 @@ namespace mhh_host
 
     template class Model<double>;
     template class Model<float>;
+
+    size_t estimate_model_bytes(const std::string& ini_text, int ktot, int precision)
+    {
+        Input in(ini_text);
+        const std::string swadvec = in.get_item<std::string>("advec", "swadvec", "", "2");
+        const int gc = swadvec == "2i5" ? 3 : 1;
+        mhh_grid_desc d;
+        d.itot = in.get_item<int>("grid", "itot", "");
+        d.jtot = in.get_item<int>("grid", "jtot", "");
+        d.ktot = ktot;
+        d.igc = gc; d.jgc = gc; d.kgc = 1;
+        d.xsize = in.get_item<double>("grid", "xsize", "");
+        d.ysize = in.get_item<double>("grid", "ysize", "");
+        d.zsize = in.get_item<double>("grid", "zsize", "");
+        size_t ctx = 0;
+        check(mhh_ctx_estimate_bytes(&d, precision, &ctx), "estimate");
+        const double tf = precision == MHH_FP64 ? 8. : 4.;
+        const double ij = double(d.itot + 2*gc)*(d.jtot + 2*gc);
+        const double nc = ij*(d.ktot + 2);
+        // u v w th, their tendencies, p, evisc; 18 boundary arrays.
+        return ctx + size_t(10.*nc*tf + 18.*ij*tf + 20.*2.*1024*1024);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -815,12 +864,7 @@ namespace
 {
     thread_local std::string g_model_error;
 
-    struct Handle
-    {
-        int prec;
-        std::unique_ptr<mhh_host::Model<double>> m64;
-        std::unique_ptr<mhh_host::Model<float>> m32;
-    };
+    using Handle = mhh_host::ModelHandle;
 
     template<typename F>
     int guard(F&& f)
@@ -887,7 +931,8 @@ int mhh_model_get_grid(mhh_model* mm, mhh_grid* out) { WITH_MODEL(mm, *out = m.g
 int mhh_model_get_profile(mhh_model* mm, const char* name, double* out)
 { WITH_MODEL(mm, { auto v = m.get_grid().profile(name); std::copy(v.begin(), v.end(), out); }); }
 int mhh_model_get_surface(mhh_model* mm, const char* name, double* out)
-{ WITH_MODEL(mm, mhh_host::check(mhh_boundary_surface_get(m.get_grid().ctx(), name, out), "surface_get")); }
+{ WITH_MODEL(mm, { mhh_host::cuda_check(cudaStreamSynchronize(m.stream), "sync");
+                   mhh_host::check(mhh_boundary_surface_get(m.get_grid().ctx(), name, out), "surface_get"); }); }
 int mhh_model_set_stream(mhh_model* mm, cudaStream_t s) { WITH_MODEL(mm, m.stream = s); }
 int mhh_model_synchronize(mhh_model* mm)
 { WITH_MODEL(mm, { cudaError_t e = cudaStreamSynchronize(m.stream); if (e != cudaSuccess) throw std::runtime_error(cudaGetErrorString(e)); }); }

@@ -68,7 +68,8 @@ namespace mhh_host
         TF *grad_bot_g = nullptr, *grad_top_g = nullptr;
         TF *flux_bot_g = nullptr, *flux_top_g = nullptr;
         double visc = 0.;
-        Field3d(const std::string& n, long long ncells, int ijcells);
+        cudaStream_t alloc_stream = nullptr;   // stream of the stream-ordered allocation and release
+        Field3d(const std::string& n, long long ncells, int ijcells, cudaStream_t s);
         ~Field3d();
     };
 
@@ -77,6 +78,8 @@ namespace mhh_host
     {
         public:
             Fields(Grid<TF>&, Input&, bool with_scalar, bool with_evisc);
+            ~Fields();
+            cudaStream_t setup = nullptr;   // allocation and release stream of the fields
             std::map<std::string, std::shared_ptr<Field3d<TF>>> mp, mt, sp, st, sd;
             double visc, svisc;
             mhh_fields dev() const;          // device pointers for the C-ABI
@@ -302,11 +305,23 @@ namespace mhh_host
             Grid<TF>& get_grid() { return *grid; }
             Fields<TF>& get_fields() { return *fields; }
             Timeloop<TF>& get_timeloop() { return *timeloop; }
+            // One fused substep on `stream` (what run_substeps(1, true)
+            // does); with a fixed time step it launches only stream work, so
+            // it can be captured into a CUDA graph.
+            void substep_fused();
+            // Advances the host-side time loop by one substep without
+            // launching (after the replay of a captured substep).
+            void advance_substep_host();
+            bool adaptive() const { return adaptive_; }
+            const std::string& ini() const { return ini_text; }
+            const std::vector<double>& levels() const { return z_full; }
             cudaStream_t stream = 0;
         private:
             void set_time_step();
             void substep_modules();
-            void substep_fused();
+            std::string ini_text;
+            std::vector<double> z_full;
+            bool adaptive_ = true;
             std::unique_ptr<Input> input;
             std::unique_ptr<Grid<TF>> grid;
             std::unique_ptr<Fields<TF>> fields;
@@ -320,4 +335,18 @@ namespace mhh_host
             Stats<TF> stats;
             mhh_substep_config cfg;
     };
+
+    // A model of either precision behind one handle (the mhh_model of the C
+    // entry points).
+    struct ModelHandle
+    {
+        int prec;
+        std::unique_ptr<Model<double>> m64;
+        std::unique_ptr<Model<float>> m32;
+        template<typename F> void visit(F&& f) { if (prec == MHH_FP64) f(*m64); else f(*m32); }
+    };
+
+    // Device bytes a model of this .ini text and ktot will allocate (fields,
+    // boundary arrays and the context), from the grid alone.
+    size_t estimate_model_bytes(const std::string& ini_text, int ktot, int precision);
 }

@@ -31,9 +31,21 @@ def test_kernel_library_exports_all(libs):
 
 def test_host_library_exports_all(libs):
     _, host = libs
-    names = declared("mhh_model.h")
+    names = declared("mhh_model.h") + declared("mhh_batch.h")
     missing = [n for n in names if not hasattr(host, n)]
     assert not missing, missing
+
+
+def test_batch_errors_without_device(libs):
+    """Argument errors of the ensemble and server entry points."""
+    _, host = libs
+    host.mhh_server_create.restype = ctypes.c_int
+    host.mhh_server_create.argtypes = [ctypes.c_double, ctypes.c_int, ctypes.c_void_p]
+    assert host.mhh_server_create(1e9, 0, None) == -1
+    host.mhh_ensemble_add.restype = ctypes.c_int
+    assert host.mhh_ensemble_add(None, None) == -1
+    host.mhh_batch_last_error.restype = ctypes.c_char_p
+    assert host.mhh_batch_last_error()
 
 
 def test_errors_without_device(libs):

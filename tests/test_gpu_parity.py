@@ -283,3 +283,22 @@ def test_launches_counted(mhh):
     n0 = mhh.launch_count()
     m.run_steps(1)
     assert mhh.launch_count() - n0 >= 3 * 10
+
+
+@pytest.mark.parametrize("precision", [64, 32], ids=["fp64", "fp32"])
+def test_profile_statistics(mhh, precision):
+    """Mean and variance profiles on the device against numpy over the
+    interior of every level."""
+    case = cases.drycbl(40, 24, 20, 4000., 2400., 2000., seed=61, noise_z=600.)
+    m = mhh.Model(case, precision=precision)
+    m.run_steps(1)
+    g = m.grid
+    for name in ("u", "w", "th"):
+        mean, var = m.profile_stats(name)
+        a = m.get(name)[:, g.jstart:g.jend, g.istart:g.iend]
+        ref_mean = a.mean(axis=(1, 2))
+        ref_var = ((a - ref_mean[:, None, None])**2).mean(axis=(1, 2))
+        # Sums of many terms of both signs: round-off relative to the field's
+        # magnitude, not to the (possibly near-zero) mean.
+        assert np.allclose(mean, ref_mean, rtol=1e-12, atol=1e-13 * np.abs(a).max()), name
+        assert np.allclose(var, ref_var, rtol=1e-9, atol=1e-14 * max(ref_var.max(), 1e-30)), name
