@@ -138,6 +138,8 @@ int mhh_ctx_estimate_bytes(const mhh_grid_desc* desc, int precision, size_t* byt
    1 = the rescaled recurrence (two FP64 FMAs per cell), -1 = automatic
    (0 for FP64 contexts, 1 for FP32 contexts; the default). */
 int mhh_set_option(const char* name, int value);
+/* "fft_column_pairs": complex sequence pairs per block of the y FFT, 4 (the
+   default) or 8. */
 /* "tendency_kchunk" / "viscosity_kchunk": levels per block of the marching
    kernels, 4, 8, 16, 32 or 64, or 0 (the default: 32, halved down to 8 while
    the grid would give fewer than two blocks per SM). */
@@ -184,7 +186,9 @@ int mhh_boundary_surface_exec(mhh_ctx* ctx, const mhh_fields* f, const mhh_bcfie
 /* Cold-start state of the surface layer (src/boundary_surface.cxx:545-580)
    and the z/L lookup table (include/boundary_surface_kernels.h:77-130). */
 int mhh_boundary_surface_init(mhh_ctx* ctx, int thermo_bc);
-/* Surface 2-D arrays to host (icells*jcells doubles): ustar obuk dudz dvdz dbdz. */
+/* Surface 2-D arrays to host (icells*jcells doubles): ustar obuk dudz dvdz dbdz;
+   and back (restart, Boundary_surface<TF>::load, src/boundary_surface.cxx:584-643). */
+int mhh_boundary_surface_set(mhh_ctx* ctx, const char* name, const double* in);
 int mhh_boundary_surface_get(mhh_ctx* ctx, const char* name, double* out);
 
 /* ---------------------------------------------------------------------- */

@@ -49,6 +49,17 @@ int mhh_model_get_grid(mhh_model* m, mhh_grid* out);
 int mhh_model_get_profile(mhh_model* m, const char* name, double* out);
 int mhh_model_get_surface(mhh_model* m, const char* name, double* out);
 
+/* Restart files in the reference's formats, in directory dir (NULL: the
+   working directory), named by iotime = itime / 10^iotimeprec s:
+   u|v|w|th.%07d (interior, model precision), time.%07d (itime, idt as
+   64-bit unsigned, iteration as 32-bit int), with the surface model
+   dudz_mo|dvdz_mo|dbdz_mo.%07d (interior 2-D, double) and th_gradbot.%07d.
+   Fields.save/load (src/fields.cxx:1244-1344), Timeloop.save/load
+   (src/timeloop.cxx:446-529), Boundary_surface.save/load
+   (src/boundary_surface.cxx:584-700).  Files are never overwritten. */
+int mhh_model_save(mhh_model* m, const char* dir, int* iotime);
+int mhh_model_load(mhh_model* m, const char* dir, int iotime);
+
 /* Streams and device access for batched drivers. */
 int mhh_model_set_stream(mhh_model* m, cudaStream_t s);
 int mhh_model_synchronize(mhh_model* m);

@@ -149,6 +149,8 @@ def load():
     _declare(host, "mhh_model_synchronize", I, [P])
     _declare(host, "mhh_model_get_device_fields", I, [P, ctypes.POINTER(Fields), ctypes.POINTER(BcFields)])
     _declare(host, "mhh_model_get_ctx", P, [P])
+    _declare(host, "mhh_model_save", I, [P, ctypes.c_char_p, ctypes.POINTER(I)])
+    _declare(host, "mhh_model_load", I, [P, ctypes.c_char_p, I])
     # Ensembles and the server (include/mhh_batch.h)
     _declare(host, "mhh_batch_last_error", ctypes.c_char_p, [])
     _declare(host, "mhh_ensemble_create", I, [ctypes.POINTER(P)])
@@ -316,6 +318,15 @@ class Model:
 
     def synchronize(self):
         check(self.host.mhh_model_synchronize(self.h))
+
+    def save(self, directory):
+        """Restart files of the current state in `directory`; returns iotime."""
+        t = ctypes.c_int()
+        check(self.host.mhh_model_save(self.h, os.fsencode(directory), ctypes.byref(t)), "save")
+        return t.value
+
+    def load(self, directory, iotime):
+        check(self.host.mhh_model_load(self.h, os.fsencode(directory), int(iotime)), "load")
 
     def profile_stats(self, name):
         """Horizontal mean and variance of every level of field `name`

@@ -72,6 +72,9 @@ namespace mhh
     int viscosity_variant() { return g_visc_variant; }
     void set_viscosity_variant(int v) { g_visc_variant = v; }
     static int g_tend_kchunk = 0, g_visc_kchunk = 0;
+    static int g_fft_col_pairs = 4;
+    int fft_column_pairs() { return g_fft_col_pairs; }
+    void set_fft_column_pairs(int p) { g_fft_col_pairs = p; }
     static int g_tdma_variant = -1;
     int tdma_variant() { return g_tdma_variant; }
     void set_tdma_variant(int v) { g_tdma_variant = v; }
@@ -571,6 +574,12 @@ int mhh_set_option(const char* name, int value)
         set_tdma_variant(value);
         return MHH_OK;
     }
+    if (!std::strcmp(name, "fft_column_pairs"))
+    {
+        if (value != 4 && value != 8) return fail(MHH_ERR_ARG, "fft_column_pairs is 4 or 8");
+        set_fft_column_pairs(value);
+        return MHH_OK;
+    }
     if (!std::strcmp(name, "tendency_kchunk") || !std::strcmp(name, "viscosity_kchunk"))
     {
         if (value != 0 && value != 4 && value != 8 && value != 16 && value != 32 && value != 64)
@@ -900,6 +909,21 @@ int mhh_boundary_surface_exec(mhh_ctx* c, const mhh_fields* f, const mhh_bcfield
 {
     if (!c || !f || !bc) return fail(MHH_ERR_ARG, "NULL argument");
     return c->prec == MHH_FP64 ? surface_exec<double>(c, f, bc, thermo_bc, s) : surface_exec<float>(c, f, bc, thermo_bc, s);
+}
+
+int mhh_boundary_surface_set(mhh_ctx* c, const char* name, const double* in)
+{
+    if (!c || !name || !in) return fail(MHH_ERR_ARG, "NULL argument");
+    double* dst = nullptr;
+    if (!std::strcmp(name, "dudz")) dst = c->sw.dudz;
+    else if (!std::strcmp(name, "dvdz")) dst = c->sw.dvdz;
+    else if (!std::strcmp(name, "dbdz")) dst = c->sw.dbdz;
+    else if (!std::strcmp(name, "obuk")) dst = c->sw.obuk;
+    else if (!std::strcmp(name, "ustar")) dst = c->sw.ustar;
+    if (!dst) return fail(MHH_ERR_ARG, "unknown surface array");
+    if (cudaMemcpy(dst, in, sizeof(double)*c->d.ijcells, cudaMemcpyHostToDevice) != cudaSuccess)
+        return fail(MHH_ERR_CUDA, "cudaMemcpy");
+    return MHH_OK;
 }
 
 int mhh_boundary_surface_get(mhh_ctx* c, const char* name, double* out)

@@ -135,6 +135,9 @@ namespace mhh
     // (0 for double fields, 1 for float fields).
     int tdma_variant();
     void set_tdma_variant(int v);
+    // Complex sequence pairs per block of the column (y) FFT: 4 or 8.
+    int fft_column_pairs();
+    void set_fft_column_pairs(int p);
 
     int tdma_table(PresWork& pw, int itot, int jtot, int ktot, cudaStream_t s);
 

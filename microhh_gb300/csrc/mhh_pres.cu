@@ -261,6 +261,17 @@ namespace mhh
         return (s / L.itot)*(long long)L.itot*n + (s % L.itot);
     }
 
+    template<typename TF>
+    __device__ __forceinline__ void fft_cp_async(TF* dst, const TF* src, bool valid)
+    {
+        const unsigned s = (unsigned)__cvta_generic_to_shared(dst);
+        const int nb = valid ? (int)sizeof(TF) : 0;
+        if constexpr (sizeof(TF) == 4)
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" :: "r"(s), "l"(src), "r"(nb) : "memory");
+        else
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" :: "r"(s), "l"(src), "r"(nb) : "memory");
+    }
+
     // One block transforms 2P real sequences: load them into shared memory,
     // pack pairs as complex, FFT, separate into halfcomplex (forward) or take
     // real and imaginary parts (inverse), store.  NFIX > 0 selects the
@@ -291,7 +302,9 @@ namespace mhh
             { T2 w; w.x = tt[2*e]; w.y = tt[2*e+1]; tws[e] = w; }
         }
 
-        // 1. Load 2P real sequences into buf1 viewed as real [2P][n].
+        // 1. Load 2P real sequences into buf1 viewed as real [2P][n], with
+        //    asynchronous copies so that all of a thread's loads are in
+        //    flight together (a missing sequence reads as zero).
         TF* r1 = reinterpret_cast<TF*>(buf1);
         const int tot = 2*P*n;
         if (L.rows)
@@ -299,7 +312,8 @@ namespace mhh
             for (int e = threadIdx.x; e < tot; e += blockDim.x)
             {
                 const int ls = e / n, j = e - ls*n;
-                r1[ls*ns + j] = ls < nloc ? data[seq_base(L, s0 + ls, n) + j] : TF(0);
+                const bool ok = ls < nloc;
+                fft_cp_async(r1 + ls*ns + j, ok ? data + seq_base(L, s0 + ls, n) + j : data, ok);
             }
         }
         else
@@ -307,9 +321,12 @@ namespace mhh
             for (int e = threadIdx.x; e < tot; e += blockDim.x)
             {
                 const int j = e / (2*P), ls = e - j*(2*P);
-                r1[ls*ns + j] = ls < nloc ? data[seq_base(L, s0 + ls, n) + (long long)j*L.itot] : TF(0);
+                const bool ok = ls < nloc;
+                fft_cp_async(r1 + ls*ns + j, ok ? data + seq_base(L, s0 + ls, n) + (long long)j*L.itot : data, ok);
             }
         }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
         __syncthreads();
 
         // 2. Complex input: z = x + i y (forward) or conj(X + i Y) (inverse).
@@ -438,6 +455,7 @@ namespace mhh
         constexpr int PR = (2*sizeof(typename C2<TF>::T)*4*NF <= 96*1024) ? 4 : 1;
         constexpr int PC = (sizeof(TF) == 4 && 2*sizeof(typename C2<TF>::T)*8*NF <= 96*1024) ? 8 : PR;
         if (L.rows) launch_fixed<TF, INV, NF, PR>(pl, data, L, scale, s);
+        else if (fft_column_pairs() == 4 || PC == PR) launch_fixed<TF, INV, NF, PR>(pl, data, L, scale, s);
         else launch_fixed<TF, INV, NF, PC>(pl, data, L, scale, s);
         return true;
     }

@@ -449,12 +449,12 @@ namespace mhh_host
                         active.push_back(order[next]);
                         ++next;
                     }
-                    // Issue: at most two steps in flight per job, round robin.
+                    // Issue: a few steps in flight per job, round robin.
                     bool progressed = false;
                     for (int id : active)
                     {
                         Job& j = jobs[id];
-                        while (j.issued < j.nsteps && j.inflight.size() < 2) { issue_step(j); progressed = true; }
+                        while (j.issued < j.nsteps && j.inflight.size() < 3) { issue_step(j); progressed = true; }
                     }
                     // Completion.
                     for (size_t q=0; q<active.size();)
@@ -477,13 +477,11 @@ namespace mhh_host
                     }
                     if (!progressed)
                     {
+                        // Nothing completed: poll again shortly.  Blocking on
+                        // one job's event would leave the other jobs without
+                        // new work until that (possibly long) step ends.
                         if (!active.empty())
-                        {
-                            // Wait for the oldest step in flight (a step lasts
-                            // milliseconds, so arrivals are seen in time).
-                            Job& j = jobs[active.front()];
-                            if (!j.inflight.empty()) cuda_ok(cudaEventSynchronize(j.inflight.front()), "event sync");
-                        }
+                            std::this_thread::sleep_for(std::chrono::microseconds(20));
                         else if (next < order.size())
                             wait_until(jobs[order[next]].arrival);
                     }

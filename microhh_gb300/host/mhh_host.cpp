@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <cstdio>
 #include <sstream>
 
 #include <cuda_runtime.h>
@@ -651,6 +652,17 @@ namespace mhh_host
         in.get_item<double>("time", "savetime", "", 0.);
         time = 0.; itime = 0; iteration = 0; substep = 0;
         idt = to_itime(dt); idtmax = to_itime(dtmax); idtlim = idt;
+        const int iotimeprec = in.get_item<int>("time", "iotimeprec", "", 0);
+        iiotimeprec = to_itime(std::pow(10., iotimeprec));
+    }
+
+    template<typename TF>
+    void Timeloop<TF>::set_state(unsigned long itime_in, unsigned long idt_in, int iteration_in)
+    {
+        itime = itime_in; idt = idt_in; iteration = iteration_in;
+        time = double(itime)/1e9;
+        dt = double(idt)/1e9;
+        substep = 0;
     }
 
     template<typename TF>
@@ -834,6 +846,194 @@ namespace mhh_host
     template class Model<double>;
     template class Model<float>;
 
+    namespace
+    {
+        std::string restart_name(const std::string& dir, const std::string& name, int iotime)
+        {
+            char buf[64];
+            std::snprintf(buf, sizeof(buf), "%s.%07d", name.c_str(), iotime);
+            return dir.empty() ? std::string(buf) : dir + "/" + buf;
+        }
+
+        // Exclusive create, as the reference's "wbx": a restart file is never
+        // overwritten.
+        FILE* create_exclusive(const std::string& path)
+        {
+            FILE* f = std::fopen(path.c_str(), "wbx");
+            if (!f) throw std::runtime_error("cannot create " + path + " (exists or not writable)");
+            return f;
+        }
+
+        template<typename T>
+        void write_all(FILE* f, const T* p, size_t n, const std::string& path)
+        {
+            if (std::fwrite(p, sizeof(T), n, f) != n) { std::fclose(f); throw std::runtime_error("write error in " + path); }
+        }
+
+        template<typename T>
+        void read_all(const std::string& path, T* p, size_t n)
+        {
+            FILE* f = std::fopen(path.c_str(), "rb");
+            if (!f) throw std::runtime_error(path + " does not exist");
+            const size_t got = std::fread(p, sizeof(T), n, f);
+            std::fclose(f);
+            if (got != n) throw std::runtime_error("short read in " + path);
+        }
+    }
+
+    template<typename TF>
+    int Model<TF>::save(const std::string& dir)
+    {
+        if (timeloop->in_substep()) throw std::runtime_error("save between full RK3 steps only");
+        cuda_check(cudaStreamSynchronize(stream), "sync");
+        const mhh_grid& g = grid->get_grid_data();
+        const int iotime = timeloop->get_iotime();
+        std::vector<double> full(g.ncells);
+        // Prognostic 3-D fields: interior levels kstart..kend-1, rows of itot,
+        // in the model precision.
+        std::vector<std::string> names = {"u", "v", "w"};
+        if (fields->sp.count("th")) names.push_back("th");
+        for (const auto& n : names)
+        {
+            fields->get_to_host(n, full.data());
+            const std::string path = restart_name(dir, n, iotime);
+            FILE* f = create_exclusive(path);
+            std::vector<TF> row(g.itot);
+            for (int k=g.kstart; k<g.kend; ++k)
+                for (int j=g.jstart; j<g.jend; ++j)
+                {
+                    for (int i=0; i<g.itot; ++i) row[i] = TF(full[g.istart + i + (size_t)j*g.icells + (size_t)k*g.ijcells]);
+                    write_all(f, row.data(), row.size(), path);
+                }
+            std::fclose(f);
+        }
+        // The integer time.
+        {
+            const std::string path = restart_name(dir, "time", iotime);
+            FILE* f = create_exclusive(path);
+            const unsigned long it = timeloop->get_itime(), idt = timeloop->get_idt();
+            const int iter = timeloop->get_iteration();
+            write_all(f, &it, 1, path);
+            write_all(f, &idt, 1, path);
+            write_all(f, &iter, 1, path);
+            std::fclose(f);
+        }
+        // Surface model: the MO gradients of the last substep (the next
+        // viscosity uses them) and the scalar's bottom gradient of a flux BC.
+        if (boundary->get_switch() == "surface")
+        {
+            std::vector<double> a2(g.ijcells);
+            std::vector<std::string> mo = {"dudz", "dvdz"};
+            if (fields->sp.count("th")) mo.push_back("dbdz");
+            for (const auto& n : mo)
+            {
+                check(mhh_boundary_surface_get(grid->ctx(), n.c_str(), a2.data()), "surface_get");
+                const std::string path = restart_name(dir, n + "_mo", iotime);
+                FILE* f = create_exclusive(path);
+                std::vector<double> plane((size_t)g.itot*g.jtot);
+                for (int j=0; j<g.jtot; ++j)
+                    for (int i=0; i<g.itot; ++i)
+                        plane[i + (size_t)j*g.itot] = a2[g.istart + i + (size_t)(j + g.jstart)*g.icells];
+                write_all(f, plane.data(), plane.size(), path);
+                std::fclose(f);
+            }
+            if (fields->sp.count("th") && boundary->sbcbot == MHH_BC_FLUX)
+            {
+                std::vector<TF> gb(g.ijcells);
+                cuda_check(cudaMemcpy(gb.data(), fields->sp.at("th")->grad_bot_g, sizeof(TF)*g.ijcells,
+                                      cudaMemcpyDeviceToHost), "copy");
+                const std::string path = restart_name(dir, "th_gradbot", iotime);
+                FILE* f = create_exclusive(path);
+                std::vector<TF> plane((size_t)g.itot*g.jtot);
+                for (int j=0; j<g.jtot; ++j)
+                    for (int i=0; i<g.itot; ++i)
+                        plane[i + (size_t)j*g.itot] = gb[g.istart + i + (size_t)(j + g.jstart)*g.icells];
+                write_all(f, plane.data(), plane.size(), path);
+                std::fclose(f);
+            }
+        }
+        return iotime;
+    }
+
+    template<typename TF>
+    void Model<TF>::load(const std::string& dir, int iotime)
+    {
+        cuda_check(cudaStreamSynchronize(stream), "sync");
+        const mhh_grid& g = grid->get_grid_data();
+        std::vector<std::string> names = {"u", "v", "w"};
+        if (fields->sp.count("th")) names.push_back("th");
+        const size_t nint = (size_t)g.itot*g.jtot*g.ktot;
+        std::vector<TF> buf(nint);
+        std::vector<double> full(g.ncells, 0.);
+        for (const auto& n : names)
+        {
+            read_all(restart_name(dir, n, iotime), buf.data(), nint);
+            std::fill(full.begin(), full.end(), 0.);
+            for (int k=0; k<g.ktot; ++k)
+                for (int j=0; j<g.jtot; ++j)
+                    for (int i=0; i<g.itot; ++i)
+                        full[g.istart + i + (size_t)(j + g.jstart)*g.icells + (size_t)(k + g.kstart)*g.ijcells]
+                            = double(buf[i + (size_t)j*g.itot + (size_t)k*g.itot*g.jtot]);
+            fields->set_from_host(n, full.data());
+        }
+        // The tendencies are zero between full steps.
+        for (auto* m : {&fields->mt, &fields->st})
+            for (auto& it : *m)
+                cuda_check(cudaMemset(it.second->fld_g, 0, sizeof(TF)*g.ncells), "memset");
+        {
+            unsigned long it = 0, idt = 0;
+            int iter = 0;
+            const std::string path = restart_name(dir, "time", iotime);
+            FILE* f = std::fopen(path.c_str(), "rb");
+            if (!f) throw std::runtime_error(path + " does not exist");
+            const bool ok = std::fread(&it, sizeof(it), 1, f) == 1 && std::fread(&idt, sizeof(idt), 1, f) == 1
+                         && std::fread(&iter, sizeof(iter), 1, f) == 1;
+            std::fclose(f);
+            if (!ok) throw std::runtime_error("short read in " + path);
+            timeloop->set_state(it, idt, iter);
+        }
+        if (boundary->get_switch() == "surface")
+        {
+            std::vector<double> plane((size_t)g.itot*g.jtot), a2(g.ijcells, 0.);
+            std::vector<std::string> mo = {"dudz", "dvdz"};
+            if (fields->sp.count("th")) mo.push_back("dbdz");
+            for (const auto& n : mo)
+            {
+                read_all(restart_name(dir, n + "_mo", iotime), plane.data(), plane.size());
+                // Interior plus the periodic ghost columns and rows.
+                for (int j=0; j<g.jcells; ++j)
+                    for (int i=0; i<g.icells; ++i)
+                    {
+                        const int ii = ((i - g.istart) % g.itot + g.itot) % g.itot;
+                        const int jj = ((j - g.jstart) % g.jtot + g.jtot) % g.jtot;
+                        a2[i + (size_t)j*g.icells] = plane[ii + (size_t)jj*g.itot];
+                    }
+                check(mhh_boundary_surface_set(grid->ctx(), n.c_str(), a2.data()), "surface_set");
+            }
+            if (fields->sp.count("th") && boundary->sbcbot == MHH_BC_FLUX)
+            {
+                std::vector<TF> p((size_t)g.itot*g.jtot), gb(g.ijcells);
+                cuda_check(cudaMemcpy(gb.data(), fields->sp.at("th")->grad_bot_g, sizeof(TF)*g.ijcells,
+                                      cudaMemcpyDeviceToHost), "copy");
+                read_all(restart_name(dir, "th_gradbot", iotime), p.data(), p.size());
+                for (int j=0; j<g.jcells; ++j)
+                    for (int i=0; i<g.icells; ++i)
+                    {
+                        const int ii = ((i - g.istart) % g.itot + g.itot) % g.itot;
+                        const int jj = ((j - g.jstart) % g.jtot + g.jtot) % g.jtot;
+                        gb[i + (size_t)j*g.icells] = p[ii + (size_t)jj*g.itot];
+                    }
+                cuda_check(cudaMemcpy(fields->sp.at("th")->grad_bot_g, gb.data(), sizeof(TF)*g.ijcells,
+                                      cudaMemcpyHostToDevice), "copy");
+            }
+        }
+    }
+
+    template int Model<double>::save(const std::string&);
+    template int Model<float>::save(const std::string&);
+    template void Model<double>::load(const std::string&, int);
+    template void Model<float>::load(const std::string&, int);
+
     size_t estimate_model_bytes(const std::string& ini_text, int ktot, int precision)
     {
         Input in(ini_text);
@@ -938,6 +1138,9 @@ int mhh_model_synchronize(mhh_model* mm)
 { WITH_MODEL(mm, { cudaError_t e = cudaStreamSynchronize(m.stream); if (e != cudaSuccess) throw std::runtime_error(cudaGetErrorString(e)); }); }
 int mhh_model_get_device_fields(mhh_model* mm, mhh_fields* f, mhh_bcfields* bc)
 { WITH_MODEL(mm, { *f = m.get_fields().dev(); *bc = m.get_fields().bc(); }); }
+int mhh_model_save(mhh_model* mm, const char* dir, int* iotime)
+{ WITH_MODEL(mm, { const int t = m.save(dir ? dir : ""); if (iotime) *iotime = t; }); }
+int mhh_model_load(mhh_model* mm, const char* dir, int iotime) { WITH_MODEL(mm, m.load(dir ? dir : "", iotime)); }
 mhh_ctx* mhh_model_get_ctx(mhh_model* mm)
 {
     Handle* h = reinterpret_cast<Handle*>(mm);

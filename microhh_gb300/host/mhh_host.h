@@ -273,12 +273,16 @@ namespace mhh_host
             int get_iteration() const { return iteration; }
             double get_time() const { return time; }
             void advance_substep() { substep = (substep + 1) % 3; }
+            // Restart state, src/timeloop.cxx:446-529: the integer time and
+            // step and the iteration; iotime = itime / 10^iotimeprec s.
+            void set_state(unsigned long itime_in, unsigned long idt_in, int iteration_in);
+            int get_iotime() const { return int(itime/iiotimeprec); }
         private:
             Grid<TF>& grid;
             Fields<TF>& fields;
             bool adaptivestep;
             double dt, dtmax, time;
-            unsigned long itime, idt, idtmax, idtlim;
+            unsigned long itime, idt, idtmax, idtlim, iiotimeprec;
             int substep, iteration;
     };
 
@@ -302,6 +306,12 @@ namespace mhh_host
             double get_cfl();
             double get_dn();
             double get_div();
+            // Restart files in the reference's formats (src/fields.cxx:1244-1344,
+            // src/field3d_io.cxx:672-752, src/timeloop.cxx:446-529,
+            // src/boundary_surface.cxx:584-700) in directory dir, named by
+            // iotime; save returns the iotime it wrote.
+            int save(const std::string& dir);
+            void load(const std::string& dir, int iotime);
             Grid<TF>& get_grid() { return *grid; }
             Fields<TF>& get_fields() { return *fields; }
             Timeloop<TF>& get_timeloop() { return *timeloop; }

@@ -79,17 +79,35 @@ def channel_study(mhh, steps=2000, avg=500):
             "errors": _compare(p32, p64), "seconds_fp32": s32, "seconds_fp64": s64}
 
 
+def cbl_fp64_floor(mhh, size=512, steps=1800, avg=300):
+    """The same FP64 run with the tridiagonal solve in the rescaled
+    recurrence (a change of round-off only, 1e-16 per operation): its
+    difference from the plain FP64 run is the chaotic-divergence floor that
+    any FP32-vs-FP64 comparison of these statistics sits on."""
+    case = cases.drycbl(size, size, size // 2, 50. * size, 50. * size, 4000., seed=2)
+    names = ("u", "v", "w", "th")
+    mhh.set_option("tdma_kernel", 1)
+    try:
+        p, secs = _averaged(mhh, case, mhh.FP64, steps, avg, names)
+    finally:
+        mhh.set_option("tdma_kernel", -1)
+    return {"case": f"dry CBL {size}x{size}x{size//2}, FP64 with the rescaled tridiagonal recurrence",
+            "seconds_fp64": secs, "profiles_fp64_perturbed": {n: [p[n][0].tolist(), p[n][1].tolist()] for n in names}}
+
+
 if __name__ == "__main__":
     import argparse
     import json
     import microhh_gb300 as mhh
     ap = argparse.ArgumentParser()
-    ap.add_argument("--which", default="both", choices=["cbl", "channel", "both"])
+    ap.add_argument("--which", default="both", choices=["cbl", "channel", "both", "floor"])
     ap.add_argument("--size", type=int, default=512)
     ap.add_argument("--steps", type=int, default=1800)
     ap.add_argument("--avg", type=int, default=300)
     a = ap.parse_args()
     out = {}
+    if a.which == "floor":
+        print(json.dumps({"floor": cbl_fp64_floor(mhh, a.size, a.steps, a.avg)}), flush=True)
     if a.which in ("channel", "both"):
         out["channel"] = channel_study(mhh)
         print(json.dumps({"channel": out["channel"]}), flush=True)

@@ -302,3 +302,28 @@ def test_profile_statistics(mhh, precision):
         # magnitude, not to the (possibly near-zero) mean.
         assert np.allclose(mean, ref_mean, rtol=1e-12, atol=1e-13 * np.abs(a).max()), name
         assert np.allclose(var, ref_var, rtol=1e-9, atol=1e-14 * max(ref_var.max(), 1e-30)), name
+
+
+@pytest.mark.parametrize("precision", [64, 32], ids=["fp64", "fp32"])
+def test_restart_is_bitwise(mhh, precision, tmp_path):
+    """Save after two steps, load into a fresh model and run two more: the
+    fields equal those of four uninterrupted steps bit for bit (the restart
+    test of the reference, python/microhh_tools.py:493-539)."""
+    case = cases.drycbl(40, 24, 20, 4000., 2400., 2000., seed=62, noise_z=600.)
+    a = mhh.Model(case, precision=precision)
+    a.run_steps(4)
+    b = mhh.Model(case, precision=precision)
+    b.run_steps(2)
+    iotime = b.save(str(tmp_path))
+    assert iotime == 4
+    tf = 8 if precision == 64 else 4
+    assert (tmp_path / "th.0000004").stat().st_size == 40 * 24 * 20 * tf
+    assert (tmp_path / "time.0000004").stat().st_size == 8 + 8 + 4
+    with pytest.raises(mhh.MhhError):
+        b.save(str(tmp_path))       # never overwrites
+    c = mhh.Model(case, precision=precision)
+    c.load(str(tmp_path), iotime)
+    c.run_steps(2)
+    assert c.time() == a.time()
+    for n in case.prognostic_names():
+        assert np.array_equal(c.get(n), a.get(n)), n
