@@ -139,7 +139,9 @@ int mhh_ctx_estimate_bytes(const mhh_grid_desc* desc, int precision, size_t* byt
    (0 for FP64 contexts, 1 for FP32 contexts; the default). */
 int mhh_set_option(const char* name, int value);
 /* "fft_column_pairs": complex sequence pairs per block of the y FFT, 4 (the
-   default) or 8. */
+   default) or 8.  "pres_fuse": 1 (the default) computes the Poisson
+   right-hand side inside the forward x FFT and stores the inverse x FFT into
+   the ghost layout of p; 0 runs them as separate kernels. */
 /* "tendency_kchunk" / "viscosity_kchunk": levels per block of the marching
    kernels, 4, 8, 16, 32 or 64, or 0 (the default: 32, halved down to 8 while
    the grid would give fewer than two blocks per SM). */

@@ -73,6 +73,8 @@ namespace mhh
     void set_viscosity_variant(int v) { g_visc_variant = v; }
     static int g_tend_kchunk = 0, g_visc_kchunk = 0;
     static int g_fft_col_pairs = 4;
+    static int g_pres_fuse = 1;
+    int pres_fuse() { return g_pres_fuse; }
     int fft_column_pairs() { return g_fft_col_pairs; }
     void set_fft_column_pairs(int p) { g_fft_col_pairs = p; }
     static int g_tdma_variant = -1;
@@ -420,6 +422,37 @@ namespace
         const Prof<TF>& pr = prof<TF>(c);
         FieldList<TF> fl;
         TF* pk = T<TF>(c->pw.pk);
+        if (pres_fuse() && d.itot > 1)
+        {
+            // The right-hand side is computed inside the forward x transform
+            // and the inverse x transform stores into the ghost layout of p:
+            // two field passes fewer each way.
+            {
+                Timed t("pres_in", s);
+                fl.n = 1; fl.p[0] = T<TF>(f->ut); launch_cyclic(fl, d, MHH_EDGE_EW, s);
+                fl.p[0] = T<TF>(f->vt); launch_cyclic(fl, d, MHH_EDGE_NS, s);
+            }
+            FftFuse<TF> fz;
+            std::memset(&fz, 0, sizeof(fz));
+            fz.d = d; fz.pr = pr;
+            fz.u = CT<TF>(f->u); fz.v = CT<TF>(f->v); fz.w = CT<TF>(f->w);
+            fz.ut = CT<TF>(f->ut); fz.vt = CT<TF>(f->vt); fz.wt = CT<TF>(f->wt);
+            fz.dti = TF(1./sub_dt);
+            fz.p = T<TF>(f->p);
+            fz.mode = 1;
+            { Timed t("fft_x", s); launch_fft_x<TF>(c->pw.px, pk, d.jtot*d.ktot, false, 1., s, &fz); }
+            { Timed t("fft_y", s); launch_fft_y<TF>(c->pw.py, pk, d.itot, d.jtot, d.ktot, false, 1., s); }
+            { Timed t("tdma", s); launch_tdma<TF>(d, c->pw, pk, opts_of(c), s); }
+            { Timed t("fft_y", s); launch_fft_y<TF>(c->pw.py, pk, d.itot, d.jtot, d.ktot, true, 1./d.jtot, s); }
+            fz.mode = 2;
+            { Timed t("fft_x", s); launch_fft_x<TF>(c->pw.px, pk, d.jtot*d.ktot, true, 1./d.itot, s, &fz); }
+            {
+                Timed t("pres_scatter", s);
+                fl.p[0] = T<TF>(f->p); launch_cyclic(fl, d, MHH_EDGE_BOTH, s);
+            }
+        }
+        else
+        {
         {
             Timed t("pres_in", s);
             fl.n = 1; fl.p[0] = T<TF>(f->ut); launch_cyclic(fl, d, MHH_EDGE_EW, s);
@@ -436,6 +469,7 @@ namespace
             Timed t("pres_scatter", s);
             launch_pres_scatter<TF>(d, pk, T<TF>(f->p), s);
             fl.p[0] = T<TF>(f->p); launch_cyclic(fl, d, MHH_EDGE_BOTH, s);
+        }
         }
         if (with_out)
         {
@@ -572,6 +606,12 @@ int mhh_set_option(const char* name, int value)
     {
         if (value < -1 || value > 1) return fail(MHH_ERR_ARG, "tdma_kernel is -1, 0 or 1");
         set_tdma_variant(value);
+        return MHH_OK;
+    }
+    if (!std::strcmp(name, "pres_fuse"))
+    {
+        if (value != 0 && value != 1) return fail(MHH_ERR_ARG, "pres_fuse is 0 or 1");
+        g_pres_fuse = value;
         return MHH_OK;
     }
     if (!std::strcmp(name, "fft_column_pairs"))

@@ -80,6 +80,41 @@ namespace mhh
         atomicMax(dst, (unsigned long long)__double_as_longlong(v));
     }
 
+    // Exact float <-> double conversions on the integer pipe (IEEE 754
+    // binary32/binary64 layouts): the FP64 pipe of this GPU is narrow and
+    // its conversions would cost as much as the solve.  Zeros, subnormals,
+    // infinities, NaNs and results outside the normal float range take the
+    // hardware conversion.
+    __device__ __forceinline__ double f2d_exact(float f)
+    {
+        const unsigned u = __float_as_uint(f);
+        const unsigned e = (u >> 23) & 0xffu;
+        if (e == 0u || e == 0xffu)
+            return (u << 1) == 0u ? __hiloint2double(int(u & 0x80000000u), 0) : double(f);
+        const unsigned hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u >> 3) & 0xfffffu);
+        return __hiloint2double(int(hi), int(u << 29));
+    }
+
+    // Round to nearest, ties to even.
+    __device__ __forceinline__ float d2f_rn(double x)
+    {
+        const unsigned hi = unsigned(__double2hiint(x)), lo = unsigned(__double2loint(x));
+        const unsigned e = (hi >> 20) & 0x7ffu;
+        if (e < 897u || e > 1150u) return float(x);
+        const unsigned r = (((hi & 0x7fffffffu) << 3) | (lo >> 29)) - (896u << 23);
+        const unsigned rem = lo & 0x1fffffffu;
+        const unsigned up = (rem > 0x10000000u || (rem == 0x10000000u && (r & 1u))) ? 1u : 0u;
+        return __uint_as_float((hi & 0x80000000u) | (r + up));
+    }
+
+    // A double of the 2-D surface state in the compute type CT, and back.
+    template<typename CT> __device__ __forceinline__ CT from_d(double x);
+    template<> __device__ __forceinline__ double from_d<double>(double x) { return x; }
+    template<> __device__ __forceinline__ float from_d<float>(double x) { return d2f_rn(x); }
+    template<typename CT> __device__ __forceinline__ double to_d(CT x);
+    template<> __device__ __forceinline__ double to_d<double>(double x) { return x; }
+    template<> __device__ __forceinline__ double to_d<float>(float x) { return f2d_exact(x); }
+
     constexpr double KAPPA = 0.4;   // include/constants.h:28
     constexpr double GRAV = 9.81;   // include/constants.h:29
     constexpr double DSMALL = 1.e-9;

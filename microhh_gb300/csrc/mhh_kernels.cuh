@@ -137,13 +137,30 @@ namespace mhh
     void set_tdma_variant(int v);
     // Complex sequence pairs per block of the column (y) FFT: 4 or 8.
     int fft_column_pairs();
+    // 1 (default): the pressure right-hand side and the scatter into p are
+    // fused into the x transforms; 0: separate kernels.
+    int pres_fuse();
     void set_fft_column_pairs(int p);
 
     int tdma_table(PresWork& pw, int itot, int jtot, int ktot, cudaStream_t s);
 
     template<typename TF> void launch_pres_in(const Dims& d, const Prof<TF>& pr, const TF* u, const TF* v, const TF* w,
                                               const TF* ut, const TF* vt, const TF* wt, TF* pk, double dti, cudaStream_t s);
-    template<typename TF> void launch_fft_x(const FftPlan& pl, TF* data, int nrows, bool inverse, double scale, cudaStream_t s);
+    // Work fused into the row (x) FFT: mode 1 computes the pressure
+    // right-hand side in place of loading the forward transform's input;
+    // mode 2 stores the inverse transform's output into the ghost layout of p.
+    template<typename TF>
+    struct FftFuse
+    {
+        int mode;
+        Dims d;
+        Prof<TF> pr;
+        const TF *u, *v, *w, *ut, *vt, *wt;
+        TF dti;
+        TF* p;
+    };
+    template<typename TF> void launch_fft_x(const FftPlan& pl, TF* data, int nrows, bool inverse, double scale, cudaStream_t s,
+                                            const FftFuse<TF>* fuse = nullptr);
     template<typename TF> void launch_fft_y(const FftPlan& pl, TF* data, int itot, int jtot, int ktot, bool inverse,
                                             double scale, cudaStream_t s);
     template<typename TF> void launch_tdma(const Dims& d, const PresWork& pw, TF* pk, const KernelOpts& o, cudaStream_t s);

@@ -245,6 +245,25 @@ namespace mhh
         static __device__ __forceinline__ void run(T2*&, T2*&, const T2*) {}
     };
 
+    // Right-hand side of the Poisson equation at interior cell (i, j, k)
+    // (indices without ghosts), src/pres_2.cxx:155-196: the divergence of the
+    // velocity that the tendencies would give after dt.
+    template<typename TF>
+    __device__ __forceinline__ TF pres_rhs(const Dims& d, const Prof<TF>& pr, const TF* __restrict__ u,
+                                           const TF* __restrict__ v, const TF* __restrict__ w,
+                                           const TF* __restrict__ ut, const TF* __restrict__ vt,
+                                           const TF* __restrict__ wt, int i, int j, int k, TF dti)
+    {
+        const long long c = ijk(d, i + d.igc, j + d.jgc, k + d.kgc);
+        const long long ii = 1, jj = d.icells, kk = d.ijcells;
+        const int kg = k + d.kgc;
+        const TF rho = ld(pr.rhoref, kg);
+        return rho*((ld(ut, c+ii) + ld(u, c+ii)*dti) - (ld(ut, c) + ld(u, c)*dti))*dxi_of<TF>(d)
+             + rho*((ld(vt, c+jj) + ld(v, c+jj)*dti) - (ld(vt, c) + ld(v, c)*dti))*dyi_of<TF>(d)
+             + (ld(pr.rhorefh, kg+1)*(ld(wt, c+kk) + ld(w, c+kk)*dti)
+              - ld(pr.rhorefh, kg  )*(ld(wt, c   ) + ld(w, c   )*dti))*ld(pr.dzi, kg);
+    }
+
     // Element j of real sequence s sits at base(s) + j*stride:
     //   rows (x):    base = s*n,                         stride = 1
     //   columns (y): base = (s / itot)*itot*n + s % itot, stride = itot
@@ -276,9 +295,9 @@ namespace mhh
     // pack pairs as complex, FFT, separate into halfcomplex (forward) or take
     // real and imaginary parts (inverse), store.  NFIX > 0 selects the
     // fixed-length path (NFIX = n, PFIX = P); NFIX = 0 the run-time plan.
-    template<typename TF, bool INV, int NFIX, int PFIX>
+    template<typename TF, bool INV, int NFIX, int PFIX, int FUSE>
     __global__ void __launch_bounds__(256)
-    k_fft(FftPlan pl, TF* __restrict__ data, SeqLayout L, int Prt, TF scale)
+    k_fft(FftPlan pl, TF* __restrict__ data, SeqLayout L, int Prt, TF scale, FftFuse<TF> fz)
     {
         using T2 = typename C2<TF>::T;
         extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -307,7 +326,24 @@ namespace mhh
         //    flight together (a missing sequence reads as zero).
         TF* r1 = reinterpret_cast<TF*>(buf1);
         const int tot = 2*P*n;
-        if (L.rows)
+        if (FUSE == 1)
+        {
+            // Rows of the pressure right-hand side computed in place of
+            // loading them: row s is (j, k) = (s % jtot, s / jtot).
+            for (int e = threadIdx.x; e < tot; e += blockDim.x)
+            {
+                const int ls = e / n, i = e - ls*n;
+                TF val = TF(0);
+                if (ls < nloc)
+                {
+                    const long long row = s0 + ls;
+                    const int kr = (int)(row / fz.d.jtot), jr = (int)(row - (long long)kr*fz.d.jtot);
+                    val = pres_rhs(fz.d, fz.pr, fz.u, fz.v, fz.w, fz.ut, fz.vt, fz.wt, i, jr, kr, fz.dti);
+                }
+                r1[ls*ns + i] = val;
+            }
+        }
+        else if (L.rows)
         {
             for (int e = threadIdx.x; e < tot; e += blockDim.x)
             {
@@ -399,8 +435,25 @@ namespace mhh
         }
         __syncthreads();
 
-        // 5. Store.
-        if (L.rows)
+        // 5. Store (with FUSE == 2 straight into the ghost layout of p, with
+        //    the bottom ghost level p[kstart-1] = p[kstart], src/pres_2.cxx:330-358).
+        if (FUSE == 2)
+        {
+            for (int e = threadIdx.x; e < tot; e += blockDim.x)
+            {
+                const int ls = e / n, i = e - ls*n;
+                if (ls < nloc)
+                {
+                    const long long row = s0 + ls;
+                    const int kr = (int)(row / fz.d.jtot), jr = (int)(row - (long long)kr*fz.d.jtot);
+                    const TF val = rout[ls*ns + i];
+                    const long long c = ijk(fz.d, i + fz.d.igc, jr + fz.d.jgc, kr + fz.d.kgc);
+                    fz.p[c] = val;
+                    if (kr == 0) fz.p[c - fz.d.ijcells] = val;
+                }
+            }
+        }
+        else if (L.rows)
         {
             for (int e = threadIdx.x; e < tot; e += blockDim.x)
             {
@@ -435,81 +488,98 @@ namespace mhh
         return P;
     }
 
-    template<typename TF, bool INV, int NF, int PF>
-    static void launch_fixed(const FftPlan& pl, TF* data, SeqLayout L, TF scale, cudaStream_t s)
+    template<typename TF, bool INV, int NF, int PF, int FUSE>
+    static void launch_fixed(const FftPlan& pl, TF* data, SeqLayout L, TF scale, const FftFuse<TF>& fz, cudaStream_t s)
     {
         const size_t smem = sizeof(typename C2<TF>::T)*((size_t)2*(PF*NF + PF) + NF);
         const long long nblk = (L.nseq + 2*PF - 1) / (2*PF);
-        static const bool attr = cudaFuncSetAttribute(k_fft<TF, INV, NF, PF>,
+        static const bool attr = cudaFuncSetAttribute(k_fft<TF, INV, NF, PF, FUSE>,
             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess;
         (void)attr;
-        k_fft<TF, INV, NF, PF><<<(unsigned)nblk, 256, smem, s>>>(pl, data, L, PF, scale);
+        k_fft<TF, INV, NF, PF, FUSE><<<(unsigned)nblk, 256, smem, s>>>(pl, data, L, PF, scale, fz);
     }
 
     template<typename TF, bool INV, int NF>
-    static bool try_fixed_n(const FftPlan& pl, TF* data, SeqLayout L, TF scale, cudaStream_t s)
+    static bool try_fixed_n(const FftPlan& pl, TF* data, SeqLayout L, TF scale, const FftFuse<TF>& fz, cudaStream_t s)
     {
         if (pl.n != NF) return false;
-        // Rows: 4 pairs per block; columns: 8 (float) or 4 (double) pairs so a
-        // warp reads at least 64 contiguous bytes per row.
+        // Rows: 4 pairs per block; columns: 4 or 8 (float) pairs per block.
         constexpr int PR = (2*sizeof(typename C2<TF>::T)*4*NF <= 96*1024) ? 4 : 1;
         constexpr int PC = (sizeof(TF) == 4 && 2*sizeof(typename C2<TF>::T)*8*NF <= 96*1024) ? 8 : PR;
-        if (L.rows) launch_fixed<TF, INV, NF, PR>(pl, data, L, scale, s);
-        else if (fft_column_pairs() == 4 || PC == PR) launch_fixed<TF, INV, NF, PR>(pl, data, L, scale, s);
-        else launch_fixed<TF, INV, NF, PC>(pl, data, L, scale, s);
+        if (L.rows)
+        {
+            if constexpr (!INV) { if (fz.mode == 1) { launch_fixed<TF, INV, NF, PR, 1>(pl, data, L, scale, fz, s); return true; } }
+            else { if (fz.mode == 2) { launch_fixed<TF, INV, NF, PR, 2>(pl, data, L, scale, fz, s); return true; } }
+            launch_fixed<TF, INV, NF, PR, 0>(pl, data, L, scale, fz, s);
+        }
+        else if (fft_column_pairs() == 4 || PC == PR) launch_fixed<TF, INV, NF, PR, 0>(pl, data, L, scale, fz, s);
+        else launch_fixed<TF, INV, NF, PC, 0>(pl, data, L, scale, fz, s);
         return true;
     }
 
     template<typename TF, bool INV>
-    static bool launch_fixed_any(const FftPlan& pl, TF* data, SeqLayout L, TF scale, cudaStream_t s)
+    static bool launch_fixed_any(const FftPlan& pl, TF* data, SeqLayout L, TF scale, const FftFuse<TF>& fz, cudaStream_t s)
     {
-        return try_fixed_n<TF, INV, 512>(pl, data, L, scale, s) || try_fixed_n<TF, INV, 256>(pl, data, L, scale, s)
-            || try_fixed_n<TF, INV, 128>(pl, data, L, scale, s) || try_fixed_n<TF, INV, 64>(pl, data, L, scale, s)
-            || try_fixed_n<TF, INV, 32>(pl, data, L, scale, s) || try_fixed_n<TF, INV, 1024>(pl, data, L, scale, s)
-            || try_fixed_n<TF, INV, 192>(pl, data, L, scale, s) || try_fixed_n<TF, INV, 96>(pl, data, L, scale, s)
-            || try_fixed_n<TF, INV, 48>(pl, data, L, scale, s) || try_fixed_n<TF, INV, 384>(pl, data, L, scale, s)
-            || try_fixed_n<TF, INV, 768>(pl, data, L, scale, s) || try_fixed_n<TF, INV, 16>(pl, data, L, scale, s);
+        return try_fixed_n<TF, INV, 512>(pl, data, L, scale, fz, s) || try_fixed_n<TF, INV, 256>(pl, data, L, scale, fz, s)
+            || try_fixed_n<TF, INV, 128>(pl, data, L, scale, fz, s) || try_fixed_n<TF, INV, 64>(pl, data, L, scale, fz, s)
+            || try_fixed_n<TF, INV, 32>(pl, data, L, scale, fz, s) || try_fixed_n<TF, INV, 1024>(pl, data, L, scale, fz, s)
+            || try_fixed_n<TF, INV, 192>(pl, data, L, scale, fz, s) || try_fixed_n<TF, INV, 96>(pl, data, L, scale, fz, s)
+            || try_fixed_n<TF, INV, 48>(pl, data, L, scale, fz, s) || try_fixed_n<TF, INV, 384>(pl, data, L, scale, fz, s)
+            || try_fixed_n<TF, INV, 768>(pl, data, L, scale, fz, s) || try_fixed_n<TF, INV, 16>(pl, data, L, scale, fz, s);
+    }
+
+    template<typename TF, bool INV, int FUSE>
+    static void launch_generic(const FftPlan& pl, TF* data, SeqLayout L, TF scale, const FftFuse<TF>& fz, cudaStream_t s)
+    {
+        const int n = pl.n;
+        const int P = pairs_per_block<TF>(n, L.rows != 0);
+        const size_t smem = 2*sizeof(typename C2<TF>::T)*((size_t)P*n + P);
+        const long long nblk = (L.nseq + 2*P - 1) / (2*P);
+        static const bool attr = cudaFuncSetAttribute(k_fft<TF, INV, 0, 0, FUSE>,
+            cudaFuncAttributeMaxDynamicSharedMemorySize, FFT_GENERIC_SMEM) == cudaSuccess;
+        (void)attr;
+        k_fft<TF, INV, 0, 0, FUSE><<<(unsigned)nblk, 256, smem, s>>>(pl, data, L, P, scale, fz);
     }
 
     template<typename TF>
-    static void launch_fft(const FftPlan& pl, TF* data, SeqLayout L, bool inverse, TF scale, cudaStream_t s)
+    static void launch_fft(const FftPlan& pl, TF* data, SeqLayout L, bool inverse, TF scale, const FftFuse<TF>& fz,
+                           cudaStream_t s)
     {
         const int n = pl.n;
         if (n == 1) return;
         count_launch();
-        if (inverse ? launch_fixed_any<TF, true>(pl, data, L, scale, s) : launch_fixed_any<TF, false>(pl, data, L, scale, s))
+        if (inverse ? launch_fixed_any<TF, true>(pl, data, L, scale, fz, s) : launch_fixed_any<TF, false>(pl, data, L, scale, fz, s))
             return;
-        const int P = pairs_per_block<TF>(n, L.rows != 0);
-        const size_t smem = 2*sizeof(typename C2<TF>::T)*((size_t)P*n + P);
-        const long long nblk = (L.nseq + 2*P - 1) / (2*P);
         if (inverse)
         {
-            static const bool attr = cudaFuncSetAttribute(k_fft<TF, true, 0, 0>,
-                cudaFuncAttributeMaxDynamicSharedMemorySize, FFT_GENERIC_SMEM) == cudaSuccess;
-            (void)attr;
-            k_fft<TF, true, 0, 0><<<(unsigned)nblk, 256, smem, s>>>(pl, data, L, P, scale);
+            if (L.rows && fz.mode == 2) launch_generic<TF, true, 2>(pl, data, L, scale, fz, s);
+            else launch_generic<TF, true, 0>(pl, data, L, scale, fz, s);
         }
         else
         {
-            static const bool attr = cudaFuncSetAttribute(k_fft<TF, false, 0, 0>,
-                cudaFuncAttributeMaxDynamicSharedMemorySize, FFT_GENERIC_SMEM) == cudaSuccess;
-            (void)attr;
-            k_fft<TF, false, 0, 0><<<(unsigned)nblk, 256, smem, s>>>(pl, data, L, P, scale);
+            if (L.rows && fz.mode == 1) launch_generic<TF, false, 1>(pl, data, L, scale, fz, s);
+            else launch_generic<TF, false, 0>(pl, data, L, scale, fz, s);
         }
     }
 
     template<typename TF>
-    void launch_fft_x(const FftPlan& pl, TF* data, int nrows, bool inverse, double scale, cudaStream_t s)
+    void launch_fft_x(const FftPlan& pl, TF* data, int nrows, bool inverse, double scale, cudaStream_t s,
+                      const FftFuse<TF>* fuse)
     {
         SeqLayout L; L.rows = 1; L.itot = 0; L.nseq = nrows;
-        launch_fft<TF>(pl, data, L, inverse, TF(scale), s);
+        FftFuse<TF> fz;
+        std::memset(&fz, 0, sizeof(fz));
+        if (fuse) fz = *fuse;
+        launch_fft<TF>(pl, data, L, inverse, TF(scale), fz, s);
     }
 
     template<typename TF>
     void launch_fft_y(const FftPlan& pl, TF* data, int itot, int jtot, int ktot, bool inverse, double scale, cudaStream_t s)
     {
         SeqLayout L; L.rows = 0; L.itot = itot; L.nseq = (long long)itot*ktot;
-        launch_fft<TF>(pl, data, L, inverse, TF(scale), s);
+        FftFuse<TF> fz;
+        std::memset(&fz, 0, sizeof(fz));
+        launch_fft<TF>(pl, data, L, inverse, TF(scale), fz, s);
         (void)jtot;
     }
 
@@ -559,15 +629,7 @@ namespace mhh
         const int j = blockIdx.y*blockDim.y + threadIdx.y;
         const int k = blockIdx.z;
         if (i >= d.itot || j >= d.jtot) return;
-        const long long c = ijk(d, i + d.igc, j + d.jgc, k + d.kgc);
-        const long long ii = 1, jj = d.icells, kk = d.ijcells;
-        const int kg = k + d.kgc;
-        const TF rho = ld(pr.rhoref, kg);
-        pk[i + (long long)j*d.itot + (long long)k*d.itot*d.jtot] =
-              rho*((ld(ut, c+ii) + ld(u, c+ii)*dti) - (ld(ut, c) + ld(u, c)*dti))*dxi_of<TF>(d)
-            + rho*((ld(vt, c+jj) + ld(v, c+jj)*dti) - (ld(vt, c) + ld(v, c)*dti))*dyi_of<TF>(d)
-            + (ld(pr.rhorefh, kg+1)*(ld(wt, c+kk) + ld(w, c+kk)*dti)
-             - ld(pr.rhorefh, kg  )*(ld(wt, c   ) + ld(w, c   )*dti))*ld(pr.dzi, kg);
+        pk[i + (long long)j*d.itot + (long long)k*d.itot*d.jtot] = pres_rhs(d, pr, u, v, w, ut, vt, wt, i, j, k, dti);
     }
 
     template<typename TF>
@@ -754,33 +816,6 @@ namespace mhh
         }
     }
 
-    // Exact float <-> double conversions on the integer pipe (IEEE 754
-    // binary32/binary64 layouts): the FP64 pipe of this GPU is narrow and
-    // its conversions would cost as much as the solve.  Zeros, subnormals,
-    // infinities, NaNs and results outside the normal float range take the
-    // hardware conversion.
-    __device__ __forceinline__ double f2d_exact(float f)
-    {
-        const unsigned u = __float_as_uint(f);
-        const unsigned e = (u >> 23) & 0xffu;
-        if (e == 0u || e == 0xffu)
-            return (u << 1) == 0u ? __hiloint2double(int(u & 0x80000000u), 0) : double(f);
-        const unsigned hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u >> 3) & 0xfffffu);
-        return __hiloint2double(int(hi), int(u << 29));
-    }
-
-    // Round to nearest, ties to even.
-    __device__ __forceinline__ float d2f_rn(double x)
-    {
-        const unsigned hi = unsigned(__double2hiint(x)), lo = unsigned(__double2loint(x));
-        const unsigned e = (hi >> 20) & 0x7ffu;
-        if (e < 897u || e > 1150u) return float(x);
-        const unsigned r = (((hi & 0x7fffffffu) << 3) | (lo >> 29)) - (896u << 23);
-        const unsigned rem = lo & 0x1fffffffu;
-        const unsigned up = (rem > 0x10000000u || (rem == 0x10000000u && (r & 1u))) ? 1u : 0u;
-        return __uint_as_float((hi & 0x80000000u) | (r + up));
-    }
-
     template<typename TF> __device__ __forceinline__ double to_f64(TF v);
     template<> __device__ __forceinline__ double to_f64<float>(float v) { return f2d_exact(v); }
     template<> __device__ __forceinline__ double to_f64<double>(double v) { return v; }
@@ -959,7 +994,7 @@ namespace mhh
 
 #define MHH_PRES_INST(TF) \
     template void launch_pres_in<TF>(const Dims&, const Prof<TF>&, const TF*, const TF*, const TF*, const TF*, const TF*, const TF*, TF*, double, cudaStream_t); \
-    template void launch_fft_x<TF>(const FftPlan&, TF*, int, bool, double, cudaStream_t); \
+    template void launch_fft_x<TF>(const FftPlan&, TF*, int, bool, double, cudaStream_t, const FftFuse<TF>*); \
     template void launch_fft_y<TF>(const FftPlan&, TF*, int, int, int, bool, double, cudaStream_t); \
     template void launch_tdma<TF>(const Dims&, const PresWork&, TF*, const KernelOpts&, cudaStream_t); \
     template void launch_pres_scatter<TF>(const Dims&, const TF*, TF*, cudaStream_t);

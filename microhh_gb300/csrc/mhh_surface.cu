@@ -47,7 +47,8 @@ namespace mhh
         return (double)__fadd_rn(zL[n-1], __fmul_rn(__fdiv_rn(num, den), dz));
     }
 
-    // Filtered wind speed, include/boundary_surface_kernels.h:132-178 (interior).
+    // Filtered wind speed, include/boundary_surface_kernels.h:132-178
+    // (interior), in the field precision.
     template<typename TF>
     __global__ void k_dutot(Dims d, const TF* __restrict__ u, const TF* __restrict__ v,
                             const TF* __restrict__ ubot, const TF* __restrict__ vbot, double* __restrict__ dutot)
@@ -58,19 +59,21 @@ namespace mhh
         const long long ii = 1, jj = d.icells;
         const long long ij = i + j*jj;
         const long long c = ij + (long long)d.kstart*d.ijcells;
-        auto U = [&](long long q) { return double(u[q]); };
-        auto V = [&](long long q) { return double(v[q]); };
-        const double uf = (1./9)*(
-              0.5*U(c-ii-jj) + U(c-jj) + U(c+ii-jj) + 0.5*U(c+2*ii-jj)
-            + 0.5*U(c-ii   ) + U(c   ) + U(c+ii   ) + 0.5*U(c+2*ii   )
-            + 0.5*U(c-ii+jj) + U(c+jj) + U(c+ii+jj) + 0.5*U(c+2*ii+jj));
-        const double vf = (1./9)*(
-              0.5*V(c-ii-jj) + V(c-ii) + V(c-ii+jj) + 0.5*V(c-ii+2*jj)
-            + 0.5*V(c   -jj) + V(c   ) + V(c   +jj) + 0.5*V(c   +2*jj)
-            + 0.5*V(c+ii-jj) + V(c+ii) + V(c+ii+jj) + 0.5*V(c+ii+2*jj));
-        const double du2 = sq(uf - 0.5*(double(ubot[ij]) + double(ubot[ij+ii])))
-                         + sq(vf - 0.5*(double(vbot[ij]) + double(vbot[ij+jj])));
-        dutot[ij] = fmax(pow(du2, 0.5), 1.e-1);
+        using CT = TF;
+        auto U = [&](long long q) { return CT(u[q]); };
+        auto V = [&](long long q) { return CT(v[q]); };
+        const CT h = CT(0.5);
+        const CT uf = CT(1./9)*(
+              h*U(c-ii-jj) + U(c-jj) + U(c+ii-jj) + h*U(c+2*ii-jj)
+            + h*U(c-ii   ) + U(c   ) + U(c+ii   ) + h*U(c+2*ii   )
+            + h*U(c-ii+jj) + U(c+jj) + U(c+ii+jj) + h*U(c+2*ii+jj));
+        const CT vf = CT(1./9)*(
+              h*V(c-ii-jj) + V(c-ii) + V(c-ii+jj) + h*V(c-ii+2*jj)
+            + h*V(c   -jj) + V(c   ) + V(c   +jj) + h*V(c   +2*jj)
+            + h*V(c+ii-jj) + V(c+ii) + V(c+ii+jj) + h*V(c+ii+2*jj));
+        const CT du2 = sq(uf - h*(CT(ubot[ij]) + CT(ubot[ij+ii])))
+                     + sq(vf - h*(CT(vbot[ij]) + CT(vbot[ij+jj])));
+        dutot[ij] = to_d<CT>(fmax(pow(du2, CT(0.5)), CT(1.e-1)));
     }
 
     // The Monin-Obukhov functions of one cell, each evaluated once: the
@@ -115,7 +118,7 @@ namespace mhh
         const int n = blockIdx.x*blockDim.x + threadIdx.x;
         if (n >= d.ijcells) return;
         using CT = TF;
-        const CT du = CT(sw.dutot[n]);
+        const CT du = from_d<CT>(sw.dutot[n]);
         const CT zs = CT(zsl);
         CT L;
         if (!thermo)
@@ -136,9 +139,10 @@ namespace mhh
             L = zs/CT(find_zL(sw.zL, sw.f, &sw.nobuk[n], Ri));
         }
         const MostCell<CT> mc = most_cell<CT>(zs, CT(z0m), CT(sw.z0h), L);
-        sw.obuk[n] = L;
-        sw.ustar[n] = du*mc.fm;
-        sw.fm[n] = mc.fm; sw.fh[n] = mc.fh; sw.phim[n] = mc.phim; sw.phih[n] = mc.phih;
+        sw.obuk[n] = to_d<CT>(L);
+        sw.ustar[n] = to_d<CT>(du*mc.fm);
+        sw.fm[n] = to_d<CT>(mc.fm); sw.fh[n] = to_d<CT>(mc.fh);
+        sw.phim[n] = to_d<CT>(mc.phim); sw.phih[n] = to_d<CT>(mc.phih);
     }
 
     // Momentum fluxes, src/boundary_surface.cxx:163-190 (interior).
@@ -153,9 +157,11 @@ namespace mhh
         const long long ii = 1, jj = d.icells;
         const long long ij = i + j*jj;
         const long long c = ij + (long long)d.kstart*d.ijcells;
-        const double fc = sw.ustar[ij]*sw.fm[ij];
-        uflux[ij] = TF(-(double(u[c]) - double(ubot[ij]))*0.5*(sw.ustar[ij-ii]*sw.fm[ij-ii] + fc));
-        vflux[ij] = TF(-(double(v[c]) - double(vbot[ij]))*0.5*(sw.ustar[ij-jj]*sw.fm[ij-jj] + fc));
+        using CT = TF;
+        auto D = [&](const double* a, long long q) { return from_d<CT>(a[q]); };
+        const CT fc = D(sw.ustar, ij)*D(sw.fm, ij);
+        uflux[ij] = -(CT(u[c]) - CT(ubot[ij]))*CT(0.5)*(D(sw.ustar, ij-ii)*D(sw.fm, ij-ii) + fc);
+        vflux[ij] = -(CT(v[c]) - CT(vbot[ij]))*CT(0.5)*(D(sw.ustar, ij-jj)*D(sw.fm, ij-jj) + fc);
     }
 
     // Surface gradients of u and v and the scalar surface value, gradient or
@@ -170,21 +176,24 @@ namespace mhh
         const int n = blockIdx.x*blockDim.x + threadIdx.x;
         if (n >= d.ijcells) return;
         const long long c = n + (long long)d.kstart*d.ijcells;
-        ugrad[n] = TF((double(u[c]) - double(ubot[n]))/zsl);
-        vgrad[n] = TF((double(v[c]) - double(vbot[n]))/zsl);
+        using CT = TF;
+        const CT z = CT(zsl);
+        ugrad[n] = (CT(u[c]) - CT(ubot[n]))/z;
+        vgrad[n] = (CT(v[c]) - CT(vbot[n]))/z;
         if (thermo)
         {
-            const double th = double(s[c]);
+            const CT th = CT(s[c]);
+            const CT us = from_d<CT>(sw.ustar[n]), fh = from_d<CT>(sw.fh[n]);
             if (thermo_bc == MHH_BC_DIRICHLET)
             {
-                sflux[n] = TF(-(th - double(sbot[n]))*sw.ustar[n]*sw.fh[n]);
-                sgrad[n] = TF((th - double(sbot[n]))/zsl);
+                sflux[n] = -(th - CT(sbot[n]))*us*fh;
+                sgrad[n] = (th - CT(sbot[n]))/z;
             }
             else
             {
-                const double bot = double(sflux[n])/(sw.ustar[n]*sw.fh[n]) + th;
-                sbot[n] = TF(bot);
-                sgrad[n] = TF((th - bot)/zsl);
+                const CT bot = CT(sflux[n])/(us*fh) + th;
+                sbot[n] = bot;
+                sgrad[n] = (th - bot)/z;
             }
         }
     }
@@ -201,19 +210,21 @@ namespace mhh
         const long long ii = 1, jj = d.icells;
         const long long ij = i + j*jj;
         const long long c = ij + (long long)d.kstart*d.ijcells;
-        const double du_c = 0.5*((double(u[c]) - double(ubot[ij])) + (double(u[c+ii]) - double(ubot[ij+ii])));
-        const double dv_c = 0.5*((double(v[c]) - double(vbot[ij])) + (double(v[c+jj]) - double(vbot[ij+jj])));
-        const double us = sw.ustar[ij];
-        const double fmv = sw.fm[ij];
-        const double ufb = -du_c*us*fmv;
-        const double vfb = -dv_c*us*fmv;
-        const double ph = sw.phim[ij];
-        sw.dudz[ij] = -ufb/(KAPPA*zsl*us)*ph;
-        sw.dvdz[ij] = -vfb/(KAPPA*zsl*us)*ph;
+        using CT = TF;
+        const CT du_c = CT(0.5)*((CT(u[c]) - CT(ubot[ij])) + (CT(u[c+ii]) - CT(ubot[ij+ii])));
+        const CT dv_c = CT(0.5)*((CT(v[c]) - CT(vbot[ij])) + (CT(v[c+jj]) - CT(vbot[ij+jj])));
+        const CT us = from_d<CT>(sw.ustar[ij]);
+        const CT fmv = from_d<CT>(sw.fm[ij]);
+        const CT ufb = -du_c*us*fmv;
+        const CT vfb = -dv_c*us*fmv;
+        const CT ph = from_d<CT>(sw.phim[ij]);
+        const CT kz = CT(KAPPA)*CT(zsl);
+        sw.dudz[ij] = to_d<CT>(-ufb/(kz*us)*ph);
+        sw.dvdz[ij] = to_d<CT>(-vfb/(kz*us)*ph);
         if (thermo)
         {
-            const double bfb = GRAV/threfh_s*double(sflux[ij]);
-            sw.dbdz[ij] = -bfb/(KAPPA*zsl*us)*sw.phih[ij];
+            const CT bfb = CT(GRAV)/CT(threfh_s)*CT(sflux[ij]);
+            sw.dbdz[ij] = to_d<CT>(-bfb/(kz*us)*from_d<CT>(sw.phih[ij]));
         }
     }
 

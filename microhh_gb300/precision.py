@@ -95,17 +95,32 @@ def cbl_fp64_floor(mhh, size=512, steps=1800, avg=300):
             "seconds_fp64": secs, "profiles_fp64_perturbed": {n: [p[n][0].tolist(), p[n][1].tolist()] for n in names}}
 
 
+def cbl_fp64_float_start(mhh, size=512, steps=1800, avg=300):
+    """The FP64 path started from the float-rounded initial state (theta
+    rounded to float, as the FP32 form stores it): its difference from the
+    plain FP64 run is how far the flow alone carries an initial perturbation
+    of float size, the yardstick for the FP32 form's differences."""
+    case = cases.drycbl(size, size, size // 2, 50. * size, 50. * size, 4000., seed=2)
+    case.fields["th"] = case.fields["th"].astype(np.float32).astype(np.float64)
+    names = ("u", "v", "w", "th")
+    p, secs = _averaged(mhh, case, mhh.FP64, steps, avg, names)
+    return {"case": f"dry CBL {size}x{size}x{size//2}, FP64 from the float-rounded initial theta",
+            "seconds_fp64": secs, "profiles_fp64_floatstart": {n: [p[n][0].tolist(), p[n][1].tolist()] for n in names}}
+
+
 if __name__ == "__main__":
     import argparse
     import json
     import microhh_gb300 as mhh
     ap = argparse.ArgumentParser()
-    ap.add_argument("--which", default="both", choices=["cbl", "channel", "both", "floor"])
+    ap.add_argument("--which", default="both", choices=["cbl", "channel", "both", "floor", "floatstart"])
     ap.add_argument("--size", type=int, default=512)
     ap.add_argument("--steps", type=int, default=1800)
     ap.add_argument("--avg", type=int, default=300)
     a = ap.parse_args()
     out = {}
+    if a.which == "floatstart":
+        print(json.dumps({"floatstart": cbl_fp64_float_start(mhh, a.size, a.steps, a.avg)}), flush=True)
     if a.which == "floor":
         print(json.dumps({"floor": cbl_fp64_floor(mhh, a.size, a.steps, a.avg)}), flush=True)
     if a.which in ("channel", "both"):

@@ -327,3 +327,23 @@ def test_restart_is_bitwise(mhh, precision, tmp_path):
     assert c.time() == a.time()
     for n in case.prognostic_names():
         assert np.array_equal(c.get(n), a.get(n)), n
+
+
+@pytest.mark.parametrize("precision", [64, 32], ids=["fp64", "fp32"])
+def test_pressure_fusion_is_bitwise(mhh, precision):
+    """The right-hand side and the scatter fused into the x transforms give
+    the same fields bit for bit as the separate kernels (a fixed FFT length
+    and a run-time-plan length)."""
+    for case in (cases.drycbl(40, 24, 20, 4000., 2400., 2000., seed=63, noise_z=600.),
+                 cases.drycbl(60, 40, 24, 6000., 4000., 2400., seed=64, noise_z=600.)):
+        out = []
+        for fuse in (0, 1):
+            mhh.set_option("pres_fuse", fuse)
+            try:
+                m = mhh.Model(case, precision=precision)
+                m.run_steps(2)
+                out.append({n: m.get(n) for n in case.prognostic_names() + ["p"]})
+            finally:
+                mhh.set_option("pres_fuse", 1)
+        for n in out[0]:
+            assert np.array_equal(out[0][n], out[1][n]), (case.name, n)
