@@ -262,6 +262,16 @@ int mhh_pres_2_get_divergence_noalloc(mhh_ctx* ctx, const mhh_fields* f, double*
 int mhh_fft_forward(mhh_ctx* ctx, void* data, cudaStream_t stream);
 int mhh_fft_backward(mhh_ctx* ctx, void* data, cudaStream_t stream);
 
+/* Buffer<TF> damping layer (src/buffer.cxx:37-160, swupdate=false): setup
+   from [buffer] zstart, sigma, beta; the relaxation targets of u, v and th
+   (kcells each, the case's initial profiles; w relaxes to zero); exec adds
+   -sigma(z) (a - abuf) to the tendencies above zstart.  Once set up, the
+   fused substep applies it after advection and diffusion, as the reference's
+   time loop does (src/model.cxx:416). */
+int mhh_buffer_setup(mhh_ctx* ctx, double zstart, double sigma, double beta);
+int mhh_buffer_set_profile(mhh_ctx* ctx, const char* name, const double* prof);
+int mhh_buffer_exec(mhh_ctx* ctx, const mhh_fields* f, cudaStream_t stream);
+
 /* Horizontal mean and variance (about the mean) of every level of a 3-D
    field, kcells values each, in double (Field3d_operators<TF>::
    calc_mean_profile, src/field3d_operators.cxx:46-67, with the variance of

@@ -60,6 +60,12 @@ int mhh_model_get_surface(mhh_model* m, const char* name, double* out);
 int mhh_model_save(mhh_model* m, const char* dir, int* iotime);
 int mhh_model_load(mhh_model* m, const char* dir, int iotime);
 
+/* Relaxation target of the buffer layer ([buffer] swbuffer=true) for u, v
+   or th: kcells values in the ghost layout, the case's initial profiles
+   (src/buffer.cxx:130-150).  u and v, and th with a thermo scheme, must be
+   set before the first step. */
+int mhh_model_set_buffer_profile(mhh_model* m, const char* name, const double* prof);
+
 /* Streams and device access for batched drivers. */
 int mhh_model_set_stream(mhh_model* m, cudaStream_t s);
 int mhh_model_synchronize(mhh_model* m);

@@ -69,10 +69,20 @@ _kern = None
 _host = None
 
 
+_last_call = [""]
+
+
+def _note_call(result, func, args):
+    _last_call[0] = func.__name__
+    return result
+
+
 def _declare(lib, name, restype, argtypes):
     f = getattr(lib, name)
     f.restype = restype
     f.argtypes = argtypes
+    if restype is ctypes.c_int:
+        f.errcheck = _note_call
     return f
 
 
@@ -125,6 +135,9 @@ def load():
     _declare(kern, "mhh_fft_forward", I, [P, P, S])
     _declare(kern, "mhh_fft_backward", I, [P, P, S])
     _declare(kern, "mhh_timeloop_rk3", I, [P, P, P, I, D, S])
+    _declare(kern, "mhh_buffer_setup", I, [P, D, D, D])
+    _declare(kern, "mhh_buffer_set_profile", I, [P, ctypes.c_char_p, dp])
+    _declare(kern, "mhh_buffer_exec", I, [P, ctypes.POINTER(Fields), S])
     _declare(kern, "mhh_substep_begin", I, [P, ctypes.POINTER(SubstepConfig), ctypes.POINTER(Fields),
                                            ctypes.POINTER(BcFields), S])
     _declare(kern, "mhh_substep_end", I, [P, ctypes.POINTER(SubstepConfig), ctypes.POINTER(Fields),
@@ -146,6 +159,7 @@ def load():
     _declare(host, "mhh_model_get_profile", I, [P, ctypes.c_char_p, dp])
     _declare(host, "mhh_model_get_surface", I, [P, ctypes.c_char_p, dp])
     _declare(host, "mhh_model_set_stream", I, [P, S])
+    _declare(host, "mhh_model_set_buffer_profile", I, [P, ctypes.c_char_p, dp])
     _declare(host, "mhh_model_synchronize", I, [P])
     _declare(host, "mhh_model_get_device_fields", I, [P, ctypes.POINTER(Fields), ctypes.POINTER(BcFields)])
     _declare(host, "mhh_model_get_ctx", P, [P])
@@ -179,7 +193,16 @@ def load():
 def check(rc, what="mhh"):
     if rc != 0:
         kern, host = load()
-        msg = host.mhh_batch_last_error() or host.mhh_model_last_error() or kern.mhh_last_error() or b""
+        # The message of the library whose entry point returned rc: each
+        # keeps its last error until its next failure.
+        fn = _last_call[0]
+        if fn.startswith(("mhh_ensemble_", "mhh_server_")):
+            msg = host.mhh_batch_last_error()
+        elif fn.startswith("mhh_model_"):
+            msg = host.mhh_model_last_error()
+        else:
+            msg = kern.mhh_last_error()
+        msg = msg or b""
         raise MhhError(f"{what} failed ({rc}): {msg.decode(errors='replace')}")
 
 
@@ -249,6 +272,9 @@ class Model:
         if case is not None:
             for n in case.prognostic_names():
                 self.set(n, case.embed(case.fields[n]))
+            if case.swbuffer:
+                for n, prof in case.buffer_profiles().items():
+                    self.set_buffer_profile(n, prof)
 
     def close(self):
         if getattr(self, "h", None):
@@ -264,6 +290,12 @@ class Model:
     def set(self, name, arr):
         a = np.ascontiguousarray(arr, dtype=np.float64).reshape(self.shape)
         check(self.host.mhh_model_set_field(self.h, name.encode(), _dptr(a)), f"set {name}")
+
+    def set_buffer_profile(self, name, prof):
+        p = np.ascontiguousarray(prof, dtype=np.float64)
+        if p.size != self.grid.kcells:
+            raise ValueError(f"buffer profile needs {self.grid.kcells} values")
+        check(self.host.mhh_model_set_buffer_profile(self.h, name.encode(), _dptr(p)), f"buffer profile {name}")
 
     def get(self, name):
         a = np.empty(self.shape, dtype=np.float64)

@@ -63,6 +63,10 @@ class Case:
     dt: float = 2.0
     dtmax: float = 0.0
     adaptivestep: bool = False
+    swbuffer: bool = False             # [buffer] damping layer above buffer_zstart
+    buffer_zstart: float = 0.0
+    buffer_sigma: float = 2.0
+    buffer_beta: float = 2.0
     fields: dict = field(default_factory=dict)   # name -> (ktot, jtot, itot) float64
 
     @property
@@ -118,7 +122,22 @@ class Case:
         if self.dtmax > 0:
             lines.append(f"dtmax={f(self.dtmax)}")
         lines += [f"adaptivestep={'true' if self.adaptivestep else 'false'}", "rkorder=3", ""]
+        if self.swbuffer:
+            lines += ["[buffer]", "swbuffer=true", f"zstart={f(self.buffer_zstart)}",
+                      f"sigma={f(self.buffer_sigma)}", f"beta={f(self.buffer_beta)}", ""]
         return "\n".join(lines)
+
+    def buffer_profiles(self):
+        """The relaxation targets of the buffer layer: the horizontal means of
+        the initial u, v and th (the reference reads the case's initial
+        profiles), as kcells arrays with zero ghost levels."""
+        out = {}
+        for n in ("u", "v", "th"):
+            if n in self.fields:
+                prof = np.zeros(self.ktot + 2)
+                prof[1:-1] = self.fields[n].mean(axis=(1, 2))
+                out[n] = prof
+        return out
 
 
 def uniform_z(ktot, zsize):

@@ -137,6 +137,12 @@ struct mhh_ctx
     cudaStream_t setup;             // set-up and release stream (stream-ordered allocations)
 
     double* statbuf;              // 2*kcells: mean and variance profiles
+    // Buffer layer: 5*kcells values in the field precision (sigma at full
+    // and half levels, u, v, s profiles), the host copy in double, and the
+    // first level the layer touches.
+    void* bufprof;
+    std::vector<double> hbuf;
+    int buf_on, buf_kb, buf_set;   // buf_set: bits of the u, v, th profiles given
     unsigned long long* red;      // device reduction word
     unsigned long long* red_host; // pinned host copy
     double dnmul2;                // Diff_2 multiplier
@@ -568,6 +574,9 @@ namespace
         {
             Timed t("tendency", s);
             launch_tendency<TF>(d, pr, a, cfg->advec, cfg->diff, surf, scal, buoy, force, opts_of(c), s);
+            if (c->buf_on)
+                launch_buffer<TF>(d, (const TF*)c->bufprof, c->buf_kb, CT<TF>(f->u), CT<TF>(f->v), CT<TF>(f->w),
+                                  CT<TF>(f->s), T<TF>(f->ut), T<TF>(f->vt), T<TF>(f->wt), T<TF>(f->st), s);
         }
         const double cB[3] = {1./3., 15./16., 8./15.};
         int rc = pres_exec<TF>(c, f, cB[substep]*dt, false, s);
@@ -726,6 +735,10 @@ int mhh_ctx_create(const mhh_grid_desc* desc, const double* z, int precision, co
     cudaMemGetInfo(&free0, &total0);
     mhh_ctx* c = new mhh_ctx();
     c->statbuf = nullptr;
+    c->bufprof = nullptr;
+    c->buf_on = 0;
+    c->buf_kb = 0;
+    c->buf_set = 0;
     c->opt_tend = c->opt_visc = c->opt_tdma = c->opt_tend_kchunk = c->opt_visc_kchunk = -2;
     c->dev_bytes = 0;
     if (cudaStreamCreateWithFlags(&c->setup, cudaStreamNonBlocking) != cudaSuccess)
@@ -855,7 +868,7 @@ int mhh_ctx_destroy(mhh_ctx* c)
     for (auto& p : c->dprof) if (p) cudaFreeAsync(p, c->setup);
     fft_plan_free(&c->pw.px, c->setup); fft_plan_free(&c->pw.py, c->setup);
     void* ptrs[] = {c->pw.pk, c->pw.work, c->pw.rtab, c->pw.gtab, c->pw.htab, c->pw.stab, c->pw.stabd, c->pw.bmati, c->pw.bmatj, c->pw.a, c->pw.c, c->pw.dz2, c->pw.dz2rho,
-                    c->red, c->statbuf, c->sw.fm, c->sw.fh, c->sw.phim, c->sw.phih, c->sw.ustar, c->sw.obuk, c->sw.dudz, c->sw.dvdz, c->sw.dbdz, c->sw.dutot,
+                    c->red, c->statbuf, c->bufprof, c->sw.fm, c->sw.fh, c->sw.phim, c->sw.phih, c->sw.ustar, c->sw.obuk, c->sw.dudz, c->sw.dvdz, c->sw.dbdz, c->sw.dutot,
                     c->sw.nobuk, c->sw.zL, c->sw.f, c->sw.mlen2, c->sw.mlen2f};
     for (void* p : ptrs) if (p) cudaFreeAsync(p, c->setup);
     if (c->red_host) cudaFreeHost(c->red_host);
@@ -1137,6 +1150,87 @@ namespace mhh
 
 extern "C" {
 
+static bool buffer_ready(const mhh_ctx* c, const mhh_fields* f)
+{
+    const int need = f->s ? 7 : 3;
+    return (c->buf_set & need) == need;
+}
+
+static int upload_buffer(mhh_ctx* c)
+{
+    const size_t n = c->hbuf.size();
+    const size_t tf = c->prec == MHH_FP64 ? 8 : 4;
+    if (!c->bufprof && cudaMallocAsync(&c->bufprof, tf*n, c->setup) != cudaSuccess)
+        return fail(MHH_ERR_CUDA, "cudaMallocAsync buffer");
+    if (cudaStreamSynchronize(c->setup) != cudaSuccess) return fail(MHH_ERR_CUDA, "buffer allocation");
+    cudaError_t e;
+    if (c->prec == MHH_FP64)
+        e = cudaMemcpy(c->bufprof, c->hbuf.data(), 8*n, cudaMemcpyHostToDevice);
+    else
+    {
+        std::vector<float> f(c->hbuf.begin(), c->hbuf.end());
+        e = cudaMemcpy(c->bufprof, f.data(), 4*n, cudaMemcpyHostToDevice);
+    }
+    return e == cudaSuccess ? MHH_OK : fail(MHH_ERR_CUDA, "upload buffer");
+}
+
+int mhh_buffer_setup(mhh_ctx* c, double zstart, double sigma, double beta)
+{
+    if (!c) return fail(MHH_ERR_ARG, "NULL argument");
+    const Dims& d = c->d;
+    const int kc = d.kcells;
+    if (c->hbuf.empty()) c->hbuf.assign(5*(size_t)kc, 0.);
+    // src/buffer.cxx:100-130: the layer starts at the first full (half)
+    // level at or above zstart; sigma(z) = sigma ((z - zstart)/(zsize - zstart))^beta.
+    int kb = d.kstart, kbh = d.kstart;
+    for (int k=d.kstart; k<d.kend; ++k)
+    {
+        if (c->h[P_Z][k] < zstart) ++kb;
+        if (c->h[P_ZH][k] < zstart) ++kbh;
+    }
+    if (kbh == d.kend) return fail(MHH_ERR_ARG, "Buffer is too close to the model top");
+    const double zsizebuf = d.zsize - zstart;
+    for (int k=0; k<kc; ++k)
+    {
+        c->hbuf[k] = k >= kb && k < d.kend ? sigma*std::pow((c->h[P_Z][k] - zstart)/zsizebuf, beta) : 0.;
+        c->hbuf[kc + k] = k >= kbh && k < d.kend ? sigma*std::pow((c->h[P_ZH][k] - zstart)/zsizebuf, beta) : 0.;
+    }
+    c->buf_kb = std::min(kb, kbh);
+    c->buf_on = 1;
+    return upload_buffer(c);
+}
+
+int mhh_buffer_set_profile(mhh_ctx* c, const char* name, const double* prof)
+{
+    if (!c || !name || !prof) return fail(MHH_ERR_ARG, "NULL argument");
+    if (!c->buf_on) return fail(MHH_ERR_ARG, "buffer layer not set up");
+    int q = -1;
+    if (!std::strcmp(name, "u")) q = 2;
+    else if (!std::strcmp(name, "v")) q = 3;
+    else if (!std::strcmp(name, "th")) q = 4;
+    if (q < 0) return fail(MHH_ERR_ARG, "buffer profiles are u, v and th");
+    const int kc = c->d.kcells;
+    std::copy(prof, prof + kc, c->hbuf.begin() + (size_t)q*kc);
+    c->buf_set |= 1 << (q - 2);
+    return upload_buffer(c);
+}
+
+int mhh_buffer_exec(mhh_ctx* c, const mhh_fields* f, cudaStream_t s)
+{
+    if (!c || !f) return fail(MHH_ERR_ARG, "NULL argument");
+    if (!c->buf_on) return MHH_OK;
+    if (!buffer_ready(c, f)) return fail(MHH_ERR_ARG, "buffer profiles of u, v (and th) not set");
+    if (c->prec == MHH_FP64)
+        launch_buffer<double>(c->d, (const double*)c->bufprof, c->buf_kb, (const double*)f->u, (const double*)f->v,
+                              (const double*)f->w, (const double*)f->s, (double*)f->ut, (double*)f->vt, (double*)f->wt,
+                              (double*)f->st, s);
+    else
+        launch_buffer<float>(c->d, (const float*)c->bufprof, c->buf_kb, (const float*)f->u, (const float*)f->v,
+                             (const float*)f->w, (const float*)f->s, (float*)f->ut, (float*)f->vt, (float*)f->wt,
+                             (float*)f->st, s);
+    return check_cuda("buffer");
+}
+
 int mhh_stats_profile(mhh_ctx* c, const void* field, double* mean, double* var, cudaStream_t s)
 {
     if (!c || !field || !mean || !var) return fail(MHH_ERR_ARG, "NULL argument");
@@ -1219,6 +1313,7 @@ int mhh_substep_end(mhh_ctx* c, const mhh_substep_config* cfg, const mhh_fields*
     if (!c || !cfg || !f || !bc || !f->p || substep < 0 || substep > 2) return fail(MHH_ERR_ARG, "bad argument");
     if (cfg->advec == MHH_ADVEC_2I5 && (c->d.igc < 3 || c->d.jgc < 3)) return fail(MHH_ERR_ARG, "Advec_2i5 needs 3 ghost cells");
     if (cfg->diff == MHH_DIFF_SMAG2 && !f->evisc) return fail(MHH_ERR_ARG, "evisc is NULL");
+    if (c->buf_on && !buffer_ready(c, f)) return fail(MHH_ERR_ARG, "buffer profiles of u, v (and th) not set");
     return c->prec == MHH_FP64 ? substep_end<double>(c, cfg, f, bc, substep, dt, s)
                                : substep_end<float>(c, cfg, f, bc, substep, dt, s);
 }

@@ -88,6 +88,12 @@ namespace mhh
                                                    bool surf, bool scal, bool buoy, cudaStream_t s);
     template<typename TF> void launch_tendency_flux(const Dims& d, const Prof<TF>& pr, const TendArgs<TF>& a,
                                                     bool surf, bool scal, bool buoy, int kchunk, cudaStream_t s);
+    // Buffer-layer relaxation, src/buffer.cxx:37-59: prof holds, kcells each,
+    // sigma(z) at full levels, sigma(zh) at half levels (zero below the
+    // layer) and the u, v, s buffer profiles.
+    template<typename TF> void launch_buffer(const Dims& d, const TF* prof, int kb, const TF* u, const TF* v,
+                                             const TF* w, const TF* s, TF* ut, TF* vt, TF* wt, TF* st,
+                                             cudaStream_t strm);
     template<typename TF> void launch_rk3(TF* a, TF* at, const Dims& d, int substep, double dt, cudaStream_t s);
     template<typename TF> void launch_presout_rk3(const Dims& d, const Prof<TF>& pr, const TF* p, TF* u, TF* v, TF* w,
                                                   TF* s, TF* ut, TF* vt, TF* wt, TF* st, int substep, double dt,

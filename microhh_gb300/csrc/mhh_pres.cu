@@ -329,7 +329,9 @@ namespace mhh
         if (FUSE == 1)
         {
             // Rows of the pressure right-hand side computed in place of
-            // loading them: row s is (j, k) = (s % jtot, s / jtot).
+            // loading them: row s is (j, k) = (s % jtot, s / jtot).  Unrolled
+            // so that the loads of several elements are in flight together.
+            #pragma unroll 4
             for (int e = threadIdx.x; e < tot; e += blockDim.x)
             {
                 const int ls = e / n, i = e - ls*n;

@@ -429,6 +429,42 @@ namespace mhh
             at[n] = TF(0);
     }
 
+    // ---------------------------------------------------------------------
+    // Buffer (damping) layer, src/buffer.cxx:37-59: at -= sigma(z) (a - abuf)
+    // for u, v, s at the full levels and w (towards zero) at the half levels
+    // inside the layer; levels with sigma = 0 are below it and untouched.
+    // ---------------------------------------------------------------------
+    template<typename TF>
+    __global__ void k_buffer(Dims d, const TF* __restrict__ prof, int kb, const TF* __restrict__ u,
+                             const TF* __restrict__ v, const TF* __restrict__ w, const TF* __restrict__ s,
+                             TF* __restrict__ ut, TF* __restrict__ vt, TF* __restrict__ wt, TF* __restrict__ st)
+    {
+        const int i = d.istart + blockIdx.x*blockDim.x + threadIdx.x;
+        const int j = d.jstart + blockIdx.y*blockDim.y + threadIdx.y;
+        const int k = kb + blockIdx.z;
+        if (i >= d.iend || j >= d.jend || k >= d.kend) return;
+        const int kc = d.kcells;
+        const TF sf = prof[k], sh = prof[kc + k];
+        const long long c = ijk(d, i, j, k);
+        if (sf != TF(0))
+        {
+            ut[c] -= sf*(u[c] - prof[2*kc + k]);
+            vt[c] -= sf*(v[c] - prof[3*kc + k]);
+            if (s) st[c] -= sf*(s[c] - prof[4*kc + k]);
+        }
+        if (sh != TF(0)) wt[c] -= sh*(w[c] - TF(0));
+    }
+
+    template<typename TF>
+    void launch_buffer(const Dims& d, const TF* prof, int kb, const TF* u, const TF* v, const TF* w, const TF* s,
+                       TF* ut, TF* vt, TF* wt, TF* st, cudaStream_t strm)
+    {
+        if (kb >= d.kend) return;
+        dim3 block(32, 8), grid((d.itot + 31)/32, (d.jtot + 7)/8, d.kend - kb);
+        k_buffer<TF><<<grid, block, 0, strm>>>(d, prof, kb, u, v, w, s, ut, vt, wt, st);
+        count_launch();
+    }
+
     template<typename TF>
     void launch_rk3(TF* a, TF* at, const Dims& d, int substep, double dt, cudaStream_t s)
     {
@@ -588,6 +624,7 @@ namespace mhh
         const TF*, const double*, const double*, const double*, double, double, double, int, bool, bool, const KernelOpts&, cudaStream_t); \
     template void launch_tendency<TF>(const Dims&, const Prof<TF>&, const TendArgs<TF>&, int, int, bool, bool, bool, bool, const KernelOpts&, cudaStream_t); \
     template void launch_rk3<TF>(TF*, TF*, const Dims&, int, double, cudaStream_t); \
+    template void launch_buffer<TF>(const Dims&, const TF*, int, const TF*, const TF*, const TF*, const TF*, TF*, TF*, TF*, TF*, cudaStream_t); \
     template void launch_presout_rk3<TF>(const Dims&, const Prof<TF>&, const TF*, TF*, TF*, TF*, TF*, TF*, TF*, TF*, TF*, int, double, cudaStream_t); \
     template void launch_reduce<TF>(int, const Dims&, const Prof<TF>&, const TF*, const TF*, const TF*, const TF*, double, unsigned long long*, cudaStream_t);
 

@@ -475,6 +475,45 @@ namespace mhh_host
     }
 
     // ---------------------------------------------------------------------
+    // Buffer, src/buffer.cxx:61-200
+    // ---------------------------------------------------------------------
+    template<typename TF>
+    Buffer<TF>::Buffer(Grid<TF>& g, Fields<TF>& f, Input& in) : grid(g), fields(f)
+    {
+        swbuffer = in.get_item<bool>("buffer", "swbuffer", "", false);
+        zstart = sigma = beta = 0.;
+        if (swbuffer)
+        {
+            if (in.get_item<bool>("buffer", "swupdate", "", false))
+                throw std::runtime_error("buffer swupdate=true is not on this path");
+            zstart = in.get_item<double>("buffer", "zstart", "");
+            sigma = in.get_item<double>("buffer", "sigma", "", 2.);
+            beta = in.get_item<double>("buffer", "beta", "", 2.);
+        }
+    }
+
+    template<typename TF>
+    void Buffer<TF>::create()
+    {
+        if (swbuffer) check(mhh_buffer_setup(grid.ctx(), zstart, sigma, beta), "buffer setup");
+    }
+
+    template<typename TF>
+    void Buffer<TF>::set_profile(const std::string& name, const double* prof)
+    {
+        if (!swbuffer) throw std::runtime_error("the buffer layer is off (swbuffer=false)");
+        check(mhh_buffer_set_profile(grid.ctx(), name.c_str(), prof), "buffer profile");
+    }
+
+    template<typename TF>
+    void Buffer<TF>::exec(cudaStream_t s)
+    {
+        if (!swbuffer) return;
+        mhh_fields f = fields.dev();
+        check(mhh_buffer_exec(grid.ctx(), &f, s), "buffer");
+    }
+
+    // ---------------------------------------------------------------------
     // Advec, src/advec.cxx:38-96 and the schemes.
     // ---------------------------------------------------------------------
     template<typename TF>
@@ -727,6 +766,8 @@ namespace mhh_host
         boundary = std::make_unique<Boundary<TF>>(*grid, *fields, *input);
         thermo = std::make_unique<Thermo_dry<TF>>(*grid, *fields, *input);
         force = std::make_unique<Force<TF>>(*grid, *fields, *input);
+        buffer = std::make_unique<Buffer<TF>>(*grid, *fields, *input);
+        buffer->create();
         advec = Advec<TF>::factory(*grid, *fields, *input);
         diff = Diff<TF>::factory(*grid, *fields, *boundary, *input);
         pres = Pres<TF>::factory(*grid, *fields, *input);
@@ -746,7 +787,7 @@ namespace mhh_host
     {
         cudaStreamSynchronize(stream);
         cudaStreamSynchronize(0);
-        pres.reset(); diff.reset(); advec.reset(); force.reset(); thermo.reset(); boundary.reset();
+        pres.reset(); diff.reset(); advec.reset(); buffer.reset(); force.reset(); thermo.reset(); boundary.reset();
         fields.reset(); timeloop.reset(); grid.reset();
     }
 
@@ -785,6 +826,7 @@ namespace mhh_host
         boundary->set_ghost_cells(stream);
         advec->exec(stats);
         diff->exec(stats);
+        buffer->exec(stream);
         force->exec(timeloop->get_sub_time_step(), stream);
         pres->exec(timeloop->get_sub_time_step(), stats);
         timeloop->exec(stream);
@@ -825,6 +867,9 @@ namespace mhh_host
 
     template<typename TF>
     void Model<TF>::run_steps(int n, bool fused) { run_substeps(3*n, fused); }
+
+    template<typename TF>
+    void Model<TF>::set_buffer_profile(const std::string& name, const double* prof) { buffer->set_profile(name, prof); }
 
     template<typename TF>
     double Model<TF>::get_cfl()
@@ -1134,6 +1179,11 @@ int mhh_model_get_surface(mhh_model* mm, const char* name, double* out)
 { WITH_MODEL(mm, { mhh_host::cuda_check(cudaStreamSynchronize(m.stream), "sync");
                    mhh_host::check(mhh_boundary_surface_get(m.get_grid().ctx(), name, out), "surface_get"); }); }
 int mhh_model_set_stream(mhh_model* mm, cudaStream_t s) { WITH_MODEL(mm, m.stream = s); }
+int mhh_model_set_buffer_profile(mhh_model* mm, const char* name, const double* prof)
+{
+    if (!name || !prof) return MHH_ERR_ARG;
+    WITH_MODEL(mm, m.set_buffer_profile(name, prof));
+}
 int mhh_model_synchronize(mhh_model* mm)
 { WITH_MODEL(mm, { cudaError_t e = cudaStreamSynchronize(m.stream); if (e != cudaSuccess) throw std::runtime_error(cudaGetErrorString(e)); }); }
 int mhh_model_get_device_fields(mhh_model* mm, mhh_fields* f, mhh_bcfields* bc)

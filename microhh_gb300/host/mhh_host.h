@@ -140,6 +140,25 @@ namespace mhh_host
             Fields<TF>& fields;
     };
 
+    // ---- Buffer, include/buffer.h:35-70 ----------------------------------
+    // Damping layer above zstart with the case's initial profiles as targets
+    // (swupdate = false); the profiles are set through set_profile before
+    // the first step.
+    template<typename TF>
+    class Buffer
+    {
+        public:
+            Buffer(Grid<TF>&, Fields<TF>&, Input&);
+            void create();                           // src/buffer.cxx:100-130
+            void set_profile(const std::string& name, const double* prof);
+            void exec(cudaStream_t);                 // src/buffer.cxx:160-200
+            bool swbuffer;
+            double zstart, sigma, beta;
+        private:
+            Grid<TF>& grid;
+            Fields<TF>& fields;
+    };
+
     // ---- Advec, include/advec.h:45-70 ------------------------------------
     template<typename TF>
     class Advec
@@ -303,6 +322,8 @@ namespace mhh_host
             // sequence of the reference loop.
             void run_steps(int n, bool fused);
             void run_substeps(int n, bool fused);
+            // Relaxation target of the buffer layer for u, v or th (kcells).
+            void set_buffer_profile(const std::string& name, const double* prof);
             double get_cfl();
             double get_dn();
             double get_div();
@@ -338,6 +359,7 @@ namespace mhh_host
             std::unique_ptr<Boundary<TF>> boundary;
             std::unique_ptr<Thermo_dry<TF>> thermo;
             std::unique_ptr<Force<TF>> force;
+            std::unique_ptr<Buffer<TF>> buffer;
             std::unique_ptr<Advec<TF>> advec;
             std::unique_ptr<Diff<TF>> diff;
             std::unique_ptr<Pres<TF>> pres;

@@ -98,6 +98,9 @@ struct orc_model
     /* pressure solver */
     double *bmati, *bmatj, *pa, *pc, *work3d, *bb, *work2d, *fftbuf;
 
+    /* buffer layer (src/buffer.cxx) */
+    double *bufu, *bufv, *bufth;
+
     /* time loop */
     int substep, iteration;
     unsigned long itime, idt, idtlim, idtmax;

@@ -54,6 +54,9 @@ typedef struct
 
     double dt, dtmax;
     int adaptivestep;
+
+    int swbuffer;     /* 1: damping layer above buf_zstart ([buffer] swbuffer) */
+    double buf_zstart, buf_sigma, buf_beta;
 } orc_params;
 
 typedef struct orc_model orc_model;
@@ -98,6 +101,10 @@ void orc_exec_boundary(orc_model* m);
 void orc_exec_advec(orc_model* m);
 void orc_exec_diff(orc_model* m);
 void orc_exec_force(orc_model* m);
+void orc_exec_buffer(orc_model* m);
+/* Buffer profile of u, v or th (kcells values), the relaxation target of the
+   damping layer (the initial profiles of the case). */
+int orc_set_buffer_profile(orc_model* m, const char* name, const double* prof);
 void orc_exec_pres(orc_model* m, double sub_dt);
 void orc_exec_timeloop(orc_model* m);
 

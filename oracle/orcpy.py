@@ -35,6 +35,8 @@ class Params(ctypes.Structure):
         ("swlspres", ctypes.c_int), ("dpdx", ctypes.c_double),
         ("z0m", ctypes.c_double), ("z0h", ctypes.c_double),
         ("dt", ctypes.c_double), ("dtmax", ctypes.c_double), ("adaptivestep", ctypes.c_int),
+        ("swbuffer", ctypes.c_int), ("buf_zstart", ctypes.c_double), ("buf_sigma", ctypes.c_double),
+        ("buf_beta", ctypes.c_double),
     ]
 
 
@@ -75,8 +77,10 @@ def load(ref=False):
     lib.orc_get_itime.restype = ctypes.c_ulong
     lib.orc_get_itime.argtypes = [P]
     for fn in ("orc_set_cyclic_and_ghost", "orc_exec_viscosity", "orc_exec_thermo", "orc_exec_boundary",
-               "orc_exec_advec", "orc_exec_diff", "orc_exec_force", "orc_exec_timeloop"):
+               "orc_exec_advec", "orc_exec_diff", "orc_exec_force", "orc_exec_timeloop", "orc_exec_buffer"):
         getattr(lib, fn).argtypes = [P]
+    lib.orc_set_buffer_profile.restype = ctypes.c_int
+    lib.orc_set_buffer_profile.argtypes = [P, ctypes.c_char_p, dp]
     lib.orc_exec_pres.argtypes = [P, ctypes.c_double]
     for fn in ("orc_r2hc", "orc_hc2r"):
         getattr(lib, fn).argtypes = [ctypes.c_int, ctypes.c_int, dp, ctypes.c_long, ctypes.c_long]
@@ -125,6 +129,11 @@ class Model:
         if self.lib.orc_get_field(self.h, name.encode(), _dptr(a)) != 0:
             raise KeyError(name)
         return a
+
+    def set_buffer_profile(self, name, prof):
+        a = np.ascontiguousarray(prof, dtype=np.float64)
+        if self.lib.orc_set_buffer_profile(self.h, name.encode(), _dptr(a)) != 0:
+            raise KeyError(name)
 
     def profile(self, name):
         a = np.empty(self.kcells, dtype=np.float64)
@@ -195,6 +204,8 @@ def params_from_case(case):
     p.z0m, p.z0h = case.z0m, case.z0h
     p.dt, p.dtmax = case.dt, case.dtmax
     p.adaptivestep = 1 if case.adaptivestep else 0
+    p.swbuffer = 1 if case.swbuffer else 0
+    p.buf_zstart, p.buf_sigma, p.buf_beta = case.buffer_zstart, case.buffer_sigma, case.buffer_beta
     return p
 
 
@@ -203,4 +214,7 @@ def model_from_case(case, ref=False):
     m = Model(params_from_case(case), case.z, ref=ref)
     for name in case.prognostic_names():
         m.set(name, case.embed(case.fields[name]))
+    if case.swbuffer:
+        for name, prof in case.buffer_profiles().items():
+            m.set_buffer_profile(name, prof)
     return m

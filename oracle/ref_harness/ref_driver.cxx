@@ -1,8 +1,8 @@
 // ref_driver.cxx -- the oracle C API (mhh_oracle.h) on top of the reference's
 // own module classes (TEST INFRASTRUCTURE ONLY).  The substep follows the
 // run-mode loop of src/model.cxx:356-505; the modules are the reference's
-// Advec_2i5 / Advec_2, Diff_smag2 / Diff_2, Pres_2, Timeloop, Boundary_cyclic
-// and Boundary_surface compiled unchanged.
+// Advec_2i5 / Advec_2, Diff_smag2 / Diff_2, Pres_2, Timeloop, Boundary_cyclic,
+// Boundary_surface and Buffer compiled unchanged.
 #include <cstring>
 #include <memory>
 #include <sstream>
@@ -22,6 +22,7 @@
 #include "fft.h"
 #include "timeloop.h"
 #include "boundary_surface.h"
+#include "buffer.h"
 #include "stats.h"
 #include "constants.h"
 
@@ -42,6 +43,7 @@ struct orc_model
     std::unique_ptr<Advec<TF>> advec;
     std::unique_ptr<Diff<TF>> diff;
     std::unique_ptr<Pres<TF>> pres;
+    std::unique_ptr<Buffer<TF>> buffer;
     // The statistics object is never touched by the hot path (all its calls
     // are no-ops in the harness); it only has to exist as a reference.
     alignas(64) unsigned char stats_mem[sizeof(Stats<TF>)];
@@ -78,6 +80,10 @@ namespace
         s << "time dt - " << p->dt << "\n";
         if (p->dtmax > 0.) s << "time dtmax - " << p->dtmax << "\n";
         s << "time adaptivestep - " << (p->adaptivestep ? 1 : 0) << "\n";
+        s << "buffer swbuffer - " << (p->swbuffer ? 1 : 0) << "\n";
+        if (p->swbuffer)
+            s << "buffer zstart - " << p->buf_zstart << "\n" << "buffer sigma - " << p->buf_sigma << "\n"
+              << "buffer beta - " << p->buf_beta << "\n";
         return s.str();
     }
 
@@ -148,6 +154,7 @@ orc_model* orc_create(const orc_params* p, const double* z)
     else
         m->diff = std::make_unique<Diff_2<TF>>(m->master, *m->grid, *m->fields, *m->boundary, input);
     m->pres = std::make_unique<Pres_2<TF>>(m->master, *m->grid, *m->fields, *m->fft, input);
+    m->buffer = std::make_unique<Buffer<TF>>(m->master, *m->grid, *m->fields, input);
 
     // Grid and fields (ghost-cell counts are final now).
     m->grid->init();
@@ -174,6 +181,7 @@ orc_model* orc_create(const orc_params* p, const double* z)
 
     // Model::init and Model::load_or_save (src/model.cxx:185-300).
     m->boundary->init(input, *m->thermo, Sim_mode::Run);
+    m->buffer->init();
     m->diff->init();
     m->pres->init();
     m->boundary->set_values();
@@ -266,6 +274,19 @@ void orc_exec_boundary(orc_model* m)
 void orc_exec_advec(orc_model* m) { m->advec->exec(m->stats()); }
 void orc_exec_diff(orc_model* m) { m->diff->exec(m->stats()); }
 void orc_exec_force(orc_model* m) { exec_force(m); }
+void orc_exec_buffer(orc_model* m) { m->buffer->exec(m->stats()); }
+
+// Buffer::create (src/buffer.cxx:100-158) reads the initial profiles; it runs
+// again after every profile handed over, with the profiles given so far.
+int orc_set_buffer_profile(orc_model* m, const char* name, const double* prof)
+{
+    const std::string n(name);
+    if (!m->p.swbuffer || (n != "u" && n != "v" && n != "th")) return -1;
+    auto& gd = m->grid->get_grid_data();
+    ref_harness::set_init_profile(n, std::vector<double>(prof + gd.kstart, prof + gd.kend));
+    m->buffer->create(*m->input, *reinterpret_cast<Netcdf_handle*>(m->misc_mem), m->stats());
+    return 0;
+}
 void orc_exec_pres(orc_model* m, double sub_dt) { m->pres->exec(sub_dt, m->stats()); }
 void orc_exec_timeloop(orc_model* m) { m->timeloop->exec(); m->timeloop->step_time(); }
 
@@ -281,6 +302,7 @@ void orc_run_substeps(orc_model* m, int n)
         m->boundary->set_ghost_cells();
         orc_exec_advec(m);
         orc_exec_diff(m);
+        orc_exec_buffer(m);
         orc_exec_force(m);
         orc_exec_pres(m, m->timeloop->get_sub_time_step());
         orc_exec_timeloop(m);

@@ -29,6 +29,12 @@ namespace ref_harness
     // Heights of the ktot full levels handed to Grid<double>::create.
     void set_pending_z(const std::vector<double>& z);
 
+    // Initial profiles (ktot interior values by name) that the stand-in
+    // Netcdf_handle::get_variable returns to Buffer::create; a name without
+    // an entry reads as zeros, as a missing variable does in
+    // src/netcdf_interface.cxx:659-684.
+    void set_init_profile(const std::string& name, const std::vector<double>& prof);
+
     // Dry Boussinesq thermodynamics with prognostic "th" (restated from
     // src/thermo_dry.cxx; only what the hot path calls).
     class Thermo_dry_ref : public Thermo<double>

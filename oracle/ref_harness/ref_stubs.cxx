@@ -24,6 +24,7 @@
 #include "constants.h"
 #include "field3d_io.h"
 #include "cuda_buffer.h"
+#include "netcdf_interface.h"
 
 #include "../orc_fft.h"
 
@@ -289,10 +290,15 @@ void Fields<TF>::init_momentum_field(const std::string& name, const std::string&
     mp[name]->visc = visc;
 }
 
+// src/fields.cxx:843-846 (only called with swupdate, which the path does not use)
+template<>
+void Fields<TF>::set_calc_mean_profs(bool sw) { calc_mean_profs = sw; }
+
 template<>
 void Fields<TF>::init_prognostic_field(const std::string& name, const std::string& longname,
-        const std::string& unit, const std::string& group, const std::array<int,3>& loc, const bool&)
+        const std::string& unit, const std::string& group, const std::array<int,3>& loc, const bool& required)
 {
+    required_read[name] = required;   // src/fields.cxx:904
     sp[name] = std::make_shared<Field3d<TF>>(master, grid, name, longname, unit, group, loc);
     st[name] = std::make_shared<Field3d<TF>>(master, grid, name + "t", longname, unit, group, loc);
     ap[name] = sp[name]; at[name] = st[name];
@@ -670,4 +676,38 @@ namespace ref_harness
         auto& gd = grid.get_grid_data();
         return Constants::grav<TF>/thref[gd.kstart]*(thref[gd.kstart] - threfh[gd.kstart]);
     }
+}
+
+// ---------------------------------------------------------------------------
+// Initial profiles for Buffer::create (src/buffer.cxx:130-150), in place of
+// the "init" group of the case's NetCDF input.
+// ---------------------------------------------------------------------------
+namespace
+{
+    std::map<std::string, std::vector<double>> g_init_profiles;
+}
+
+void ref_harness::set_init_profile(const std::string& name, const std::vector<double>& prof)
+{
+    g_init_profiles[name] = prof;
+}
+
+Netcdf_group& Netcdf_handle::get_group(const std::string&)
+{
+    // Never dereferenced: get_variable below ignores the handle.
+    return *reinterpret_cast<Netcdf_group*>(this);
+}
+
+// The first prod(count) values of `values` receive the variable (the vector is
+// not resized), or zeros when it does not exist
+// (src/netcdf_interface.cxx:647-692).
+template<>
+void Netcdf_handle::get_variable<double>(std::vector<double>& values, const std::string& name,
+                                         const std::vector<int>&, const std::vector<int>& count, const bool)
+{
+    size_t n = 1;
+    for (int c : count) n *= size_t(c);
+    auto it = g_init_profiles.find(name);
+    for (size_t q=0; q<n; ++q)
+        values[q] = it != g_init_profiles.end() && q < it->second.size() ? it->second[q] : 0.;
 }

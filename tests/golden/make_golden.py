@@ -2,13 +2,14 @@
 
 The fixtures are produced by the reference's own hot-path sources
 (Advec_2i5, Advec_2, Diff_smag2, Diff_2, Pres_2, Timeloop, Boundary_cyclic,
-Boundary_surface), compiled unchanged into oracle/_ref/libmhh_ref.so by
+Boundary_surface, Buffer), compiled unchanged into oracle/_ref/libmhh_ref.so by
 ``make -C oracle ref`` (which needs the MicroHH source tree).  Each fixture
 holds the seeded initial fields and the fields and diagnostics after one RK3
 step (three substeps), so that the CPU restatement in oracle/ and the CUDA
 path can both be checked against the reference without the reference tree.
 
-Run from the repository root:  python tests/golden/make_golden.py
+Run from the repository root:  python tests/golden/make_golden.py [name ...]
+(no names: every fixture).
 """
 import os
 import sys
@@ -45,6 +46,17 @@ def golden_cases():
     c = cases.channel(16, 12, 10, seed=15, dt=1e-3, adaptivestep=True)
     c.name = "channel_16x12x10"
     out[c.name] = c
+    # Buffer layer (src/buffer.cxx) over the top third, with a mean wind and
+    # perturbations at every level so that every field is relaxed.
+    c = cases.drycbl(16, 12, 12, 1600., 1200., 1200., seed=16, noise_z=1200.)
+    rng = np.random.Generator(np.random.PCG64(16))
+    c.fields["u"] = 2.0 + 0.02 * np.arange(12)[:, None, None] + 0.3 * rng.standard_normal((12, 12, 16))
+    c.fields["v"] = -1.0 + 0.3 * rng.standard_normal((12, 12, 16))
+    c.fields["w"] = 0.1 * rng.standard_normal((12, 12, 16))
+    c.fields["w"][0] = 0.0
+    c.swbuffer, c.buffer_zstart, c.buffer_sigma, c.buffer_beta = True, 800., 0.01, 2.
+    c.name = "cbl_buffer_16x12x12"
+    out[c.name] = c
     return out
 
 
@@ -71,10 +83,16 @@ def run_reference(case, ref=True):
 def main():
     orcpy.build(ref=True)
     here = os.path.dirname(os.path.abspath(__file__))
+    only = set(sys.argv[1:])
     for name, case in golden_cases().items():
+        if only and name not in only:
+            continue
         res = run_reference(case)
         for n in case.prognostic_names():
             res["in_" + n] = case.embed(case.fields[n])
+        if case.swbuffer:
+            for n, prof in case.buffer_profiles().items():
+                res["buf_" + n] = prof
         path = os.path.join(here, name + ".npz")
         np.savez_compressed(path, **res)
         print("wrote", path, os.path.getsize(path))

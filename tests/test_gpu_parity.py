@@ -62,6 +62,9 @@ def test_golden_fp64(mhh, path, fused):
     m = mhh.Model(case, precision=mhh.FP64)
     for n in case.prognostic_names():
         m.set(n, g["in_" + n])
+    for key in g.files:
+        if key.startswith("buf_"):
+            m.set_buffer_profile(key[4:], g[key])
     m.run_substeps(3, fused=fused)
     for key in g.files:
         if key.startswith("out_"):
@@ -347,3 +350,67 @@ def test_pressure_fusion_is_bitwise(mhh, precision):
                 mhh.set_option("pres_fuse", 1)
         for n in out[0]:
             assert np.array_equal(out[0][n], out[1][n]), (case.name, n)
+
+
+def buffered_cbl(itot, jtot, ktot, seed):
+    """A dry CBL with a mean wind and perturbations at every level, and a
+    buffer layer (src/buffer.cxx) over the top third of the domain."""
+    case = cases.drycbl(itot, jtot, ktot, 100. * itot, 100. * jtot, 100. * ktot, seed=seed, noise_z=100. * ktot)
+    rng = np.random.default_rng(seed)
+    sh = (ktot, jtot, itot)
+    case.fields["u"] = 2. + 0.01 * np.arange(ktot)[:, None, None] + rng.normal(0., 0.3, sh)
+    case.fields["v"] = -1. + rng.normal(0., 0.3, sh)
+    case.fields["w"] = rng.normal(0., 0.1, sh)
+    case.fields["w"][0] = 0.
+    case.swbuffer = True
+    case.buffer_zstart = 2. / 3. * case.zsize
+    case.buffer_sigma = 0.01
+    case.buffer_beta = 2.
+    return case
+
+
+@pytest.mark.parametrize("fused", [True, False], ids=["fused", "modules"])
+def test_buffer_layer_fp64(mhh, oracle_lib, fused):
+    case = buffered_cbl(48, 40, 30, seed=61)
+    m = mhh.Model(case, precision=mhh.FP64)
+    o = oracle_lib.model_from_case(case)
+    m.run_steps(1, fused=fused)
+    o.run_substeps(3)
+    for n in case.prognostic_names() + ["p"]:
+        err = rel_err(m.get(n), o.get(n))
+        assert err <= TOL_LARGE, (n, err)
+    # The layer acts: without it the upper levels end elsewhere.
+    case.swbuffer = False
+    off = mhh.Model(case, precision=mhh.FP64)
+    off.run_steps(1, fused=fused)
+    ktop = case.ktot
+    for n in ("u", "v", "w", "th"):
+        d = np.abs(off.get(n)[ktop] - m.get(n)[ktop]).max()
+        assert d > 1e-6, (n, d)
+    m.close(); off.close(); o.close()
+
+
+def test_buffer_layer_fp32(mhh, oracle_lib):
+    """FP32 form with the buffer layer against the FP64 oracle, from the same
+    float-representable state, at the FP32 form's tolerances (2e-3 relative
+    for the velocities, 1e-4 K per RK3 step for theta)."""
+    case = buffered_cbl(48, 40, 30, seed=62)
+    for n in case.fields:
+        case.fields[n] = case.fields[n].astype(np.float32).astype(np.float64)
+    m = mhh.Model(case, precision=mhh.FP32)
+    o = oracle_lib.model_from_case(case)
+    m.run_steps(2)
+    o.run_substeps(6)
+    for n in ("u", "v", "w"):
+        err = rel_err(m.get(n), o.get(n))
+        assert err <= 2e-3, (n, err)
+    assert np.abs(case.interior(m.get("th") - o.get("th"))).max() <= 2e-4
+    m.close(); o.close()
+
+
+def test_buffer_needs_profiles(mhh):
+    case = buffered_cbl(16, 16, 12, seed=63)
+    m = mhh.Model(ini=case.to_ini(), z=case.z, precision=mhh.FP64)
+    with pytest.raises(mhh.MhhError, match="buffer"):
+        m.run_steps(1)
+    m.close()

@@ -43,6 +43,9 @@ def test_restatement_matches_reference(oracle_lib, path):
     m = oracle_lib.Model(oracle_lib.params_from_case(case), case.z)
     for n in case.prognostic_names():
         m.set(n, g["in_" + n])
+    for key in g.files:
+        if key.startswith("buf_"):
+            m.set_buffer_profile(key[4:], g[key])
     m.run_substeps(3)
     for key in g.files:
         if key.startswith("out_"):
@@ -86,3 +89,51 @@ def test_divergence_free_after_projection(oracle_lib):
     # (src/model.cxx:367-382), so the ghost cells are refreshed first.
     m.lib.orc_set_cyclic_and_ghost(m.h)
     assert m.div() < 1e-12 * max(1.0, np.abs(m.get("w")).max())
+
+
+def buffered_cbl(itot=24, jtot=20, ktot=16, seed=31):
+    """A dry CBL with a mean wind and perturbations at every level, and a
+    buffer layer over the top third of the domain."""
+    case = cases.drycbl(itot, jtot, ktot, 100. * itot, 100. * jtot, 100. * ktot, seed=seed, noise_z=100. * ktot)
+    rng = np.random.default_rng(seed)
+    sh = (ktot, jtot, itot)
+    case.fields["u"] = 2. + 0.01 * np.arange(ktot)[:, None, None] + rng.normal(0., 0.3, sh)
+    case.fields["v"] = -1. + rng.normal(0., 0.3, sh)
+    case.fields["w"] = rng.normal(0., 0.1, sh)
+    case.fields["w"][0] = 0.
+    case.swbuffer = True
+    case.buffer_zstart = 2. / 3. * case.zsize
+    case.buffer_sigma = 0.01
+    case.buffer_beta = 2.
+    return case
+
+
+def test_buffer_restatement(oracle_lib):
+    """orc_exec_buffer against src/buffer.cxx:37-59 written out with numpy:
+    at -= sigma ((z - zstart)/(zsize - zstart))^beta (a - abuf) at the levels
+    with z >= zstart (half levels and abuf = 0 for w)."""
+    case = buffered_cbl()
+    m = oracle_lib.model_from_case(case)
+    fields = {n: case.embed(case.fields[n]) for n in ("u", "v", "w", "th")}
+    for n in ("ut", "vt", "wt", "tht"):
+        m.set(n, np.zeros(m.shape))
+    m.lib.orc_exec_buffer(m.h)
+    z = np.zeros(m.kcells)
+    z[1:-1] = case.z
+    zh = np.zeros(m.kcells)
+    zh[2:-1] = 0.5 * (case.z[1:] + case.z[:-1])
+    prof = case.buffer_profiles()
+    zs, zsize = case.buffer_zstart, case.zsize
+    for n, t, lev in (("u", "ut", z), ("v", "vt", z), ("w", "wt", zh), ("th", "tht", z)):
+        want = np.zeros(m.shape)
+        abuf = prof.get(n, np.zeros(m.kcells))
+        for k in range(1, m.kcells - 1):
+            if lev[k] < zs:
+                continue
+            sig = case.buffer_sigma * ((lev[k] - zs) / (zsize - zs)) ** case.buffer_beta
+            want[k] = -sig * (fields[n][k] - abuf[k])
+        got = m.get(t)
+        inner = (slice(1, -1), slice(m.jgc, -m.jgc), slice(m.igc, -m.igc))
+        assert np.abs(got[inner] - want[inner]).max() <= 1e-15 * max(1., np.abs(want).max()), n
+        assert np.abs(want).max() > 0., n
+    m.close()
