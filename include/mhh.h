@@ -49,7 +49,8 @@ enum mhh_edge { MHH_EDGE_EW = 1, MHH_EDGE_NS = 2, MHH_EDGE_BOTH = 3 };
 typedef struct mhh_ctx mhh_ctx;
 
 /* Grid description: the inputs of Grid<TF> (src/grid.cxx:47-100) plus the
-   ghost-cell counts the schemes ask for (Advec_2i5: 3,3,1; otherwise 1,1,1). */
+   ghost-cell counts the schemes ask for (Advec_2i5: 3,3,1, or 3,3,2 with a
+   flux-limited scalar; otherwise 1,1,1). */
 typedef struct
 {
     int itot, jtot, ktot;
@@ -200,6 +201,12 @@ int mhh_boundary_surface_get(mhh_ctx* ctx, const char* name, double* out);
 /* Advec_2i5<TF>::exec (src/advec_2i5.cxx:995-1063): adds the 5th-order
    upwind advection tendencies to ut, vt, wt and st. */
 int mhh_advec_2i5_exec(mhh_ctx* ctx, const mhh_fields* f, cudaStream_t stream);
+/* Advec_2i5 with th in [advec] fluxlimit_list (src/advec_2i5.cxx:36-46,
+   1047-1056; include/advec_monotonic.h:28-219): limit_scalar = 1 advects the
+   scalar with the Koren flux limiter, in mhh_advec_2i5_exec and in the fused
+   substep.  The reference then runs with kgc = 2 (the context accepts 1 or
+   2); ktot >= 4. */
+int mhh_advec_2i5_set_fluxlimit(mhh_ctx* ctx, int limit_scalar);
 /* Advec_2<TF>::exec (src/advec_2.cxx:280-351). */
 int mhh_advec_2_exec(mhh_ctx* ctx, const mhh_fields* f, cudaStream_t stream);
 /* Advec_2i5<TF>::get_cfl / Advec_2<TF>::get_cfl (src/advec_2i5.cxx:953-971,

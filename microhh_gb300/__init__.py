@@ -135,6 +135,7 @@ def load():
     _declare(kern, "mhh_fft_forward", I, [P, P, S])
     _declare(kern, "mhh_fft_backward", I, [P, P, S])
     _declare(kern, "mhh_timeloop_rk3", I, [P, P, P, I, D, S])
+    _declare(kern, "mhh_advec_2i5_set_fluxlimit", I, [P, I])
     _declare(kern, "mhh_buffer_setup", I, [P, D, D, D])
     _declare(kern, "mhh_buffer_set_profile", I, [P, ctypes.c_char_p, dp])
     _declare(kern, "mhh_buffer_exec", I, [P, ctypes.POINTER(Fields), S])

@@ -67,6 +67,7 @@ class Case:
     buffer_zstart: float = 0.0
     buffer_sigma: float = 2.0
     buffer_beta: float = 2.0
+    fluxlimit: bool = False            # [advec] fluxlimit_list=th (Advec_2i5 only)
     fields: dict = field(default_factory=dict)   # name -> (ktot, jtot, itot) float64
 
     @property
@@ -74,23 +75,29 @@ class Case:
         return 3 if self.advec == "2i5" else 1
 
     @property
+    def kgc(self):
+        # Advec_2i5 with a flux-limited scalar asks for two vertical ghost
+        # levels (src/advec_2i5.cxx:36-46).
+        return 2 if self.advec == "2i5" and self.fluxlimit else 1
+
+    @property
     def ncells_interior(self):
         return self.itot * self.jtot * self.ktot
 
     def ghost_shape(self):
         g = self.igc
-        return (self.ktot + 2, self.jtot + 2 * g, self.itot + 2 * g)
+        return (self.ktot + 2 * self.kgc, self.jtot + 2 * g, self.itot + 2 * g)
 
     def embed(self, interior):
         """Places an interior (ktot, jtot, itot) array into a zeroed ghost layout."""
-        g = self.igc
+        g, kg = self.igc, self.kgc
         out = np.zeros(self.ghost_shape(), dtype=np.float64)
-        out[1:-1, g:g + self.jtot, g:g + self.itot] = interior
+        out[kg:kg + self.ktot, g:g + self.jtot, g:g + self.itot] = interior
         return out
 
     def interior(self, full):
-        g = self.igc
-        return full[1:-1, g:g + self.jtot, g:g + self.itot]
+        g, kg = self.igc, self.kgc
+        return full[kg:kg + self.ktot, g:g + self.jtot, g:g + self.itot]
 
     def prognostic_names(self):
         return ["u", "v", "w"] + (["th"] if self.thermo else [])
@@ -103,7 +110,8 @@ class Case:
             "[grid]", f"itot={self.itot}", f"jtot={self.jtot}", f"ktot={self.ktot}",
             f"xsize={f(self.xsize)}", f"ysize={f(self.ysize)}", f"zsize={f(self.zsize)}",
             "swspatialorder=2", "",
-            "[advec]", f"swadvec={self.advec}", f"cflmax={f(self.cflmax)}", "",
+            "[advec]", f"swadvec={self.advec}", f"cflmax={f(self.cflmax)}",
+            *(["fluxlimit_list=th"] if self.fluxlimit else []), "",
             "[diff]", f"swdiff={self.diff}", f"cs={f(self.cs)}", f"tPr={f(self.tpr)}",
             f"dnmax={f(self.dnmax)}", f"swmason={'true' if self.swmason else 'false'}", "",
             "[thermo]", f"swthermo={'dry' if self.thermo else '0'}", "swbasestate=boussinesq",
@@ -134,8 +142,8 @@ class Case:
         out = {}
         for n in ("u", "v", "th"):
             if n in self.fields:
-                prof = np.zeros(self.ktot + 2)
-                prof[1:-1] = self.fields[n].mean(axis=(1, 2))
+                prof = np.zeros(self.ktot + 2 * self.kgc)
+                prof[self.kgc:self.kgc + self.ktot] = self.fields[n].mean(axis=(1, 2))
                 out[n] = prof
         return out
 

@@ -143,6 +143,7 @@ struct mhh_ctx
     void* bufprof;
     std::vector<double> hbuf;
     int buf_on, buf_kb, buf_set;   // buf_set: bits of the u, v, th profiles given
+    int fluxlimit_s;               // Advec_2i5 advects the scalar with the flux limiter
     unsigned long long* red;      // device reduction word
     unsigned long long* red_host; // pinned host copy
     double dnmul2;                // Diff_2 multiplier
@@ -573,7 +574,8 @@ namespace
         const bool buoy = scal && c->phys.thermo;
         {
             Timed t("tendency", s);
-            launch_tendency<TF>(d, pr, a, cfg->advec, cfg->diff, surf, scal, buoy, force, opts_of(c), s);
+            const int adv = cfg->advec == MHH_ADVEC_2I5 && c->fluxlimit_s ? ADVEC_2I5_LIM : cfg->advec;
+            launch_tendency<TF>(d, pr, a, adv, cfg->diff, surf, scal, buoy, force, opts_of(c), s);
             if (c->buf_on)
                 launch_buffer<TF>(d, (const TF*)c->bufprof, c->buf_kb, CT<TF>(f->u), CT<TF>(f->v), CT<TF>(f->w),
                                   CT<TF>(f->s), T<TF>(f->ut), T<TF>(f->vt), T<TF>(f->wt), T<TF>(f->st), s);
@@ -720,8 +722,8 @@ int mhh_ctx_create(const mhh_grid_desc* desc, const double* z, int precision, co
 {
     if (!desc || !z || !phys || !out) return fail(MHH_ERR_ARG, "NULL argument");
     if (precision != MHH_FP64 && precision != MHH_FP32) return fail(MHH_ERR_ARG, "precision must be 64 or 32");
-    if (desc->itot < 1 || desc->jtot < 1 || desc->ktot < 1 || desc->igc < 1 || desc->jgc < 1 || desc->kgc != 1)
-        return fail(MHH_ERR_ARG, "bad grid sizes or ghost cells (kgc must be 1)");
+    if (desc->itot < 1 || desc->jtot < 1 || desc->ktot < 1 || desc->igc < 1 || desc->jgc < 1 || desc->kgc < 1 || desc->kgc > 2)
+        return fail(MHH_ERR_ARG, "bad grid sizes or ghost cells (kgc must be 1 or 2)");
     if (desc->igc > desc->itot || desc->jgc > desc->jtot)
         return fail(MHH_ERR_ARG, "more ghost cells than interior cells");
     if ((desc->igc >= 3 || desc->jgc >= 3) && desc->ktot < 6)
@@ -739,6 +741,7 @@ int mhh_ctx_create(const mhh_grid_desc* desc, const double* z, int precision, co
     c->buf_on = 0;
     c->buf_kb = 0;
     c->buf_set = 0;
+    c->fluxlimit_s = 0;
     c->opt_tend = c->opt_visc = c->opt_tdma = c->opt_tend_kchunk = c->opt_visc_kchunk = -2;
     c->dev_bytes = 0;
     if (cudaStreamCreateWithFlags(&c->setup, cudaStreamNonBlocking) != cudaSuccess)
@@ -1004,6 +1007,7 @@ static int tend_only(mhh_ctx* c, const mhh_fields* f, const mhh_bcfields* bc, in
     if (surf && !bc) return fail(MHH_ERR_ARG, "surface diffusion needs the boundary arrays");
     if (dif == MHH_DIFF_SMAG2 && !f->evisc) return fail(MHH_ERR_ARG, "evisc is NULL");
     if (buoy && !f->s) return fail(MHH_ERR_ARG, "buoyancy needs the scalar");
+    if (adv == MHH_ADVEC_2I5 && c->fluxlimit_s) adv = ADVEC_2I5_LIM;
     if (c->prec == MHH_FP64)
     {
         TendArgs<double> a = tend_args<double>(c, f, bc); a.fbody = fbody;
@@ -1019,6 +1023,16 @@ static int tend_only(mhh_ctx* c, const mhh_fields* f, const mhh_bcfields* bc, in
 
 int mhh_advec_2i5_exec(mhh_ctx* c, const mhh_fields* f, cudaStream_t s)
 { return tend_only(c, f, nullptr, MHH_ADVEC_2I5, 0, false, false, 0., s); }
+
+int mhh_advec_2i5_set_fluxlimit(mhh_ctx* c, int limit_scalar)
+{
+    if (!c) return fail(MHH_ERR_ARG, "NULL argument");
+    // The limiter's wall treatment needs four levels (src/advec_2i5.cxx
+    // applies separate stencils at kstart, kstart+1, kend-2 and kend-1).
+    if (limit_scalar && c->d.ktot < 4) return fail(MHH_ERR_ARG, "the flux limiter needs ktot >= 4");
+    c->fluxlimit_s = limit_scalar ? 1 : 0;
+    return MHH_OK;
+}
 
 int mhh_advec_2_exec(mhh_ctx* c, const mhh_fields* f, cudaStream_t s)
 { return tend_only(c, f, nullptr, MHH_ADVEC_2, 0, false, false, 0., s); }

@@ -8,6 +8,10 @@ namespace mhh
     void count_launch(int n = 1);
     long long launch_count();
 
+    // Advection switch passed to launch_tendency for Advec_2i5 with the flux
+    // limiter on the scalar (momentum as MHH_ADVEC_2I5).
+    constexpr int ADVEC_2I5_LIM = 26;
+
     // Kernel choices of one call: variant switches (-1 = automatic) and the
     // level-chunk height of the marching kernels (0 = default 32).
     struct KernelOpts
@@ -86,8 +90,10 @@ namespace mhh
                                                cudaStream_t s);
     template<typename TF> void launch_tendency_les(const Dims& d, const Prof<TF>& pr, const TendArgs<TF>& a,
                                                    bool surf, bool scal, bool buoy, cudaStream_t s);
+    // lim: the scalar is advected with the flux limiter.
     template<typename TF> void launch_tendency_flux(const Dims& d, const Prof<TF>& pr, const TendArgs<TF>& a,
-                                                    bool surf, bool scal, bool buoy, int kchunk, cudaStream_t s);
+                                                    bool surf, bool scal, bool buoy, bool lim, int kchunk,
+                                                    cudaStream_t s);
     // Buffer-layer relaxation, src/buffer.cxx:37-59: prof holds, kcells each,
     // sigma(z) at full levels, sigma(zh) at half levels (zero below the
     // layer) and the u, v, s buffer profiles.

@@ -299,10 +299,11 @@ namespace mhh
         const TF dxi = dxi_of<TF>(d), dyi = dyi_of<TF>(d);
         const TF* u = a.u; const TF* v = a.v; const TF* w = a.w;
 
+        constexpr bool A2I5 = ADV == MHH_ADVEC_2I5 || ADV == ADVEC_2I5_LIM;
         // u
         {
             TF t = TF(0);
-            if (ADV == MHH_ADVEC_2I5) t += advec_2i5_u(d, pr, u, v, w, c, k, dxi, dyi);
+            if (A2I5) t += advec_2i5_u(d, pr, u, v, w, c, k, dxi, dyi);
             else if (ADV == MHH_ADVEC_2) t += advec_2_u(d, pr, u, v, w, c, k, dxi, dyi);
             if (DIF == MHH_DIFF_SMAG2) t += diff_smag2_u(d, pr, u, v, w, a.evisc, a.u_fluxbot, a.u_fluxtop, SURF, c, ij, k, dxi, dyi, a.visc);
             else if (DIF == MHH_DIFF_2) t += diff_2_c(d, pr, u, c, k, a.dxidxi_t, a.dyidyi_t, a.visc);
@@ -312,7 +313,7 @@ namespace mhh
         // v
         {
             TF t = TF(0);
-            if (ADV == MHH_ADVEC_2I5) t += advec_2i5_v(d, pr, u, v, w, c, k, dxi, dyi);
+            if (A2I5) t += advec_2i5_v(d, pr, u, v, w, c, k, dxi, dyi);
             else if (ADV == MHH_ADVEC_2) t += advec_2_v(d, pr, u, v, w, c, k, dxi, dyi);
             if (DIF == MHH_DIFF_SMAG2) t += diff_smag2_v(d, pr, u, v, w, a.evisc, a.v_fluxbot, a.v_fluxtop, SURF, c, ij, k, dxi, dyi, a.visc);
             else if (DIF == MHH_DIFF_2) t += diff_2_c(d, pr, v, c, k, a.dxidxi_t, a.dyidyi_t, a.visc);
@@ -323,7 +324,7 @@ namespace mhh
         {
             TF t = TF(0);
             if (BUOY) t += TF(GRAV)/ld(pr.threfh, k)*(i2(ld(a.s, c-d.ijcells), ld(a.s, c)) - ld(pr.threfh, k));
-            if (ADV == MHH_ADVEC_2I5) t += advec_2i5_w(d, pr, u, v, w, c, k, dxi, dyi);
+            if (A2I5) t += advec_2i5_w(d, pr, u, v, w, c, k, dxi, dyi);
             else if (ADV == MHH_ADVEC_2) t += advec_2_w(d, pr, u, v, w, c, k, dxi, dyi);
             if (DIF == MHH_DIFF_SMAG2) t += diff_smag2_w(d, pr, u, v, w, a.evisc, c, k, dxi, dyi, a.visc);
             else if (DIF == MHH_DIFF_2) t += diff_2_w(d, pr, w, c, k, a.dxidxi_t, a.dyidyi_t, a.visc);
@@ -333,7 +334,8 @@ namespace mhh
         if (SCAL)
         {
             TF t = TF(0);
-            if (ADV == MHH_ADVEC_2I5) t += advec_2i5_s(d, pr, a.s, u, v, w, c, k, dxi, dyi);
+            if (ADV == ADVEC_2I5_LIM) t += advec_2i5_s_lim(d, pr, a.s, u, v, w, c, k, dxi, dyi);
+            else if (ADV == MHH_ADVEC_2I5) t += advec_2i5_s(d, pr, a.s, u, v, w, c, k, dxi, dyi);
             else if (ADV == MHH_ADVEC_2) t += advec_2_s(d, pr, a.s, u, v, w, c, k, dxi, dyi);
             if (DIF == MHH_DIFF_SMAG2)
                 t += diff_smag2_s(d, pr, a.s, a.evisc, a.s_fluxbot, a.s_fluxtop, SURF, c, ij, k,
@@ -350,6 +352,21 @@ namespace mhh
         dim3 grid((d.itot + 31)/32, (d.jtot + 7)/8, d.ktot);
         k_tendency<TF, ADV, DIF, SURF, SCAL, BUOY, FORCE><<<grid, block, 0, s>>>(d, pr, a);
         count_launch();
+    }
+
+    // Advec_2i5 with the limited scalar: only the combinations with a scalar.
+    template<typename TF, int DIF>
+    static void launch_tend_lim(const Dims& d, const Prof<TF>& pr, const TendArgs<TF>& a,
+                                bool surf, bool buoy, bool force, cudaStream_t s)
+    {
+        const int mask = (surf ? 4 : 0) | (buoy ? 2 : 0) | (force ? 1 : 0);
+        switch (mask)
+        {
+#define MHH_TEND_CASE(M) case M: launch_tend_t<TF, ADVEC_2I5_LIM, DIF, ((M) & 4) != 0, true, ((M) & 2) != 0, ((M) & 1) != 0>(d, pr, a, s); break;
+            MHH_TEND_CASE(0) MHH_TEND_CASE(1) MHH_TEND_CASE(2) MHH_TEND_CASE(3)
+            MHH_TEND_CASE(4) MHH_TEND_CASE(5) MHH_TEND_CASE(6) MHH_TEND_CASE(7)
+#undef MHH_TEND_CASE
+        }
     }
 
     template<typename TF, int ADV, int DIF>
@@ -377,11 +394,22 @@ namespace mhh
         // or in the flux-form kernel (mhh_tend_flux.cu).
         // Automatic choice (-1): the flux form for float fields, the per-cell
         // kernel (the reference's operation order) for double fields.
+        // The limited scalar (adv == ADVEC_2I5_LIM) runs in the flux-form or
+        // the per-cell kernel; the tiled kernel hands it to the flux form.
         const int var = o.tend < 0 ? (sizeof(TF) == 4 ? 2 : 0) : o.tend;
-        if (var >= 1 && adv == MHH_ADVEC_2I5 && dif == MHH_DIFF_SMAG2 && !force && d.igc >= 3 && d.jgc >= 3)
+        const bool lim = adv == ADVEC_2I5_LIM && scal;
+        if (adv == ADVEC_2I5_LIM && !scal) adv = MHH_ADVEC_2I5;
+        if (var >= 1 && (adv == MHH_ADVEC_2I5 || lim) && dif == MHH_DIFF_SMAG2 && !force && d.igc >= 3 && d.jgc >= 3)
         {
-            if (var == 2) launch_tendency_flux<TF>(d, pr, a, surf, scal, buoy, o.tend_kchunk, s);
+            if (var == 2 || lim) launch_tendency_flux<TF>(d, pr, a, surf, scal, buoy, lim, o.tend_kchunk, s);
             else launch_tendency_les<TF>(d, pr, a, surf, scal, buoy, s);
+            return;
+        }
+        if (lim)
+        {
+            if (dif == MHH_DIFF_SMAG2) launch_tend_lim<TF, MHH_DIFF_SMAG2>(d, pr, a, surf, buoy, force, s);
+            else if (dif == MHH_DIFF_2) launch_tend_lim<TF, MHH_DIFF_2>(d, pr, a, surf, buoy, force, s);
+            else launch_tend_lim<TF, 0>(d, pr, a, surf, buoy, force, s);
             return;
         }
         // With scalar work requested but no scalar pointer, or buoyancy without

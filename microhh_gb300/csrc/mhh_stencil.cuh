@@ -105,6 +105,59 @@ namespace mhh
         return t - (ftop - fbot) / ld(pr.rhoref, k) * ld(pr.dzi, k);
     }
 
+    // ---- Flux limiter, include/advec_monotonic.h:28-219 -----------------
+    // Koren (1993): the face value is the upwind value plus half the limited
+    // upwind difference, phi(r) = max(0, min(2r, (1 + 2r)/3, 2)), r the ratio
+    // of the downwind to the upwind difference; the denominator keeps at
+    // least machine epsilon (of TF) in magnitude.
+
+    template<typename TF> __device__ __forceinline__ TF tf_epsilon();
+    template<> __device__ __forceinline__ double tf_epsilon<double>() { return 2.220446049250313080847e-16; }  // 2^-52
+    template<> __device__ __forceinline__ float tf_epsilon<float>() { return 1.1920928955078125e-7f; }        // 2^-23
+
+    template<typename TF>
+    __device__ __forceinline__ TF koren_face(TF up, TF upup, TF down)
+    {
+        const TF dd = up - upup;
+        const TF ad = fabs(dd);
+        // max(a, b) as (a < b ? b : a), min(a, b) as (b < a ? b : a).
+        const TF denom = copysign(TF(1), dd)*(ad < tf_epsilon<TF>() ? tf_epsilon<TF>() : ad);
+        const TF two_r = TF(2)*(down - up)/denom;
+        const TF third = TF(1./3.)*(TF(1) + two_r);
+        const TF lim = TF(2) < third ? TF(2) : third;
+        const TF lo = lim < two_r ? lim : two_r;
+        const TF phi = TF(0) < lo ? lo : TF(0);
+        return up + TF(0.5)*phi*(up - upup);
+    }
+
+    // Limited flux vel * a through the low-side face of cell c along stride
+    // st.  side -1: first face above the bottom wall (upward flow carries the
+    // upwind value unlimited); +1: last face below the top wall (likewise
+    // for downward flow); 0: elsewhere.
+    template<typename TF>
+    __device__ __forceinline__ TF flux_koren(const TF* a, long long c, long long st, TF vel, int side)
+    {
+        if (vel >= TF(0))
+            return side < 0 ? vel*ld(a, c-st) : vel*koren_face(ld(a, c-st), ld(a, c-2*st), ld(a, c));
+        return side > 0 ? vel*ld(a, c) : vel*koren_face(ld(a, c), ld(a, c+st), ld(a, c-st));
+    }
+
+    // Scalar advection with the limiter in x, y and z; no flux through the
+    // walls (advec_s_lim, include/advec_monotonic.h:101-219; ktot >= 4).
+    template<typename TF>
+    __device__ __forceinline__ TF advec_2i5_s_lim(const Dims& d, const Prof<TF>& pr, const TF* s, const TF* u,
+                                                  const TF* v, const TF* w, long long c, int k, TF dxi, TF dyi)
+    {
+        const long long jj = d.icells, kk = d.ijcells;
+        auto side = [&](int kf) { return kf == d.kstart+1 ? -1 : (kf == d.kend-1 ? 1 : 0); };
+        const int sidet = side(k+1), sideb = side(k);
+        const TF ftop = k+1 < d.kend ? flux_koren(s, c+kk, kk, ld(w, c+kk), sidet) : TF(0);
+        const TF fbot = k > d.kstart ? flux_koren(s, c, kk, ld(w, c), sideb) : TF(0);
+        return - (flux_koren(s, c+1, 1LL, ld(u, c+1), 0) - flux_koren(s, c, 1LL, ld(u, c), 0))*dxi
+               - (flux_koren(s, c+jj, jj, ld(v, c+jj), 0) - flux_koren(s, c, jj, ld(v, c), 0))*dyi
+               - (ld(pr.rhorefh, k+1)*ftop - ld(pr.rhorefh, k)*fbot) / ld(pr.rhoref, k) * ld(pr.dzi, k);
+    }
+
     // ---- Advec_2, src/advec_2.cxx:80-202 ---------------------------------
 
     template<typename TF>

@@ -24,7 +24,9 @@
 // src/advec_2i5.cxx:150-728 (6th-order interpolation with 5th-order upwind
 // dissipation, lower orders next to the walls), include/diff_kernels.h:144-484
 // (Smagorinsky fluxes; wall fluxes from the surface model) and
-// src/thermo_dry.cxx:165-181 (buoyancy).  The sum of all fluxes is formed
+// src/thermo_dry.cxx:165-181 (buoyancy); with LIM the scalar's advective
+// fluxes are those of the flux limiter (include/advec_monotonic.h:28-219).
+// The sum of all fluxes is formed
 // before it is added to the tendency, so the result differs from the
 // reference's term-by-term accumulation by round-off only.
 #include "mhh_kernels.cuh"
@@ -91,7 +93,16 @@ namespace mhh
         return TF(0);
     }
 
-    template<typename TF, bool SURF, bool SCAL, bool BUOY>
+    // Limited advective flux through the face between sm1 and sp1 (values
+    // sm2, sm1 | sp1, sp2 along the flow axis); side as for flux_koren.
+    template<typename TF>
+    __device__ __forceinline__ TF lim_flux(TF vel, TF sm2, TF sm1, TF sp1, TF sp2, int side)
+    {
+        if (vel >= TF(0)) return side < 0 ? vel*sm1 : vel*koren_face(sm1, sm2, sp1);
+        return side > 0 ? vel*sp1 : vel*koren_face(sp1, sp2, sm1);
+    }
+
+    template<typename TF, bool SURF, bool SCAL, bool BUOY, bool LIM>
     __global__ void __launch_bounds__(NTHR, FluxOcc<TF>::v)
     k_tend_flux(Dims d, Prof<TF> pr, TendArgs<TF> a, int kchunk)
     {
@@ -280,7 +291,8 @@ namespace mhh
                     if (SCAL)
                     {
                         const TF uw = PL(U0,0,0);
-                        const TF A = adv6(uw, PL(S0,-3,0), PL(S0,-2,0), PL(S0,-1,0), PL(S0,0,0), PL(S0,1,0), PL(S0,2,0));
+                        const TF A = LIM ? lim_flux(uw, PL(S0,-2,0), PL(S0,-1,0), PL(S0,0,0), PL(S0,1,0), 0)
+                                         : adv6(uw, PL(S0,-3,0), PL(S0,-2,0), PL(S0,-1,0), PL(S0,0,0), PL(S0,1,0), PL(S0,2,0));
                         const TF D = (TF(0.5)*(PL(E0,-1,0) + PL(E0,0,0))*tpri + svisc)*(PL(S0,0,0) - PL(S0,-1,0))*dxi;
                         gx[3*NGX + gxi] = D - A;
                     }
@@ -309,7 +321,8 @@ namespace mhh
                     if (SCAL)
                     {
                         const TF vs = PL(V0,0,0);
-                        const TF A = adv6(vs, PL(S0,0,-3), PL(S0,0,-2), PL(S0,0,-1), PL(S0,0,0), PL(S0,0,1), PL(S0,0,2));
+                        const TF A = LIM ? lim_flux(vs, PL(S0,0,-2), PL(S0,0,-1), PL(S0,0,0), PL(S0,0,1), 0)
+                                         : adv6(vs, PL(S0,0,-3), PL(S0,0,-2), PL(S0,0,-1), PL(S0,0,0), PL(S0,0,1), PL(S0,0,2));
                         const TF D = (TF(0.5)*(PL(E0,0,-1) + PL(E0,0,0))*tpri + svisc)*(PL(S0,0,0) - PL(S0,0,-1))*dyi;
                         gy[3*NGY + gyi] = D - A;
                     }
@@ -333,7 +346,14 @@ namespace mhh
                 {
                     const TF ds = (SURF && kf == d.kstart) ? -sfb : ((SURF && kf == d.kend) ? -sft
                                 : (TF(0.5)*(PL(E0,0,0) + PL(E1,0,0))*tpri + svisc)*(qs[3] - qs[2])*dzhi1);
-                    gzs_t = rhoh1*(ds - zadv(qs, qw[2], ot));
+                    TF as;
+                    if (LIM)
+                    {
+                        const int side = kf == d.kstart+1 ? -1 : (kf == d.kend-1 ? 1 : 0);
+                        as = ot ? lim_flux(qw[2], qs[1], qs[2], qs[3], qs[4], side) : TF(0);
+                    }
+                    else as = zadv(qs, qw[2], ot);
+                    gzs_t = rhoh1*(ds - as);
                 }
                 // w: the full level kf between w(kf) and w(kf+1).
                 if (kf < d.kend)
@@ -394,27 +414,35 @@ namespace mhh
         cp_async_wait_all();
     }
 
-    template<typename TF, bool SURF, bool SCAL, bool BUOY>
+    template<typename TF, bool SURF, bool SCAL, bool BUOY, bool LIM = false>
     static void launch_flux_t(const Dims& d, const Prof<TF>& pr, const TendArgs<TF>& a, int kchunk, cudaStream_t s)
     {
         const size_t smem = flux_smem<TF>();
         // The shared-memory limit is set once per kernel, outside any stream
         // capture that a later call may be part of.
-        static const bool attr = cudaFuncSetAttribute(k_tend_flux<TF, SURF, SCAL, BUOY>,
+        static const bool attr = cudaFuncSetAttribute(k_tend_flux<TF, SURF, SCAL, BUOY, LIM>,
             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess;
         (void)attr;
         kchunk = min(auto_kchunk(kchunk, (long long)((d.itot + FTX - 1)/FTX)*((d.jtot + FTY - 1)/FTY), d.ktot),
                      FKCHUNK_MAX);
         dim3 grid((d.itot + FTX - 1)/FTX, (d.jtot + FTY - 1)/FTY, (d.ktot + kchunk - 1)/kchunk);
-        k_tend_flux<TF, SURF, SCAL, BUOY><<<grid, NTHR, smem, s>>>(d, pr, a, kchunk);
+        k_tend_flux<TF, SURF, SCAL, BUOY, LIM><<<grid, NTHR, smem, s>>>(d, pr, a, kchunk);
         count_launch();
     }
 
     // Advec_2i5 + Diff_smag2 (+ buoyancy) in flux form; igc, jgc >= 3.
     template<typename TF>
     void launch_tendency_flux(const Dims& d, const Prof<TF>& pr, const TendArgs<TF>& a, bool surf, bool scal,
-                              bool buoy, int kchunk, cudaStream_t s)
+                              bool buoy, bool lim, int kchunk, cudaStream_t s)
     {
+        if (lim && scal)
+        {
+            if (surf && buoy) launch_flux_t<TF, true, true, true, true>(d, pr, a, kchunk, s);
+            else if (surf) launch_flux_t<TF, true, true, false, true>(d, pr, a, kchunk, s);
+            else if (buoy) launch_flux_t<TF, false, true, true, true>(d, pr, a, kchunk, s);
+            else launch_flux_t<TF, false, true, false, true>(d, pr, a, kchunk, s);
+            return;
+        }
         const int mask = (surf ? 4 : 0) | (scal ? 2 : 0) | (buoy ? 1 : 0);
         switch (mask)
         {
@@ -429,6 +457,6 @@ namespace mhh
         }
     }
 
-    template void launch_tendency_flux<double>(const Dims&, const Prof<double>&, const TendArgs<double>&, bool, bool, bool, int, cudaStream_t);
-    template void launch_tendency_flux<float>(const Dims&, const Prof<float>&, const TendArgs<float>&, bool, bool, bool, int, cudaStream_t);
+    template void launch_tendency_flux<double>(const Dims&, const Prof<double>&, const TendArgs<double>&, bool, bool, bool, bool, int, cudaStream_t);
+    template void launch_tendency_flux<float>(const Dims&, const Prof<float>&, const TendArgs<float>&, bool, bool, bool, bool, int, cudaStream_t);
 }

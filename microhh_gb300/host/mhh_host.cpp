@@ -117,6 +117,22 @@ namespace mhh_host
         return parse<T>(v, g + "." + k);
     }
 
+    std::vector<std::string> Input::get_list(const std::string& g, const std::string& k, const std::string& s,
+                                             const std::vector<std::string>& def)
+    {
+        std::string v;
+        if (!find(g, k, s, v)) return def;
+        std::vector<std::string> out;
+        std::string tok;
+        std::istringstream ss(v);
+        while (std::getline(ss, tok, ','))
+        {
+            const size_t b = tok.find_first_not_of(" \t"), e = tok.find_last_not_of(" \t");
+            if (b != std::string::npos) out.push_back(tok.substr(b, e - b + 1));
+        }
+        return out;
+    }
+
     std::vector<std::string> Input::unused_items() const
     {
         std::vector<std::string> out;
@@ -153,7 +169,7 @@ namespace mhh_host
     // Grid
     // ---------------------------------------------------------------------
     template<typename TF>
-    Grid<TF>::Grid(Input& in, int igc)
+    Grid<TF>::Grid(Input& in, int igc, int kgc)
     {
         desc.itot = in.get_item<int>("grid", "itot", "");
         desc.jtot = in.get_item<int>("grid", "jtot", "");
@@ -163,7 +179,7 @@ namespace mhh_host
         desc.zsize = in.get_item<double>("grid", "zsize", "");
         const std::string order = in.get_item<std::string>("grid", "swspatialorder", "", "2");
         if (order != "2") throw std::runtime_error("only swspatialorder=2 is on this path");
-        desc.igc = igc; desc.jgc = igc; desc.kgc = 1;
+        desc.igc = igc; desc.jgc = igc; desc.kgc = kgc;
         std::memset(&phys, 0, sizeof(phys));
         phys.visc = in.get_item<double>("fields", "visc", "");
         phys.svisc = in.get_item<double>("fields", "svisc", "", phys.visc);
@@ -550,6 +566,23 @@ namespace mhh_host
     }
 
     template<typename TF>
+    Advec_2i5<TF>::Advec_2i5(Grid<TF>& g, Fields<TF>& f, Input& in) : Advec<TF>(g, f, in)
+    {
+        const auto list = in.get_list("advec", "fluxlimit_list", "", {});
+        for (const auto& n : list)
+            if (n != "th") throw std::runtime_error("fluxlimit_list: only th is a scalar on this path");
+        const bool lim = !list.empty() && f.sp.count("th");
+        check(mhh_advec_2i5_set_fluxlimit(g.ctx(), lim ? 1 : 0), "fluxlimit");
+    }
+
+    template<typename TF>
+    int Advec_2i5<TF>::kgc(Input& in)
+    {
+        // The limited scalar's stencil reaches two levels (src/advec_2i5.cxx:44).
+        return in.get_list("advec", "fluxlimit_list", "", {}).empty() ? 1 : 2;
+    }
+
+    template<typename TF>
     void Advec_2i5<TF>::exec(Stats<TF>&)
     {
         mhh_fields f = this->fields.dev();
@@ -752,7 +785,8 @@ namespace mhh_host
     {
         input = std::make_unique<Input>(ini_text);
         const std::string swadvec = input->get_item<std::string>("advec", "swadvec", "", "2");
-        grid = std::make_unique<Grid<TF>>(*input, swadvec == "2i5" ? 3 : 1);
+        grid = std::make_unique<Grid<TF>>(*input, swadvec == "2i5" ? 3 : 1,
+                                          swadvec == "2i5" ? Advec_2i5<TF>::kgc(*input) : 1);
     }
 
     template<typename TF>
@@ -1084,11 +1118,12 @@ namespace mhh_host
         Input in(ini_text);
         const std::string swadvec = in.get_item<std::string>("advec", "swadvec", "", "2");
         const int gc = swadvec == "2i5" ? 3 : 1;
+        const int kgc = swadvec == "2i5" && !in.get_list("advec", "fluxlimit_list", "", {}).empty() ? 2 : 1;
         mhh_grid_desc d;
         d.itot = in.get_item<int>("grid", "itot", "");
         d.jtot = in.get_item<int>("grid", "jtot", "");
         d.ktot = ktot;
-        d.igc = gc; d.jgc = gc; d.kgc = 1;
+        d.igc = gc; d.jgc = gc; d.kgc = kgc;
         d.xsize = in.get_item<double>("grid", "xsize", "");
         d.ysize = in.get_item<double>("grid", "ysize", "");
         d.zsize = in.get_item<double>("grid", "zsize", "");
@@ -1096,7 +1131,7 @@ namespace mhh_host
         check(mhh_ctx_estimate_bytes(&d, precision, &ctx), "estimate");
         const double tf = precision == MHH_FP64 ? 8. : 4.;
         const double ij = double(d.itot + 2*gc)*(d.jtot + 2*gc);
-        const double nc = ij*(d.ktot + 2);
+        const double nc = ij*(d.ktot + 2*kgc);
         // u v w th, their tendencies, p, evisc; 18 boundary arrays.
         return ctx + size_t(10.*nc*tf + 18.*ij*tf + 20.*2.*1024*1024);
     }

@@ -25,6 +25,9 @@ namespace mhh_host
             explicit Input(const std::string& ini_text);
             template<typename T> T get_item(const std::string& group, const std::string& key, const std::string& sub);
             template<typename T> T get_item(const std::string& group, const std::string& key, const std::string& sub, const T def);
+            // Comma-separated list of strings, src/input.cxx:224-263.
+            std::vector<std::string> get_list(const std::string& group, const std::string& key, const std::string& sub,
+                                              const std::vector<std::string>& def);
             std::vector<std::string> unused_items() const;
         private:
             bool find(const std::string& g, const std::string& k, const std::string& s, std::string& out);
@@ -45,7 +48,7 @@ namespace mhh_host
     class Grid
     {
         public:
-            Grid(Input&, int igc);
+            Grid(Input&, int igc, int kgc);
             ~Grid();
             void create(const std::vector<double>& z);
             const mhh_grid& get_grid_data() const { return gd; }
@@ -185,9 +188,13 @@ namespace mhh_host
     class Advec_2i5 : public Advec<TF>
     {
         public:
-            using Advec<TF>::Advec;
+            // Reads [advec] fluxlimit_list (src/advec_2i5.cxx:36-46); th in the
+            // list switches its advection to the flux limiter.
+            Advec_2i5(Grid<TF>&, Fields<TF>&, Input&);
             void exec(Stats<TF>&) override;
             int get_switch() const override { return MHH_ADVEC_2I5; }
+            // Vertical ghost cells Advec_2i5 asks for with this input.
+            static int kgc(Input&);
     };
 
     template<typename TF>

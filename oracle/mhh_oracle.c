@@ -12,6 +12,7 @@
 #include "mhh_oracle.h"
 #include "orc_fft.h"
 
+#include <float.h>
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -118,11 +119,12 @@ static double* alloc0(long n) { return (double*)calloc((size_t)(n > 0 ? n : 1), 
 static void grid_init(grid_t* g, const orc_params* p, const double* zin)
 {
     g->itot = p->itot; g->jtot = p->jtot; g->ktot = p->ktot;
-    /* Advec_2i5 asks for (3,3,1) ghost cells (src/advec_2i5.cxx:42-45);
-       all other modules on this path need (1,1,1). */
+    /* Advec_2i5 asks for (3,3,1) ghost cells, (3,3,2) with a flux-limited
+       scalar (src/advec_2i5.cxx:36-46); all other modules on this path need
+       (1,1,1). */
     g->igc = (p->advec == ORC_ADVEC_2I5) ? 3 : 1;
     g->jgc = g->igc;
-    g->kgc = 1;
+    g->kgc = (p->advec == ORC_ADVEC_2I5 && p->fluxlimit_s) ? 2 : 1;
     g->icells = g->itot + 2*g->igc;
     g->jcells = g->jtot + 2*g->jgc;
     g->kcells = g->ktot + 2*g->kgc;
@@ -489,6 +491,68 @@ static void advec_2i5_s(orc_model* m, double* st, const double* s)
             }
 }
 
+/* Flux limiter of Koren (1993), include/advec_monotonic.h:28-99: the face
+   value is the upwind value plus half the limited upwind difference,
+   phi(r) = max(0, min(2r, (1 + 2r)/3, 2)), with r the ratio of the downwind
+   to the upwind difference (its denominator kept at least machine epsilon
+   in magnitude). */
+static inline double koren_face(double up, double upup, double down)
+{
+    const double d = up - upup;
+    const double denom = copysign(1., d)*dmax(fabs(d), DBL_EPSILON);
+    const double two_r = 2.*(down - up)/denom;
+    const double phi = dmax(0., dmin(two_r, dmin((1./3.)*(1. + two_r), 2.)));
+    return up + 0.5*phi*(up - upup);
+}
+
+/* Limited flux vel * s through the face between a[c-st] and a[c] (the face
+   of cell c on its low side, stride st).  side = -1: the first face above
+   the bottom wall (upward flow takes the upwind value unlimited), +1: the
+   last face below the top wall (likewise for downward flow), 0: interior. */
+static inline double flux_koren(const double* a, long c, long st, double vel, int side)
+{
+    if (vel >= 0.)
+        return side < 0 ? vel*a[c-st] : vel*koren_face(a[c-st], a[c-2*st], a[c]);
+    return side > 0 ? vel*a[c] : vel*koren_face(a[c], a[c+st], a[c-st]);
+}
+
+/* Side argument of flux_koren for the face kf of a full-level field
+   (interior faces kstart+1 .. kend-1; ktot >= 4). */
+static inline int face_side_lim(const grid_t* g, int kf)
+{
+    return kf == g->kstart+1 ? -1 : (kf == g->kend-1 ? 1 : 0);
+}
+
+/* Scalar advection with the flux limiter, include/advec_monotonic.h:101-219
+   (advec_s_lim): limited fluxes in x, y and z; no flux through the walls;
+   the first face above the bottom and the last below the top are limited
+   only for flow away from the wall. */
+static void advec_2i5_s_lim(orc_model* m, double* st, const double* s)
+{
+    const grid_t* g = &m->g;
+    const double* u = m->u; const double* v = m->v; const double* w = m->w;
+    const long ii = 1, jj = g->icells, kk = g->ijcells;
+    const double dxi = 1./g->dx, dyi = 1./g->dy;
+    #pragma omp parallel for
+    for (int k=g->kstart; k<g->kend; ++k)
+    {
+        /* No flux through the walls (faces kstart and kend). */
+        const int top = k+1 < g->kend, bot = k > g->kstart;
+        const int st_top = face_side_lim(g, k+1), st_bot = face_side_lim(g, k);
+        for (int j=g->jstart; j<g->jend; ++j)
+            for (int i=g->istart; i<g->iend; ++i)
+            {
+                const long c = IJK(g, i, j, k);
+                const double ftop = top ? flux_koren(s, c+kk, kk, w[c+kk], st_top) : 0.;
+                const double fbot = bot ? flux_koren(s, c, kk, w[c], st_bot) : 0.;
+                st[c] +=
+                    - (flux_koren(s, c+ii, ii, u[c+ii], 0) - flux_koren(s, c, ii, u[c], 0))*dxi
+                    - (flux_koren(s, c+jj, jj, v[c+jj], 0) - flux_koren(s, c, jj, v[c], 0))*dyi
+                    - (m->rhorefh[k+1]*ftop - m->rhorefh[k]*fbot) / m->rhoref[k] * g->dzi[k];
+            }
+    }
+}
+
 /* CFL of Advec_2i5, src/advec_2i5.cxx:59-148: the vertical interpolation of
    w to the cell centre is 2nd order at kstart and kend-1, 4th order at
    kstart+1 and kend-2 and 6th order elsewhere. */
@@ -600,7 +664,8 @@ void orc_exec_advec(orc_model* m)
         advec_2i5_u(m);
         advec_2i5_v(m);
         advec_2i5_w(m);
-        if (m->p.thermo) advec_2i5_s(m, m->tht, m->th);
+        if (m->p.thermo && m->p.fluxlimit_s) advec_2i5_s_lim(m, m->tht, m->th);
+        else if (m->p.thermo) advec_2i5_s(m, m->tht, m->th);
     }
     else
     {

@@ -57,6 +57,7 @@ typedef struct
 
     int swbuffer;     /* 1: damping layer above buf_zstart ([buffer] swbuffer) */
     double buf_zstart, buf_sigma, buf_beta;
+    int fluxlimit_s;  /* 1: th advected with the flux limiter ([advec] fluxlimit_list=th; 2i5 only) */
 } orc_params;
 
 typedef struct orc_model orc_model;

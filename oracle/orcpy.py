@@ -36,7 +36,7 @@ class Params(ctypes.Structure):
         ("z0m", ctypes.c_double), ("z0h", ctypes.c_double),
         ("dt", ctypes.c_double), ("dtmax", ctypes.c_double), ("adaptivestep", ctypes.c_int),
         ("swbuffer", ctypes.c_int), ("buf_zstart", ctypes.c_double), ("buf_sigma", ctypes.c_double),
-        ("buf_beta", ctypes.c_double),
+        ("buf_beta", ctypes.c_double), ("fluxlimit_s", ctypes.c_int),
     ]
 
 
@@ -206,6 +206,7 @@ def params_from_case(case):
     p.adaptivestep = 1 if case.adaptivestep else 0
     p.swbuffer = 1 if case.swbuffer else 0
     p.buf_zstart, p.buf_sigma, p.buf_beta = case.buffer_zstart, case.buffer_sigma, case.buffer_beta
+    p.fluxlimit_s = 1 if case.fluxlimit else 0
     return p
 
 

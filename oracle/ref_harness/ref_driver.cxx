@@ -66,6 +66,7 @@ namespace
         s << "fields visc - " << p->visc << "\n" << "fields svisc - " << p->svisc << "\n";
         s << "advec swadvec - " << (p->advec == ORC_ADVEC_2I5 ? "2i5" : "2") << "\n";
         s << "advec cflmax - " << p->cflmax << "\n";
+        if (p->fluxlimit_s) s << "advec fluxlimit_list - th\n";
         s << "diff swdiff - " << (p->diff == ORC_DIFF_SMAG2 ? "smag2" : "2") << "\n";
         s << "diff cs - " << p->cs << "\n" << "diff tPr - " << p->tpr << "\n" << "diff dnmax - " << p->dnmax << "\n";
         s << "diff swmason - " << (p->swmason ? 1 : 0) << "\n";

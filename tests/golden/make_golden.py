@@ -2,7 +2,7 @@
 
 The fixtures are produced by the reference's own hot-path sources
 (Advec_2i5, Advec_2, Diff_smag2, Diff_2, Pres_2, Timeloop, Boundary_cyclic,
-Boundary_surface, Buffer), compiled unchanged into oracle/_ref/libmhh_ref.so by
+Boundary_surface, Buffer, the flux limiter of advec_monotonic.h), compiled unchanged into oracle/_ref/libmhh_ref.so by
 ``make -C oracle ref`` (which needs the MicroHH source tree).  Each fixture
 holds the seeded initial fields and the fields and diagnostics after one RK3
 step (three substeps), so that the CPU restatement in oracle/ and the CUDA
@@ -56,6 +56,19 @@ def golden_cases():
     c.fields["w"][0] = 0.0
     c.swbuffer, c.buffer_zstart, c.buffer_sigma, c.buffer_beta = True, 800., 0.01, 2.
     c.name = "cbl_buffer_16x12x12"
+    out[c.name] = c
+    # th advected with the flux limiter (src/advec_2i5.cxx fluxlimit_list;
+    # two vertical ghost levels), with sharp theta fronts so that the
+    # limiter is active.
+    c = cases.drycbl(16, 12, 12, 1600., 1200., 1200., seed=17, noise_z=1200., noise=0.5)
+    rng = np.random.Generator(np.random.PCG64(17))
+    c.fields["u"] = 2.0 + 0.5 * rng.standard_normal((12, 12, 16))
+    c.fields["v"] = -1.0 + 0.5 * rng.standard_normal((12, 12, 16))
+    c.fields["w"] = 0.3 * rng.standard_normal((12, 12, 16))
+    c.fields["w"][0] = 0.0
+    c.fields["th"][:, :, 8:] += 1.0
+    c.fluxlimit = True
+    c.name = "cbl_fluxlimit_16x12x12"
     out[c.name] = c
     return out
 

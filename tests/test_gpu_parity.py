@@ -32,6 +32,17 @@ def rel_err(a, b):
     return float(np.linalg.norm(a - b) / (scale if scale > 0 else 1.0))
 
 
+def read_levels(case, name, a):
+    """The levels of a field that the time step reads.  With two vertical
+    ghost levels (flux-limited Advec_2i5) the reference's Pres_2 uses the
+    storage of p as scratch for the packed transform and never rewrites
+    level kstart-2, which no module reads (src/pres_2.cxx:155-196, 330-358):
+    that level is left out of comparisons of p."""
+    if name == "p" and case.kgc == 2:
+        return a[case.kgc - 1:]
+    return a
+
+
 def max_err(a, b):
     """Largest pointwise error relative to the field's largest magnitude."""
     scale = np.abs(b).max()
@@ -69,7 +80,7 @@ def test_golden_fp64(mhh, path, fused):
     for key in g.files:
         if key.startswith("out_"):
             n = key[4:]
-            err = rel_err(m.get(n), g[key])
+            err = rel_err(read_levels(case, n, m.get(n)), read_levels(case, n, g[key]))
             assert err <= (TOL_EVISC if n == "evisc" else TOL64), (name, n, err)
     assert m.dt() == float(g["diag_dt"])
     for d in ("cfl", "dn"):
@@ -127,7 +138,7 @@ def test_tendency_variants_fp64(mhh, path, variant):
             m.set(n, g["in_" + n])
         m.run_substeps(3, fused=True)
         for n in case.prognostic_names() + ["p"]:
-            err = rel_err(m.get(n), g["out_" + n])
+            err = rel_err(read_levels(case, n, m.get(n)), read_levels(case, n, g["out_" + n]))
             assert err <= TOL64, (name, n, err)
     finally:
         mhh.set_option("tendency_kernel", -1)
@@ -149,7 +160,7 @@ def test_viscosity_planes_fp64(mhh, path):
         for key in g.files:
             if key.startswith("out_"):
                 n = key[4:]
-                err = rel_err(m.get(n), g[key])
+                err = rel_err(read_levels(case, n, m.get(n)), read_levels(case, n, g[key]))
                 assert err <= (TOL_EVISC if n == "evisc" else TOL64), (name, n, err)
     finally:
         mhh.set_option("viscosity_kernel", -1)
@@ -191,7 +202,7 @@ def test_tdma_rescaled_recurrence_fp64(mhh, path):
             m.set(n, g["in_" + n])
         m.run_substeps(3, fused=True)
         for n in case.prognostic_names() + ["p"]:
-            err = rel_err(m.get(n), g["out_" + n])
+            err = rel_err(read_levels(case, n, m.get(n)), read_levels(case, n, g["out_" + n]))
             assert err <= TOL64, (name, n, err)
     finally:
         mhh.set_option("tdma_kernel", -1)
@@ -414,3 +425,95 @@ def test_buffer_needs_profiles(mhh):
     with pytest.raises(mhh.MhhError, match="buffer"):
         m.run_steps(1)
     m.close()
+
+
+def limited_cbl(itot, jtot, ktot, seed):
+    """A dry CBL with th advected by the flux limiter ([advec]
+    fluxlimit_list=th), a mean wind and a theta front so that the limiter
+    clips."""
+    case = cases.drycbl(itot, jtot, ktot, 100. * itot, 100. * jtot, 100. * ktot, seed=seed,
+                        noise_z=100. * ktot, noise=0.5)
+    rng = np.random.default_rng(seed)
+    sh = (ktot, jtot, itot)
+    case.fields["u"] = 2. + rng.normal(0., 0.5, sh)
+    case.fields["v"] = -1. + rng.normal(0., 0.5, sh)
+    case.fields["w"] = rng.normal(0., 0.3, sh)
+    case.fields["w"][0] = 0.
+    case.fields["th"][:, :, itot // 2:] += 1.
+    case.fluxlimit = True
+    return case
+
+
+@pytest.mark.parametrize("variant", [0, 2], ids=["percell", "flux"])
+def test_flux_limiter_fp64(mhh, oracle_lib, variant):
+    """Limited scalar advection on a grid with partial tiles in x and y and
+    three level chunks (the last partial), in both tendency kernels, against
+    the oracle; the two vertical ghost levels of the limited grid included."""
+    case = limited_cbl(40, 20, 70, seed=71)
+    mhh.set_option("tendency_kernel", variant)
+    mhh.set_option("tendency_kchunk", 32)
+    try:
+        m = mhh.Model(case, precision=mhh.FP64)
+        assert m.grid.kgc == 2
+        o = oracle_lib.model_from_case(case)
+        m.run_steps(1, fused=True)
+        o.run_substeps(3)
+        for n in case.prognostic_names() + ["p"]:
+            err = rel_err(read_levels(case, n, m.get(n)), read_levels(case, n, o.get(n)))
+            assert err <= TOL_LARGE, (n, err)
+    finally:
+        mhh.set_option("tendency_kernel", -1)
+        mhh.set_option("tendency_kchunk", 0)
+
+
+def test_flux_limiter_fp32(mhh, oracle_lib):
+    """FP32 form (flux-form kernel with the limiter) against the FP64 oracle
+    from the same float-representable state, at the FP32 tolerances."""
+    case = limited_cbl(48, 40, 30, seed=72)
+    for n in case.fields:
+        case.fields[n] = case.fields[n].astype(np.float32).astype(np.float64)
+    m = mhh.Model(case, precision=mhh.FP32)
+    o = oracle_lib.model_from_case(case)
+    m.run_steps(1)
+    o.run_substeps(3)
+    for n in ("u", "v", "w"):
+        err = rel_err(m.get(n), o.get(n))
+        assert err <= 2e-3, (n, err)
+    assert np.abs(case.interior(m.get("th") - o.get("th"))).max() <= 1e-4
+    m.close(); o.close()
+
+
+@pytest.mark.parametrize("precision", [64, 32], ids=["fp64", "fp32"])
+def test_flux_limiter_keeps_bounds(mhh, precision):
+    """The limiter is monotone: for a two-valued theta field in a uniform
+    wind along x, one forward step with the advection tendency of
+    mhh_advec_2i5_exec creates no new extrema (CFL 0.1-0.5), where the
+    unlimited 5th-order scheme over- and undershoots."""
+    import ctypes
+
+    def tendency(limit):
+        case = cases.drycbl(32, 8, 8, 3200., 800., 800., seed=73, noise=0.)
+        case.fields["u"] = np.full((8, 8, 32), 5.)
+        th = np.full((8, 8, 32), 300.)
+        th[:, :, 8:16] = 301.
+        case.fields["th"] = th
+        case.fluxlimit = limit
+        m = mhh.Model(case, precision=precision)
+        m.set("tht", np.zeros(m.shape))
+        f, _ = m.device_fields()
+        ctx = m.ctx()
+        for p in (f.u, f.v, f.w, f.s):
+            mhh.check(m.kern.mhh_boundary_cyclic(ctx, p, 3, None))
+        mhh.check(m.kern.mhh_advec_2i5_exec(ctx, ctypes.byref(f), None))
+        m.synchronize()
+        out = case.interior(m.get("th")), case.interior(m.get("tht"))
+        m.close()
+        return out
+    tol = 1e-12 if precision == 64 else 1e-4
+    th, st = tendency(True)
+    for dt in (2., 5., 10.):
+        new = th + dt * st
+        assert new.min() >= 300. - tol and new.max() <= 301. + tol, (dt, new.min(), new.max())
+    th, st = tendency(False)
+    new = th + 5. * st
+    assert new.min() < 300. - 0.1 and new.max() > 301. + 0.1
