@@ -136,11 +136,15 @@ int mhh_ctx_estimate_bytes(const mhh_grid_desc* desc, int precision, size_t* byt
    marching in k, -1 = automatic (1 for FP32 contexts, 0 for FP64; the
    default; the neutral resolved-wall case always runs per cell);
    "tdma_kernel" 0 = the Thomas recurrence in the reference's operation order,
-   1 = the rescaled recurrence (two FP64 FMAs per cell), -1 = automatic
-   (0 for FP64 contexts, 1 for FP32 contexts; the default). */
+   1 = the rescaled recurrence (two FP64 FMAs per cell) with one column per
+   thread, 2 = the same with the four columns of one eigenvalue per thread,
+   -1 = automatic (0 for FP64 contexts, 1 for FP32 contexts; the default). */
 int mhh_set_option(const char* name, int value);
-/* "fft_column_pairs": complex sequence pairs per block of the y FFT, 4 (the
-   default) or 8.  "pres_fuse": 1 (the default) computes the Poisson
+/* "fft_pipeline": 1 (the default) runs the fixed-length FFTs as persistent
+   blocks that load their next tile while transforming the current one; 0
+   runs one tile per block.  Both give identical results.
+   "fft_column_pairs": complex sequence pairs per block of the y FFT, 4 (the
+   default) or 8 (8 uses the one-tile-per-block kernel).  "pres_fuse": 1 (the default) computes the Poisson
    right-hand side inside the forward x FFT and stores the inverse x FFT into
    the ghost layout of p; 0 runs them as separate kernels. */
 /* "tendency_kchunk" / "viscosity_kchunk": levels per block of the marching

@@ -76,6 +76,8 @@ namespace mhh
     static int g_pres_fuse = 1;
     int pres_fuse() { return g_pres_fuse; }
     int fft_column_pairs() { return g_fft_col_pairs; }
+    static int g_fft_pipeline = 1;
+    int fft_pipeline() { return g_fft_pipeline; }
     void set_fft_column_pairs(int p) { g_fft_col_pairs = p; }
     static int g_tdma_variant = -1;
     int tdma_variant() { return g_tdma_variant; }
@@ -615,7 +617,7 @@ int mhh_set_option(const char* name, int value)
     }
     if (!std::strcmp(name, "tdma_kernel"))
     {
-        if (value < -1 || value > 1) return fail(MHH_ERR_ARG, "tdma_kernel is -1, 0 or 1");
+        if (value < -1 || value > 2) return fail(MHH_ERR_ARG, "tdma_kernel is -1, 0, 1 or 2");
         set_tdma_variant(value);
         return MHH_OK;
     }
@@ -623,6 +625,12 @@ int mhh_set_option(const char* name, int value)
     {
         if (value != 0 && value != 1) return fail(MHH_ERR_ARG, "pres_fuse is 0 or 1");
         g_pres_fuse = value;
+        return MHH_OK;
+    }
+    if (!std::strcmp(name, "fft_pipeline"))
+    {
+        if (value != 0 && value != 1) return fail(MHH_ERR_ARG, "fft_pipeline is 0 or 1");
+        g_fft_pipeline = value;
         return MHH_OK;
     }
     if (!std::strcmp(name, "fft_column_pairs"))
@@ -657,7 +665,7 @@ int mhh_ctx_set_option(mhh_ctx* c, const char* name, int value)
     }
     else if (!std::strcmp(name, "tdma_kernel"))
     {
-        if (!reset && (value < -1 || value > 1)) return fail(MHH_ERR_ARG, "tdma_kernel is -2, -1, 0 or 1");
+        if (!reset && (value < -1 || value > 2)) return fail(MHH_ERR_ARG, "tdma_kernel is -2, -1, 0, 1 or 2");
         c->opt_tdma = value;
     }
     else if (!std::strcmp(name, "tendency_kchunk") || !std::strcmp(name, "viscosity_kchunk"))

@@ -149,6 +149,7 @@ namespace mhh
     void set_tdma_variant(int v);
     // Complex sequence pairs per block of the column (y) FFT: 4 or 8.
     int fft_column_pairs();
+    int fft_pipeline();
     // 1 (default): the pressure right-hand side and the scatter into p are
     // fused into the x transforms; 0: separate kernels.
     int pres_fuse();

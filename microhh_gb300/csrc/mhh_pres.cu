@@ -171,7 +171,53 @@ namespace mhh
         u[3] = cadd(c2, c3); u[7] = csub(c2, c3);
     }
 
-    template<typename TF, int N, int P, int S, int PACC>
+    // Radix-R butterfly of u[0..R-1] in place (forward), for the stage with
+    // sub-length T = N/R (general radices take their twiddles from tws).
+    template<typename TF, int N, int R, int T>
+    __device__ __forceinline__ void radix_bfly(typename C2<TF>::T* u, const typename C2<TF>::T* __restrict__ tws)
+    {
+        using T2 = typename C2<TF>::T;
+        if (R == 8) dft8<TF, T2>(u);
+        else if (R == 4)
+        {
+            const T2 a = cadd(u[0], u[2]), b = csub(u[0], u[2]);
+            const T2 c = cadd(u[1], u[3]), e = mul_mi<T2>(csub(u[1], u[3]));
+            u[0] = cadd(a, c); u[2] = csub(a, c); u[1] = cadd(b, e); u[3] = csub(b, e);
+        }
+        else if (R == 2)
+        {
+            const T2 a = u[0];
+            u[0] = cadd(a, u[1]); u[1] = csub(a, u[1]);
+        }
+        else if (R == 3)
+        {
+            const TF s3 = TF(0.86602540378443864676);
+            const T2 t1 = cadd(u[1], u[2]), t4 = csub(u[1], u[2]);
+            T2 t2; t2.x = u[0].x - TF(0.5)*t1.x; t2.y = u[0].y - TF(0.5)*t1.y;
+            u[0] = cadd(u[0], t1);
+            u[1].x = t2.x + s3*t4.y; u[1].y = t2.y - s3*t4.x;
+            u[2].x = t2.x - s3*t4.y; u[2].y = t2.y + s3*t4.x;
+        }
+        else
+        {
+            T2 v[R];
+            #pragma unroll
+            for (int r=0; r<R; ++r)
+            {
+                T2 acc = u[0];
+                #pragma unroll
+                for (int q=1; q<R; ++q) acc = cadd(acc, cmul(u[q], tws[(q*r*T) % N]));
+                v[r] = acc;
+            }
+            #pragma unroll
+            for (int r=0; r<R; ++r) u[r] = v[r];
+        }
+    }
+
+    // Stockham stages S.. of P sequences of length N, sequence q at
+    // src + q*SS (SS >= N: a padded stride keeps column stores free of bank
+    // conflicts).
+    template<typename TF, int N, int P, int S, int PACC, int SS = N>
     struct FixedStages
     {
         using T2 = typename C2<TF>::T;
@@ -186,60 +232,26 @@ namespace mhh
                 const int seq = it / T;
                 const int i = it - seq*T;
                 const int k = i % PACC;
-                const T2* x = src + seq*N;
-                T2* y = dst + seq*N;
+                const T2* x = src + seq*SS;
+                T2* y = dst + seq*SS;
                 const int j = (i - k)*R + k;
                 T2 u[R];
                 u[0] = x[i];
                 #pragma unroll
                 for (int q=1; q<R; ++q)
                     u[q] = (PACC == 1) ? x[i + q*T] : cmul(x[i + q*T], tws[(q*k*step) % N]);
-                if (R == 8) dft8<TF, T2>(u);
-                else if (R == 4)
-                {
-                    const T2 a = cadd(u[0], u[2]), b = csub(u[0], u[2]);
-                    const T2 c = cadd(u[1], u[3]), e = mul_mi<T2>(csub(u[1], u[3]));
-                    u[0] = cadd(a, c); u[2] = csub(a, c); u[1] = cadd(b, e); u[3] = csub(b, e);
-                }
-                else if (R == 2)
-                {
-                    const T2 a = u[0];
-                    u[0] = cadd(a, u[1]); u[1] = csub(a, u[1]);
-                }
-                else if (R == 3)
-                {
-                    const TF s3 = TF(0.86602540378443864676);
-                    const T2 t1 = cadd(u[1], u[2]), t4 = csub(u[1], u[2]);
-                    T2 t2; t2.x = u[0].x - TF(0.5)*t1.x; t2.y = u[0].y - TF(0.5)*t1.y;
-                    u[0] = cadd(u[0], t1);
-                    u[1].x = t2.x + s3*t4.y; u[1].y = t2.y - s3*t4.x;
-                    u[2].x = t2.x - s3*t4.y; u[2].y = t2.y + s3*t4.x;
-                }
-                else
-                {
-                    T2 v[R];
-                    #pragma unroll
-                    for (int r=0; r<R; ++r)
-                    {
-                        T2 acc = u[0];
-                        #pragma unroll
-                        for (int q=1; q<R; ++q) acc = cadd(acc, cmul(u[q], tws[(q*r*T) % N]));
-                        v[r] = acc;
-                    }
-                    #pragma unroll
-                    for (int r=0; r<R; ++r) u[r] = v[r];
-                }
+                radix_bfly<TF, N, R, T>(u, tws);
                 #pragma unroll
                 for (int r=0; r<R; ++r) y[j + r*PACC] = u[r];
             }
             __syncthreads();
             T2* t = src; src = dst; dst = t;
-            FixedStages<TF, N, P, S+1, PACC*R>::run(src, dst, tws);
+            FixedStages<TF, N, P, S+1, PACC*R, SS>::run(src, dst, tws);
         }
     };
 
-    template<typename TF, int N, int P, int S>
-    struct FixedStages<TF, N, P, S, N>
+    template<typename TF, int N, int P, int S, int SS>
+    struct FixedStages<TF, N, P, S, N, SS>
     {
         using T2 = typename C2<TF>::T;
         static __device__ __forceinline__ void run(T2*&, T2*&, const T2*) {}
@@ -249,20 +261,40 @@ namespace mhh
     // (indices without ghosts), src/pres_2.cxx:155-196: the divergence of the
     // velocity that the tendencies would give after dt.
     template<typename TF>
-    __device__ __forceinline__ TF pres_rhs(const Dims& d, const Prof<TF>& pr, const TF* __restrict__ u,
-                                           const TF* __restrict__ v, const TF* __restrict__ w,
-                                           const TF* __restrict__ ut, const TF* __restrict__ vt,
-                                           const TF* __restrict__ wt, int i, int j, int k, TF dti)
+    __device__ __forceinline__ TF pres_rhs_at(const Dims& d, const Prof<TF>& pr, const TF* __restrict__ u,
+                                              const TF* __restrict__ v, const TF* __restrict__ w,
+                                              const TF* __restrict__ ut, const TF* __restrict__ vt,
+                                              const TF* __restrict__ wt, long long c, int kg, TF dti)
     {
-        const long long c = ijk(d, i + d.igc, j + d.jgc, k + d.kgc);
         const long long ii = 1, jj = d.icells, kk = d.ijcells;
-        const int kg = k + d.kgc;
         const TF rho = ld(pr.rhoref, kg);
         return rho*((ld(ut, c+ii) + ld(u, c+ii)*dti) - (ld(ut, c) + ld(u, c)*dti))*dxi_of<TF>(d)
              + rho*((ld(vt, c+jj) + ld(v, c+jj)*dti) - (ld(vt, c) + ld(v, c)*dti))*dyi_of<TF>(d)
              + (ld(pr.rhorefh, kg+1)*(ld(wt, c+kk) + ld(w, c+kk)*dti)
               - ld(pr.rhorefh, kg  )*(ld(wt, c   ) + ld(w, c   )*dti))*ld(pr.dzi, kg);
     }
+
+    template<typename TF>
+    __device__ __forceinline__ TF pres_rhs(const Dims& d, const Prof<TF>& pr, const TF* __restrict__ u,
+                                           const TF* __restrict__ v, const TF* __restrict__ w,
+                                           const TF* __restrict__ ut, const TF* __restrict__ vt,
+                                           const TF* __restrict__ wt, int i, int j, int k, TF dti)
+    {
+        return pres_rhs_at(d, pr, u, v, w, ut, vt, wt, ijk(d, i + d.igc, j + d.jgc, k + d.kgc), k + d.kgc, dti);
+    }
+
+    // Per-sequence offsets of a tile of nloc <= 16 real sequences starting at
+    // s0, computed once per tile by its first threads (the callers
+    // synchronise before use): the base of each sequence in data (sb), and
+    // for the fused x transforms the ghost-layout offset of the row's first
+    // interior cell (sc) and its level k (sk).  Keeps the 64-bit divisions
+    // by itot or jtot out of the per-element loops.
+    struct TileIdx
+    {
+        long long sb[16];
+        long long sc[16];
+        int sk[16];
+    };
 
     // Element j of real sequence s sits at base(s) + j*stride:
     //   rows (x):    base = s*n,                         stride = 1
@@ -278,6 +310,24 @@ namespace mhh
     {
         if (L.rows) return s*(long long)n;
         return (s / L.itot)*(long long)L.itot*n + (s % L.itot);
+    }
+
+    template<typename TF>
+    __device__ __forceinline__ void tile_index(TileIdx& ti, const SeqLayout& L, const FftFuse<TF>& fz, long long s0,
+                                               int nloc, int n, bool fused)
+    {
+        const int ls = threadIdx.x;
+        if (ls < nloc)
+        {
+            const long long s = s0 + ls;
+            ti.sb[ls] = seq_base(L, s, n);
+            if (fused)
+            {
+                const int kr = (int)(s / fz.d.jtot), jr = (int)(s - (long long)kr*fz.d.jtot);
+                ti.sc[ls] = ijk(fz.d, fz.d.igc, jr + fz.d.jgc, kr + fz.d.kgc);
+                ti.sk[ls] = kr;
+            }
+        }
     }
 
     template<typename TF>
@@ -324,24 +374,25 @@ namespace mhh
         // 1. Load 2P real sequences into buf1 viewed as real [2P][n], with
         //    asynchronous copies so that all of a thread's loads are in
         //    flight together (a missing sequence reads as zero).
+        __shared__ TileIdx ti;
+        tile_index<TF>(ti, L, fz, s0, nloc, n, FUSE != 0);
+        __syncthreads();
         TF* r1 = reinterpret_cast<TF*>(buf1);
         const int tot = 2*P*n;
         if (FUSE == 1)
         {
             // Rows of the pressure right-hand side computed in place of
-            // loading them: row s is (j, k) = (s % jtot, s / jtot).  Unrolled
-            // so that the loads of several elements are in flight together.
+            // loading them.  Unrolled so that the loads of several elements
+            // are in flight together.
+            const int kgc = fz.d.kgc;
             #pragma unroll 4
             for (int e = threadIdx.x; e < tot; e += blockDim.x)
             {
                 const int ls = e / n, i = e - ls*n;
                 TF val = TF(0);
                 if (ls < nloc)
-                {
-                    const long long row = s0 + ls;
-                    const int kr = (int)(row / fz.d.jtot), jr = (int)(row - (long long)kr*fz.d.jtot);
-                    val = pres_rhs(fz.d, fz.pr, fz.u, fz.v, fz.w, fz.ut, fz.vt, fz.wt, i, jr, kr, fz.dti);
-                }
+                    val = pres_rhs_at(fz.d, fz.pr, fz.u, fz.v, fz.w, fz.ut, fz.vt, fz.wt, ti.sc[ls] + i,
+                                      ti.sk[ls] + kgc, fz.dti);
                 r1[ls*ns + i] = val;
             }
         }
@@ -351,8 +402,20 @@ namespace mhh
             {
                 const int ls = e / n, j = e - ls*n;
                 const bool ok = ls < nloc;
-                fft_cp_async(r1 + ls*ns + j, ok ? data + seq_base(L, s0 + ls, n) + j : data, ok);
+                fft_cp_async(r1 + ls*ns + j, ok ? data + ti.sb[ls] + j : data, ok);
             }
+        }
+        else if (NFIX && (256 % (2*(PFIX ? PFIX : 1))) == 0)
+        {
+            // Columns: with 2P dividing the block size every thread keeps
+            // one sequence (ls) and walks its elements.
+            const int ls = threadIdx.x % (2*P);
+            const bool ok = ls < nloc;
+            const TF* src = data + (ok ? ti.sb[ls] : 0);
+            const long long st = (long long)(blockDim.x/(2*P))*L.itot;
+            const TF* sp = src + (long long)(threadIdx.x/(2*P))*L.itot;
+            for (int j = threadIdx.x/(2*P); j < n; j += blockDim.x/(2*P), sp += st)
+                fft_cp_async(r1 + ls*ns + j, ok ? sp : data, ok);
         }
         else
         {
@@ -360,7 +423,7 @@ namespace mhh
             {
                 const int j = e / (2*P), ls = e - j*(2*P);
                 const bool ok = ls < nloc;
-                fft_cp_async(r1 + ls*ns + j, ok ? data + seq_base(L, s0 + ls, n) + (long long)j*L.itot : data, ok);
+                fft_cp_async(r1 + ls*ns + j, ok ? data + ti.sb[ls] + (long long)j*L.itot : data, ok);
             }
         }
         asm volatile("cp.async.commit_group;\n" ::: "memory");
@@ -446,12 +509,10 @@ namespace mhh
                 const int ls = e / n, i = e - ls*n;
                 if (ls < nloc)
                 {
-                    const long long row = s0 + ls;
-                    const int kr = (int)(row / fz.d.jtot), jr = (int)(row - (long long)kr*fz.d.jtot);
                     const TF val = rout[ls*ns + i];
-                    const long long c = ijk(fz.d, i + fz.d.igc, jr + fz.d.jgc, kr + fz.d.kgc);
+                    const long long c = ti.sc[ls] + i;
                     fz.p[c] = val;
-                    if (kr == 0) fz.p[c - fz.d.ijcells] = val;
+                    if (ti.sk[ls] == 0) fz.p[c - fz.d.ijcells] = val;
                 }
             }
         }
@@ -460,7 +521,18 @@ namespace mhh
             for (int e = threadIdx.x; e < tot; e += blockDim.x)
             {
                 const int ls = e / n, j = e - ls*n;
-                if (ls < nloc) data[seq_base(L, s0 + ls, n) + j] = rout[ls*ns + j];
+                if (ls < nloc) data[ti.sb[ls] + j] = rout[ls*ns + j];
+            }
+        }
+        else if (NFIX && (256 % (2*(PFIX ? PFIX : 1))) == 0)
+        {
+            const int ls = threadIdx.x % (2*P);
+            if (ls < nloc)
+            {
+                const long long st = (long long)(blockDim.x/(2*P))*L.itot;
+                TF* dp = data + ti.sb[ls] + (long long)(threadIdx.x/(2*P))*L.itot;
+                for (int j = threadIdx.x/(2*P); j < n; j += blockDim.x/(2*P), dp += st)
+                    *dp = rout[ls*ns + j];
             }
         }
         else
@@ -468,9 +540,224 @@ namespace mhh
             for (int e = threadIdx.x; e < tot; e += blockDim.x)
             {
                 const int j = e / (2*P), ls = e - j*(2*P);
-                if (ls < nloc) data[seq_base(L, s0 + ls, n) + (long long)j*L.itot] = rout[ls*ns + j];
+                if (ls < nloc) data[ti.sb[ls] + (long long)j*L.itot] = rout[ls*ns + j];
             }
         }
+    }
+
+    // ---- pipelined fixed-length transforms ----------------------------------
+    // A persistent block loops over tiles of 2P real sequences.  While it
+    // transforms tile t, the asynchronous copies of its next tile are already
+    // in flight into a second input buffer, so the loads of HBM overlap the
+    // shared-memory work of the stages (one tile per block left the memory
+    // system idle between a block's load and its store).  The packing of two
+    // real sequences into one complex one is folded into the first stage and
+    // the separation into halfcomplex order into the store.
+    //
+    // Shared memory: two input buffers and one work buffer of P*SS + P
+    // complex elements, plus the twiddle table.  Tile t's input buffer also
+    // serves as the second stage buffer; the other input buffer receives
+    // tile t + gridDim.x.
+
+    // First Stockham stage (radix R0, no twiddles) with the complex input
+    // formed from the real sequences: z = x + i y (forward) or the
+    // conjugated halfcomplex pair (inverse).  Real sequence s sits at
+    // r + s*NS.
+    template<typename TF, bool INV, int N, int P, int NS, int SS>
+    __device__ __forceinline__ void fft_first_stage(const TF* __restrict__ r, typename C2<TF>::T* __restrict__ y,
+                                                    const typename C2<TF>::T* __restrict__ tws)
+    {
+        using T2 = typename C2<TF>::T;
+        constexpr int R = fixed_radix(N, 0);
+        constexpr int T = N / R;
+        for (int it = threadIdx.x; it < P*T; it += blockDim.x)
+        {
+            const int seq = it / T, i = it - seq*T;
+            const TF* hx = r + (2*seq)*NS;
+            const TF* hy = hx + NS;
+            T2 u[R];
+            #pragma unroll
+            for (int q=0; q<R; ++q)
+            {
+                const int k = i + q*T;
+                if (!INV)
+                {
+                    u[q].x = hx[k]; u[q].y = hy[k];
+                }
+                else
+                {
+                    const int kk = k <= N/2 ? k : N - k;
+                    const bool real_only = (kk == 0) || (2*kk == N);
+                    const TF sg = k <= N/2 ? TF(1) : TF(-1);
+                    const int km = real_only ? kk : N - kk;
+                    const TF xr = hx[kk], yr = hy[kk];
+                    const TF xi = real_only ? TF(0) : sg*hx[km];
+                    const TF yi = real_only ? TF(0) : sg*hy[km];
+                    u[q].x = xr - yi;
+                    u[q].y = -(xi + yr);
+                }
+            }
+            radix_bfly<TF, N, R, T>(u, tws);
+            T2* yy = y + seq*SS + i*R;
+            #pragma unroll
+            for (int q=0; q<R; ++q) yy[q] = u[q];
+        }
+        __syncthreads();
+    }
+
+    // Real output k of real sequence ls of a tile from the transformed pairs:
+    // halfcomplex separation (forward) or real/imaginary parts (inverse).
+    template<typename TF, bool INV, int N, int SS>
+    __device__ __forceinline__ TF fft_real_out(const typename C2<TF>::T* __restrict__ res, int ls, int k, TF scale)
+    {
+        using T2 = typename C2<TF>::T;
+        const T2* rq = res + (ls >> 1)*SS;
+        const bool yseq = ls & 1;
+        if (INV)
+        {
+            const T2 a = rq[k];
+            return yseq ? -a.y*scale : a.x*scale;
+        }
+        const int kk = k <= N/2 ? k : N - k;
+        const T2 a = rq[kk], b = rq[kk == 0 ? 0 : N - kk];
+        if (k <= N/2) return yseq ? TF(0.5)*(a.y + b.y) : TF(0.5)*(a.x + b.x);
+        return yseq ? TF(-0.5)*(a.x - b.x) : TF(0.5)*(a.y - b.y);
+    }
+
+    template<typename TF, bool INV, int N, int P, int FUSE, bool ROWS>
+    __global__ void __launch_bounds__(256)
+    k_fftp(TF* __restrict__ data, SeqLayout L, TF scale, FftFuse<TF> fz, const TF* __restrict__ twt, long long ntiles)
+    {
+        using T2 = typename C2<TF>::T;
+        constexpr int NS = ROWS ? N : N + 1;      // real stride of the input view
+        constexpr int SS = ROWS ? N : N + 4;      // complex stride of the stages
+        constexpr int BUF = P*SS + P;
+        extern __shared__ __align__(16) unsigned char smem_raw[];
+        T2* bufs = reinterpret_cast<T2*>(smem_raw);
+        T2* work = bufs + BUF;
+        T2* tws = bufs + 3*BUF;
+        for (int e = threadIdx.x; e < N; e += blockDim.x)
+        { T2 w; w.x = twt[2*e]; w.y = twt[2*e+1]; tws[e] = w; }
+
+        // Asynchronous copies of tile t into input buffer b (a missing
+        // sequence reads as zero).  Each thread computes the base of the
+        // sequence it copies once per tile.
+        auto issue = [&](long long t, T2* b)
+        {
+            TF* r = reinterpret_cast<TF*>(b);
+            const long long s0 = t*2*P;
+            const int nloc = (int)min((long long)2*P, L.nseq - s0);
+            if (ROWS)
+            {
+                for (int e = threadIdx.x; e < 2*P*N; e += blockDim.x)
+                {
+                    const int ls = e / N, j = e - ls*N;
+                    const bool ok = ls < nloc;
+                    fft_cp_async(r + ls*NS + j, ok ? data + (s0 + ls)*(long long)N + j : data, ok);
+                }
+            }
+            else
+            {
+                const int ls = threadIdx.x % (2*P);
+                const bool ok = ls < nloc;
+                const long long st = (long long)(blockDim.x/(2*P))*L.itot;
+                const TF* sp = data + (ok ? seq_base(L, s0 + ls, N) : 0) + (long long)(threadIdx.x/(2*P))*L.itot;
+                for (int j = threadIdx.x/(2*P); j < N; j += blockDim.x/(2*P), sp += st)
+                    fft_cp_async(r + ls*NS + j, ok ? sp : data, ok);
+            }
+            asm volatile("cp.async.commit_group;\n" ::: "memory");
+        };
+        // Ghost-layout offsets of the current tile's rows (FUSE == 2),
+        // written after the barrier that ends the previous tile and read
+        // after the barriers of the stages.
+        __shared__ TileIdx x;
+
+        long long t = blockIdx.x;
+        int cur = 0;
+        if (t < ntiles) issue(t, bufs);
+        for (; t < ntiles; t += gridDim.x)
+        {
+            T2* in = cur ? bufs + 2*BUF : bufs;
+            asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+            __syncthreads();
+            // The other input buffer was last read by the previous tile,
+            // which every thread has finished (barrier above).
+            if (t + gridDim.x < ntiles) issue(t + gridDim.x, cur ? bufs : bufs + 2*BUF);
+            if (FUSE == 2)
+            {
+                const long long s0 = t*2*P;
+                tile_index<TF>(x, L, fz, s0, (int)min((long long)2*P, L.nseq - s0), N, true);
+            }
+
+            fft_first_stage<TF, INV, N, P, NS, SS>(reinterpret_cast<const TF*>(in), work, tws);
+            T2* src = work;
+            T2* dst = in;
+            FixedStages<TF, N, P, 1, fixed_radix(N, 0), SS>::run(src, dst, tws);
+            const T2* res = src;
+
+            const long long s0 = t*2*P;
+            const int nloc = (int)min((long long)2*P, L.nseq - s0);
+            if (FUSE == 2)
+            {
+                // Straight into the ghost layout of p, with the bottom ghost
+                // level p[kstart-1] = p[kstart] (src/pres_2.cxx:330-358).
+                for (int e = threadIdx.x; e < 2*P*N; e += blockDim.x)
+                {
+                    const int ls = e / N, i = e - ls*N;
+                    if (ls < nloc)
+                    {
+                        const TF val = fft_real_out<TF, INV, N, SS>(res, ls, i, scale);
+                        const long long c = x.sc[ls] + i;
+                        fz.p[c] = val;
+                        if (x.sk[ls] == 0) fz.p[c - fz.d.ijcells] = val;
+                    }
+                }
+            }
+            else if (ROWS)
+            {
+                for (int e = threadIdx.x; e < 2*P*N; e += blockDim.x)
+                {
+                    const int ls = e / N, j = e - ls*N;
+                    if (ls < nloc) data[(s0 + ls)*(long long)N + j] = fft_real_out<TF, INV, N, SS>(res, ls, j, scale);
+                }
+            }
+            else
+            {
+                const int ls = threadIdx.x % (2*P);
+                if (ls < nloc)
+                {
+                    const long long st = (long long)(blockDim.x/(2*P))*L.itot;
+                    TF* dp = data + seq_base(L, s0 + ls, N) + (long long)(threadIdx.x/(2*P))*L.itot;
+                    for (int j = threadIdx.x/(2*P); j < N; j += blockDim.x/(2*P), dp += st)
+                        *dp = fft_real_out<TF, INV, N, SS>(res, ls, j, scale);
+                }
+            }
+            cur ^= 1;
+        }
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    }
+
+    template<typename TF, bool INV, int N, int P, int FUSE, bool ROWS>
+    static void launch_fftp(const FftPlan& pl, TF* data, SeqLayout L, TF scale, const FftFuse<TF>& fz, cudaStream_t s)
+    {
+        using T2 = typename C2<TF>::T;
+        constexpr int SS = ROWS ? N : N + 4;
+        const size_t smem = sizeof(T2)*((size_t)3*(P*SS + P) + N);
+        const long long ntiles = (L.nseq + 2*P - 1) / (2*P);
+        // Attribute and residency are set once per kernel, outside any stream
+        // capture that a later call may be part of.
+        static const int resident = [&]
+        {
+            cudaFuncSetAttribute(k_fftp<TF, INV, N, P, FUSE, ROWS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            int per_sm = 0, dev = 0, sms = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fftp<TF, INV, N, P, FUSE, ROWS>, 256, smem);
+            cudaGetDevice(&dev);
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+            return (per_sm > 0 ? per_sm : 1)*(sms > 0 ? sms : 1);
+        }();
+        const long long nblk = ntiles < resident ? ntiles : resident;
+        const TF* twt = sizeof(TF) == 8 ? reinterpret_cast<const TF*>(pl.tw_d) : reinterpret_cast<const TF*>(pl.tw_f);
+        k_fftp<TF, INV, N, P, FUSE, ROWS><<<(unsigned)nblk, 256, smem, s>>>(data, L, scale, fz, twt, ntiles);
     }
 
     // Dynamic shared-memory limit of the run-time-plan FFT (two buffers of at
@@ -508,12 +795,26 @@ namespace mhh
         // Rows: 4 pairs per block; columns: 4 or 8 (float) pairs per block.
         constexpr int PR = (2*sizeof(typename C2<TF>::T)*4*NF <= 96*1024) ? 4 : 1;
         constexpr int PC = (sizeof(TF) == 4 && 2*sizeof(typename C2<TF>::T)*8*NF <= 96*1024) ? 8 : PR;
+        // Pipelined transforms (three buffers) where they fit in 96 KB.
+        constexpr bool PIPE_R = 3*sizeof(typename C2<TF>::T)*(PR*NF + PR) + NF*sizeof(typename C2<TF>::T) <= 96*1024;
+        constexpr bool PIPE_C = 3*sizeof(typename C2<TF>::T)*(PR*(NF + 4) + PR) + NF*sizeof(typename C2<TF>::T) <= 96*1024;
+        const bool pipe = fft_pipeline() != 0;
         if (L.rows)
         {
             if constexpr (!INV) { if (fz.mode == 1) { launch_fixed<TF, INV, NF, PR, 1>(pl, data, L, scale, fz, s); return true; } }
-            else { if (fz.mode == 2) { launch_fixed<TF, INV, NF, PR, 2>(pl, data, L, scale, fz, s); return true; } }
-            launch_fixed<TF, INV, NF, PR, 0>(pl, data, L, scale, fz, s);
+            else
+            {
+                if (fz.mode == 2)
+                {
+                    if (PIPE_R && pipe) launch_fftp<TF, INV, NF, PR, 2, true>(pl, data, L, scale, fz, s);
+                    else launch_fixed<TF, INV, NF, PR, 2>(pl, data, L, scale, fz, s);
+                    return true;
+                }
+            }
+            if (PIPE_R && pipe) launch_fftp<TF, INV, NF, PR, 0, true>(pl, data, L, scale, fz, s);
+            else launch_fixed<TF, INV, NF, PR, 0>(pl, data, L, scale, fz, s);
         }
+        else if (PIPE_C && pipe && fft_column_pairs() == 4) launch_fftp<TF, INV, NF, PR, 0, false>(pl, data, L, scale, fz, s);
         else if (fft_column_pairs() == 4 || PC == PR) launch_fixed<TF, INV, NF, PR, 0>(pl, data, L, scale, fz, s);
         else launch_fixed<TF, INV, NF, PC, 0>(pl, data, L, scale, fz, s);
         return true;
@@ -939,6 +1240,87 @@ namespace mhh
         }
     }
 
+    // The rescaled solve with one column per thread: the four columns that
+    // share the coefficients of one eigenvalue (i, itot-i) x (j, jtot-j) sit
+    // in four adjacent lanes, which read the same table entries in one
+    // transaction.  Four times the threads of k_tdma_scaled, so that the FP64
+    // recurrences and the loads of the next levels of other warps overlap.
+    constexpr int TDC_KF = 8;
+
+    template<typename TF>
+    __global__ void __launch_bounds__(128)
+    k_tdma_col(int itot, int jtot, int ktot, int niu, int nju, const double* __restrict__ gtab,
+               const double* __restrict__ htab, const float* __restrict__ stab, const double* __restrict__ stabd,
+               TF* __restrict__ pk, double* __restrict__ work)
+    {
+        const int t = blockIdx.x*blockDim.x + threadIdx.x;
+        const int iu = t >> 2, q = t & 3;
+        const int ju = blockIdx.y;
+        if (iu >= niu) return;
+        const int i1 = (iu == 0 || 2*iu == itot) ? -1 : itot - iu;
+        const int j1 = (ju == 0 || 2*ju == jtot) ? -1 : jtot - ju;
+        // Lane q holds column (q&1 ? itot-i : i, q&2 ? jtot-j : j); a mirror
+        // that coincides with the first column has no lane.
+        if (((q & 1) && i1 < 0) || ((q & 2) && j1 < 0)) return;
+        const int col = ((q & 1) ? i1 : iu) + ((q & 2) ? j1 : ju)*itot;
+        const long long stride = (long long)niu*nju;
+        const long long kk = (long long)itot*jtot;
+        const long long base = iu + (long long)ju*niu;
+
+        // Forward: z_k = p_k - g_k z_{k-1}.
+        double z = 0.;
+        for (int k0=0; k0<ktot; k0+=TDC_KF)
+        {
+            const int nk = min(TDC_KF, ktot - k0);
+            double g[TDC_KF];
+            TF pv[TDC_KF];
+            #pragma unroll
+            for (int b=0; b<TDC_KF; ++b)
+                if (b < nk)
+                {
+                    g[b] = __ldg(gtab + base + (long long)(k0 + b)*stride);
+                    pv[b] = pk[col + (long long)(k0 + b)*kk];
+                }
+            #pragma unroll
+            for (int b=0; b<TDC_KF; ++b)
+                if (b < nk)
+                {
+                    z = fma(-g[b], z, to_f64<TF>(pv[b]));
+                    work[col + (long long)(k0 + b)*kk] = z;
+                }
+        }
+        // Backward: xi_k = z_k - h_k xi_{k+1}; x_k = s_k xi_k.
+        {
+            const long long k = ktot - 1;
+            const float s = __ldg(stab + base + k*stride);
+            const double sd = sizeof(TF) == 8 ? __ldg(stabd + base + k*stride) : 0.;
+            pk[col + k*kk] = scale_out<TF>(z, s, sd);
+        }
+        for (int k0=ktot-2; k0>=0; k0-=TDC_KF)
+        {
+            const int nk = min(TDC_KF, k0 + 1);
+            double h[TDC_KF], sd[TDC_KF], zv[TDC_KF];
+            float s[TDC_KF];
+            #pragma unroll
+            for (int b=0; b<TDC_KF; ++b)
+                if (b < nk)
+                {
+                    const long long k = k0 - b;
+                    h[b] = __ldg(htab + base + k*stride);
+                    s[b] = __ldg(stab + base + k*stride);
+                    sd[b] = sizeof(TF) == 8 ? __ldg(stabd + base + k*stride) : 0.;
+                    zv[b] = work[col + k*kk];
+                }
+            #pragma unroll
+            for (int b=0; b<TDC_KF; ++b)
+                if (b < nk)
+                {
+                    z = fma(-h[b], z, zv[b]);
+                    pk[col + (long long)(k0 - b)*kk] = scale_out<TF>(z, s[b], sd[b]);
+                }
+        }
+    }
+
     int tdma_table(PresWork& pw, int itot, int jtot, int ktot, cudaStream_t s)
     {
         pw.niu = itot/2 + 1;
@@ -962,6 +1344,12 @@ namespace mhh
         dim3 grid((pw.niu + 127)/128, pw.nju);
         const int v = o.tdma < 0 ? (sizeof(TF) == 4 ? 1 : 0) : o.tdma;
         if (v == 1)
+        {
+            dim3 gridc((4*pw.niu + 127)/128, pw.nju);
+            k_tdma_col<TF><<<gridc, 128, 0, s>>>(d.itot, d.jtot, d.ktot, pw.niu, pw.nju, pw.gtab, pw.htab,
+                                                 pw.stab, pw.stabd, pk, pw.work);
+        }
+        else if (v == 2)
             k_tdma_scaled<TF><<<grid, 128, 0, s>>>(d.itot, d.jtot, d.ktot, pw.niu, pw.nju, pw.gtab, pw.htab,
                                                    pw.stab, pw.stabd, pk, pw.work);
         else

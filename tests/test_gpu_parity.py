@@ -363,6 +363,26 @@ def test_pressure_fusion_is_bitwise(mhh, precision):
             assert np.array_equal(out[0][n], out[1][n]), (case.name, n)
 
 
+@pytest.mark.parametrize("precision", [64, 32], ids=["fp64", "fp32"])
+def test_fft_pipeline_is_bitwise(mhh, precision):
+    """The persistent, prefetching FFT kernels give the same fields bit for
+    bit as one tile per block (fixed lengths 64, 48, 128, 96; partial last
+    tiles)."""
+    for case in (cases.drycbl(64, 48, 20, 6400., 4800., 2000., seed=65, noise_z=600.),
+                 cases.drycbl(128, 96, 13, 12800., 9600., 1300., seed=66, noise_z=600.)):
+        out = []
+        for pipe in (0, 1):
+            mhh.set_option("fft_pipeline", pipe)
+            try:
+                m = mhh.Model(case, precision=precision)
+                m.run_steps(2)
+                out.append({n: m.get(n) for n in case.prognostic_names() + ["p"]})
+            finally:
+                mhh.set_option("fft_pipeline", 1)
+        for n in out[0]:
+            assert np.array_equal(out[0][n], out[1][n]), (case.name, n)
+
+
 def buffered_cbl(itot, jtot, ktot, seed):
     """A dry CBL with a mean wind and perturbations at every level, and a
     buffer layer (src/buffer.cxx) over the top third of the domain."""
