@@ -214,10 +214,15 @@ namespace mhh
         }
     }
 
+    // Shared-memory position of complex element idx of a stage buffer: with
+    // SWZ one element of padding per 16, so that the strided writes of the
+    // first stages (element i*R + r of thread i) spread over all banks.
+    template<bool SWZ> __device__ __forceinline__ int swz(int idx) { return SWZ ? idx + (idx >> 4) : idx; }
+
     // Stockham stages S.. of P sequences of length N, sequence q at
     // src + q*SS (SS >= N: a padded stride keeps column stores free of bank
     // conflicts).
-    template<typename TF, int N, int P, int S, int PACC, int SS = N>
+    template<typename TF, int N, int P, int S, int PACC, int SS = N, bool SWZ = false>
     struct FixedStages
     {
         using T2 = typename C2<TF>::T;
@@ -232,26 +237,25 @@ namespace mhh
                 const int seq = it / T;
                 const int i = it - seq*T;
                 const int k = i % PACC;
-                const T2* x = src + seq*SS;
-                T2* y = dst + seq*SS;
-                const int j = (i - k)*R + k;
+                const int xb = seq*SS + i;
+                const int j = seq*SS + (i - k)*R + k;
                 T2 u[R];
-                u[0] = x[i];
+                u[0] = src[swz<SWZ>(xb)];
                 #pragma unroll
                 for (int q=1; q<R; ++q)
-                    u[q] = (PACC == 1) ? x[i + q*T] : cmul(x[i + q*T], tws[(q*k*step) % N]);
+                    u[q] = (PACC == 1) ? src[swz<SWZ>(xb + q*T)] : cmul(src[swz<SWZ>(xb + q*T)], tws[(q*k*step) % N]);
                 radix_bfly<TF, N, R, T>(u, tws);
                 #pragma unroll
-                for (int r=0; r<R; ++r) y[j + r*PACC] = u[r];
+                for (int r=0; r<R; ++r) dst[swz<SWZ>(j + r*PACC)] = u[r];
             }
             __syncthreads();
             T2* t = src; src = dst; dst = t;
-            FixedStages<TF, N, P, S+1, PACC*R, SS>::run(src, dst, tws);
+            FixedStages<TF, N, P, S+1, PACC*R, SS, SWZ>::run(src, dst, tws);
         }
     };
 
-    template<typename TF, int N, int P, int S, int SS>
-    struct FixedStages<TF, N, P, S, N, SS>
+    template<typename TF, int N, int P, int S, int SS, bool SWZ>
+    struct FixedStages<TF, N, P, S, N, SS, SWZ>
     {
         using T2 = typename C2<TF>::T;
         static __device__ __forceinline__ void run(T2*&, T2*&, const T2*) {}
@@ -559,11 +563,19 @@ namespace mhh
     // serves as the second stage buffer; the other input buffer receives
     // tile t + gridDim.x.
 
+    // Complex elements of one buffer of the pipelined kernel: P sequences at
+    // stride SS (N for rows, N + 4 for columns) with the swizzle padding, and
+    // at least the real input view of 2P sequences at stride NS.
+    __host__ __device__ constexpr int fftp_buf(int N, int P, bool rows)
+    {
+        return (P*(rows ? N : N + 4)*17)/16 + 16 + P;
+    }
+
     // First Stockham stage (radix R0, no twiddles) with the complex input
     // formed from the real sequences: z = x + i y (forward) or the
     // conjugated halfcomplex pair (inverse).  Real sequence s sits at
     // r + s*NS.
-    template<typename TF, bool INV, int N, int P, int NS, int SS>
+    template<typename TF, bool INV, int N, int P, int NS, int SS, bool SWZ>
     __device__ __forceinline__ void fft_first_stage(const TF* __restrict__ r, typename C2<TF>::T* __restrict__ y,
                                                     const typename C2<TF>::T* __restrict__ tws)
     {
@@ -598,28 +610,28 @@ namespace mhh
                 }
             }
             radix_bfly<TF, N, R, T>(u, tws);
-            T2* yy = y + seq*SS + i*R;
+            const int yb = seq*SS + i*R;
             #pragma unroll
-            for (int q=0; q<R; ++q) yy[q] = u[q];
+            for (int q=0; q<R; ++q) y[swz<SWZ>(yb + q)] = u[q];
         }
         __syncthreads();
     }
 
     // Real output k of real sequence ls of a tile from the transformed pairs:
     // halfcomplex separation (forward) or real/imaginary parts (inverse).
-    template<typename TF, bool INV, int N, int SS>
+    template<typename TF, bool INV, int N, int SS, bool SWZ>
     __device__ __forceinline__ TF fft_real_out(const typename C2<TF>::T* __restrict__ res, int ls, int k, TF scale)
     {
         using T2 = typename C2<TF>::T;
-        const T2* rq = res + (ls >> 1)*SS;
+        const int qb = (ls >> 1)*SS;
         const bool yseq = ls & 1;
         if (INV)
         {
-            const T2 a = rq[k];
+            const T2 a = res[swz<SWZ>(qb + k)];
             return yseq ? -a.y*scale : a.x*scale;
         }
         const int kk = k <= N/2 ? k : N - k;
-        const T2 a = rq[kk], b = rq[kk == 0 ? 0 : N - kk];
+        const T2 a = res[swz<SWZ>(qb + kk)], b = res[swz<SWZ>(qb + (kk == 0 ? 0 : N - kk))];
         if (k <= N/2) return yseq ? TF(0.5)*(a.y + b.y) : TF(0.5)*(a.x + b.x);
         return yseq ? TF(-0.5)*(a.x - b.x) : TF(0.5)*(a.y - b.y);
     }
@@ -631,7 +643,7 @@ namespace mhh
         using T2 = typename C2<TF>::T;
         constexpr int NS = ROWS ? N : N + 1;      // real stride of the input view
         constexpr int SS = ROWS ? N : N + 4;      // complex stride of the stages
-        constexpr int BUF = P*SS + P;
+        constexpr int BUF = fftp_buf(N, P, ROWS);
         extern __shared__ __align__(16) unsigned char smem_raw[];
         T2* bufs = reinterpret_cast<T2*>(smem_raw);
         T2* work = bufs + BUF;
@@ -689,10 +701,12 @@ namespace mhh
                 tile_index<TF>(x, L, fz, s0, (int)min((long long)2*P, L.nseq - s0), N, true);
             }
 
-            fft_first_stage<TF, INV, N, P, NS, SS>(reinterpret_cast<const TF*>(in), work, tws);
+            // The swizzle pays off for rows; the padded column stride
+            // already spreads the column stores.
+            fft_first_stage<TF, INV, N, P, NS, SS, ROWS>(reinterpret_cast<const TF*>(in), work, tws);
             T2* src = work;
             T2* dst = in;
-            FixedStages<TF, N, P, 1, fixed_radix(N, 0), SS>::run(src, dst, tws);
+            FixedStages<TF, N, P, 1, fixed_radix(N, 0), SS, ROWS>::run(src, dst, tws);
             const T2* res = src;
 
             const long long s0 = t*2*P;
@@ -706,7 +720,7 @@ namespace mhh
                     const int ls = e / N, i = e - ls*N;
                     if (ls < nloc)
                     {
-                        const TF val = fft_real_out<TF, INV, N, SS>(res, ls, i, scale);
+                        const TF val = fft_real_out<TF, INV, N, SS, ROWS>(res, ls, i, scale);
                         const long long c = x.sc[ls] + i;
                         fz.p[c] = val;
                         if (x.sk[ls] == 0) fz.p[c - fz.d.ijcells] = val;
@@ -718,7 +732,7 @@ namespace mhh
                 for (int e = threadIdx.x; e < 2*P*N; e += blockDim.x)
                 {
                     const int ls = e / N, j = e - ls*N;
-                    if (ls < nloc) data[(s0 + ls)*(long long)N + j] = fft_real_out<TF, INV, N, SS>(res, ls, j, scale);
+                    if (ls < nloc) data[(s0 + ls)*(long long)N + j] = fft_real_out<TF, INV, N, SS, ROWS>(res, ls, j, scale);
                 }
             }
             else
@@ -729,7 +743,7 @@ namespace mhh
                     const long long st = (long long)(blockDim.x/(2*P))*L.itot;
                     TF* dp = data + seq_base(L, s0 + ls, N) + (long long)(threadIdx.x/(2*P))*L.itot;
                     for (int j = threadIdx.x/(2*P); j < N; j += blockDim.x/(2*P), dp += st)
-                        *dp = fft_real_out<TF, INV, N, SS>(res, ls, j, scale);
+                        *dp = fft_real_out<TF, INV, N, SS, ROWS>(res, ls, j, scale);
                 }
             }
             cur ^= 1;
@@ -741,8 +755,7 @@ namespace mhh
     static void launch_fftp(const FftPlan& pl, TF* data, SeqLayout L, TF scale, const FftFuse<TF>& fz, cudaStream_t s)
     {
         using T2 = typename C2<TF>::T;
-        constexpr int SS = ROWS ? N : N + 4;
-        const size_t smem = sizeof(T2)*((size_t)3*(P*SS + P) + N);
+        const size_t smem = sizeof(T2)*((size_t)3*fftp_buf(N, P, ROWS) + N);
         const long long ntiles = (L.nseq + 2*P - 1) / (2*P);
         // Attribute and residency are set once per kernel, outside any stream
         // capture that a later call may be part of.
@@ -796,8 +809,8 @@ namespace mhh
         constexpr int PR = (2*sizeof(typename C2<TF>::T)*4*NF <= 96*1024) ? 4 : 1;
         constexpr int PC = (sizeof(TF) == 4 && 2*sizeof(typename C2<TF>::T)*8*NF <= 96*1024) ? 8 : PR;
         // Pipelined transforms (three buffers) where they fit in 96 KB.
-        constexpr bool PIPE_R = 3*sizeof(typename C2<TF>::T)*(PR*NF + PR) + NF*sizeof(typename C2<TF>::T) <= 96*1024;
-        constexpr bool PIPE_C = 3*sizeof(typename C2<TF>::T)*(PR*(NF + 4) + PR) + NF*sizeof(typename C2<TF>::T) <= 96*1024;
+        constexpr bool PIPE_R = sizeof(typename C2<TF>::T)*(3*fftp_buf(NF, PR, true) + NF) <= 96*1024;
+        constexpr bool PIPE_C = sizeof(typename C2<TF>::T)*(3*fftp_buf(NF, PR, false) + NF) <= 96*1024;
         const bool pipe = fft_pipeline() != 0;
         if (L.rows)
         {

@@ -82,6 +82,41 @@ namespace mhh
         return vel*i6ws(a, b, c, d, e, f) - fabs(vel)*i5ws(a, b, c, d, e, f);
     }
 
+    // Two advective fluxes at once in packed float pairs (one FP32x2
+    // instruction per pair of operations): the x- and y-face fluxes of one
+    // field.  Same arithmetic as adv6 per component, fused differently.
+    __device__ __forceinline__ float2 adv6x2(float2 vel, float2 a, float2 b, float2 c, float2 d, float2 e, float2 f)
+    {
+        const float2 one_m = make_float2(-1.f, -1.f);
+        const float2 p1 = __fadd2_rn(c, d), p2 = __fadd2_rn(b, e), p3 = __fadd2_rn(a, f);
+        const float2 m1 = __ffma2_rn(c, one_m, d), m2 = __ffma2_rn(b, one_m, e), m3 = __ffma2_rn(a, one_m, f);
+        const float2 i6 = __ffma2_rn(p1, make_float2(37.f/60.f, 37.f/60.f),
+                                     __ffma2_rn(p2, make_float2(-8.f/60.f, -8.f/60.f),
+                                                __fmul2_rn(p3, make_float2(1.f/60.f, 1.f/60.f))));
+        const float2 i5 = __ffma2_rn(m1, make_float2(10.f/60.f, 10.f/60.f),
+                                     __ffma2_rn(m2, make_float2(-5.f/60.f, -5.f/60.f),
+                                                __fmul2_rn(m3, make_float2(1.f/60.f, 1.f/60.f))));
+        const float2 nav = make_float2(-fabsf(vel.x), -fabsf(vel.y));
+        return __ffma2_rn(vel, i6, __fmul2_rn(nav, i5));
+    }
+
+    __device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
+    __device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+
+    // Vertical advective fluxes of two fields (queues qa, qb) through the
+    // same face with face velocities wf.x, wf.y (order as zadv).
+    __device__ __forceinline__ float2 zadv2(const float (&qa)[6], const float (&qb)[6], float2 wf, int order)
+    {
+        if (order == 6)
+            return adv6x2(wf, f2(qa[0], qb[0]), f2(qa[1], qb[1]), f2(qa[2], qb[2]), f2(qa[3], qb[3]),
+                          f2(qa[4], qb[4]), f2(qa[5], qb[5]));
+        if (order == 4)
+            return f2(wf.x*i4ws(qa[1], qa[2], qa[3], qa[4]) - fabsf(wf.x)*i3ws(qa[1], qa[2], qa[3], qa[4]),
+                      wf.y*i4ws(qb[1], qb[2], qb[3], qb[4]) - fabsf(wf.y)*i3ws(qb[1], qb[2], qb[3], qb[4]));
+        if (order == 2) return f2(wf.x*i2(qa[2], qa[3]), wf.y*i2(qb[2], qb[3]));
+        return f2(0.f, 0.f);
+    }
+
     // Vertical advective flux through the face between queue entries 2 and 3
     // (queue entry q holds level m-2+q of the own column).
     template<typename TF>
@@ -263,68 +298,141 @@ namespace mhh
             {
                 const TF txy = (TF(0.25)*(PL(E0,-1,-1) + PL(E0,0,-1) + PL(E0,-1,0) + PL(E0,0,0)) + visc)
                              * ((PL(U0,0,0) - PL(U0,0,-1))*dyi + (PL(V0,0,0) - PL(V0,-1,0))*dxi);
-                txz = (TF(0.25)*(PL(E0,-1,0) + PL(E0,0,0) + PL(E1,-1,0) + PL(E1,0,0)) + visc)
-                    * ((PL(U1,0,0) - PL(U0,0,0))*dzhi1 + (PL(W1,0,0) - PL(W1,-1,0))*dxi);
-                tyz = (TF(0.25)*(PL(E0,0,-1) + PL(E0,0,0) + PL(E1,0,-1) + PL(E1,0,0)) + visc)
-                    * ((PL(V1,0,0) - PL(V0,0,0))*dzhi1 + (PL(W1,0,0) - PL(W1,0,-1))*dyi);
-                if (face_x)
+                if constexpr (sizeof(TF) == 4)
                 {
-                    // u at the cell centre i-1.
-                    {
-                        const TF uw = i2(PL(U0,-1,0), PL(U0,0,0));
-                        const TF A = adv6(uw, PL(U0,-3,0), PL(U0,-2,0), PL(U0,-1,0), PL(U0,0,0), PL(U0,1,0), PL(U0,2,0));
-                        const TF D = TF(2)*(PL(E0,-1,0) + visc)*(PL(U0,0,0) - PL(U0,-1,0))*dxi;
-                        gx[0*NGX + gxi] = D - A;
-                    }
-                    // v at (i-1/2, j-1/2).
-                    {
-                        const TF uw = i2(PL(U0,0,-1), PL(U0,0,0));
-                        const TF A = adv6(uw, PL(V0,-3,0), PL(V0,-2,0), PL(V0,-1,0), PL(V0,0,0), PL(V0,1,0), PL(V0,2,0));
-                        gx[1*NGX + gxi] = txy - A;
-                    }
-                    // w at (i-1/2, m+1/2).
-                    {
-                        const TF uw = i2(PL(U0,0,0), PL(U1,0,0));
-                        const TF A = adv6(uw, PL(W1,-3,0), PL(W1,-2,0), PL(W1,-1,0), PL(W1,0,0), PL(W1,1,0), PL(W1,2,0));
-                        gx[2*NGX + gxi] = txz - A;
-                    }
+                    // tau_xz and tau_yz in one packed pair.
+                    const float2 e = __ffma2_rn(__fadd2_rn(__fadd2_rn(f2(PL(E0,-1,0), PL(E0,0,-1)), f2(PL(E0,0,0), PL(E0,0,0))),
+                                                           __fadd2_rn(f2(PL(E1,-1,0), PL(E1,0,-1)), f2(PL(E1,0,0), PL(E1,0,0)))),
+                                                f2(0.25f, 0.25f), f2(visc, visc));
+                    const float2 g = __ffma2_rn(sub2(f2(PL(U1,0,0), PL(V1,0,0)), f2(PL(U0,0,0), PL(V0,0,0))), f2(dzhi1, dzhi1),
+                                                __fmul2_rn(sub2(f2(PL(W1,0,0), PL(W1,0,0)), f2(PL(W1,-1,0), PL(W1,0,-1))),
+                                                           f2(dxi, dyi)));
+                    const float2 t = __fmul2_rn(e, g);
+                    txz = t.x; tyz = t.y;
+                }
+                else
+                {
+                    txz = (TF(0.25)*(PL(E0,-1,0) + PL(E0,0,0) + PL(E1,-1,0) + PL(E1,0,0)) + visc)
+                        * ((PL(U1,0,0) - PL(U0,0,0))*dzhi1 + (PL(W1,0,0) - PL(W1,-1,0))*dxi);
+                    tyz = (TF(0.25)*(PL(E0,0,-1) + PL(E0,0,0) + PL(E1,0,-1) + PL(E1,0,0)) + visc)
+                        * ((PL(V1,0,0) - PL(V0,0,0))*dzhi1 + (PL(W1,0,0) - PL(W1,0,-1))*dyi);
+                }
+                if constexpr (sizeof(TF) == 4)
+                {
+                    // Float form: the x- and y-face advective fluxes of each
+                    // field in packed pairs (both computed by every face
+                    // thread; the plane holds the stencils of the edge faces).
+                    const float2 Au = adv6x2(make_float2(i2(PL(U0,-1,0), PL(U0,0,0)), i2(PL(V0,-1,0), PL(V0,0,0))),
+                                             make_float2(PL(U0,-3,0), PL(U0,0,-3)), make_float2(PL(U0,-2,0), PL(U0,0,-2)),
+                                             make_float2(PL(U0,-1,0), PL(U0,0,-1)), make_float2(PL(U0,0,0), PL(U0,0,0)),
+                                             make_float2(PL(U0,1,0), PL(U0,0,1)), make_float2(PL(U0,2,0), PL(U0,0,2)));
+                    const float2 Av = adv6x2(make_float2(i2(PL(U0,0,-1), PL(U0,0,0)), i2(PL(V0,0,-1), PL(V0,0,0))),
+                                             make_float2(PL(V0,-3,0), PL(V0,0,-3)), make_float2(PL(V0,-2,0), PL(V0,0,-2)),
+                                             make_float2(PL(V0,-1,0), PL(V0,0,-1)), make_float2(PL(V0,0,0), PL(V0,0,0)),
+                                             make_float2(PL(V0,1,0), PL(V0,0,1)), make_float2(PL(V0,2,0), PL(V0,0,2)));
+                    const float2 Aw = adv6x2(make_float2(i2(PL(U0,0,0), PL(U1,0,0)), i2(PL(V0,0,0), PL(V1,0,0))),
+                                             make_float2(PL(W1,-3,0), PL(W1,0,-3)), make_float2(PL(W1,-2,0), PL(W1,0,-2)),
+                                             make_float2(PL(W1,-1,0), PL(W1,0,-1)), make_float2(PL(W1,0,0), PL(W1,0,0)),
+                                             make_float2(PL(W1,1,0), PL(W1,0,1)), make_float2(PL(W1,2,0), PL(W1,0,2)));
+                    float2 As = make_float2(0.f, 0.f);
                     if (SCAL)
                     {
-                        const TF uw = PL(U0,0,0);
-                        const TF A = LIM ? lim_flux(uw, PL(S0,-2,0), PL(S0,-1,0), PL(S0,0,0), PL(S0,1,0), 0)
-                                         : adv6(uw, PL(S0,-3,0), PL(S0,-2,0), PL(S0,-1,0), PL(S0,0,0), PL(S0,1,0), PL(S0,2,0));
-                        const TF D = (TF(0.5)*(PL(E0,-1,0) + PL(E0,0,0))*tpri + svisc)*(PL(S0,0,0) - PL(S0,-1,0))*dxi;
-                        gx[3*NGX + gxi] = D - A;
+                        if (LIM)
+                            As = make_float2(lim_flux(PL(U0,0,0), PL(S0,-2,0), PL(S0,-1,0), PL(S0,0,0), PL(S0,1,0), 0),
+                                             lim_flux(PL(V0,0,0), PL(S0,0,-2), PL(S0,0,-1), PL(S0,0,0), PL(S0,0,1), 0));
+                        else
+                            As = adv6x2(make_float2(PL(U0,0,0), PL(V0,0,0)),
+                                        make_float2(PL(S0,-3,0), PL(S0,0,-3)), make_float2(PL(S0,-2,0), PL(S0,0,-2)),
+                                        make_float2(PL(S0,-1,0), PL(S0,0,-1)), make_float2(PL(S0,0,0), PL(S0,0,0)),
+                                        make_float2(PL(S0,1,0), PL(S0,0,1)), make_float2(PL(S0,2,0), PL(S0,0,2)));
+                    }
+                    // Normal diffusive fluxes of u (x) and v (y), and of s in
+                    // x and y, in packed pairs.
+                    const float2 eo = f2(PL(E0,-1,0), PL(E0,0,-1));
+                    const float2 h2 = f2(dxi, dyi);
+                    const float2 Duv = __fmul2_rn(__fmul2_rn(__fadd2_rn(eo, f2(visc, visc)), f2(2.f, 2.f)),
+                                                  __fmul2_rn(sub2(f2(PL(U0,0,0), PL(V0,0,0)), f2(PL(U0,-1,0), PL(V0,0,-1))), h2));
+                    float2 Ds = f2(0.f, 0.f);
+                    if (SCAL)
+                        Ds = __fmul2_rn(__ffma2_rn(__fmul2_rn(__fadd2_rn(eo, f2(PL(E0,0,0), PL(E0,0,0))), f2(0.5f, 0.5f)),
+                                                   f2(tpri, tpri), f2(svisc, svisc)),
+                                        __fmul2_rn(sub2(f2(PL(S0,0,0), PL(S0,0,0)), f2(PL(S0,-1,0), PL(S0,0,-1))), h2));
+                    if (face_x)
+                    {
+                        gx[0*NGX + gxi] = Duv.x - Au.x;
+                        gx[1*NGX + gxi] = txy - Av.x;
+                        gx[2*NGX + gxi] = txz - Aw.x;
+                        if (SCAL) gx[3*NGX + gxi] = Ds.x - As.x;
+                    }
+                    if (face_y)
+                    {
+                        gy[0*NGY + gyi] = txy - Au.y;
+                        gy[1*NGY + gyi] = Duv.y - Av.y;
+                        gy[2*NGY + gyi] = tyz - Aw.y;
+                        if (SCAL) gy[3*NGY + gyi] = Ds.y - As.y;
                     }
                 }
-                if (face_y)
+                else
                 {
-                    // u at (i-1/2, j-1/2).
+                    if (face_x)
                     {
-                        const TF vs = i2(PL(V0,-1,0), PL(V0,0,0));
-                        const TF A = adv6(vs, PL(U0,0,-3), PL(U0,0,-2), PL(U0,0,-1), PL(U0,0,0), PL(U0,0,1), PL(U0,0,2));
-                        gy[0*NGY + gyi] = txy - A;
+                        // u at the cell centre i-1.
+                        {
+                            const TF uw = i2(PL(U0,-1,0), PL(U0,0,0));
+                            const TF A = adv6(uw, PL(U0,-3,0), PL(U0,-2,0), PL(U0,-1,0), PL(U0,0,0), PL(U0,1,0), PL(U0,2,0));
+                            const TF D = TF(2)*(PL(E0,-1,0) + visc)*(PL(U0,0,0) - PL(U0,-1,0))*dxi;
+                            gx[0*NGX + gxi] = D - A;
+                        }
+                        // v at (i-1/2, j-1/2).
+                        {
+                            const TF uw = i2(PL(U0,0,-1), PL(U0,0,0));
+                            const TF A = adv6(uw, PL(V0,-3,0), PL(V0,-2,0), PL(V0,-1,0), PL(V0,0,0), PL(V0,1,0), PL(V0,2,0));
+                            gx[1*NGX + gxi] = txy - A;
+                        }
+                        // w at (i-1/2, m+1/2).
+                        {
+                            const TF uw = i2(PL(U0,0,0), PL(U1,0,0));
+                            const TF A = adv6(uw, PL(W1,-3,0), PL(W1,-2,0), PL(W1,-1,0), PL(W1,0,0), PL(W1,1,0), PL(W1,2,0));
+                            gx[2*NGX + gxi] = txz - A;
+                        }
+                        if (SCAL)
+                        {
+                            const TF uw = PL(U0,0,0);
+                            const TF A = LIM ? lim_flux(uw, PL(S0,-2,0), PL(S0,-1,0), PL(S0,0,0), PL(S0,1,0), 0)
+                                             : adv6(uw, PL(S0,-3,0), PL(S0,-2,0), PL(S0,-1,0), PL(S0,0,0), PL(S0,1,0), PL(S0,2,0));
+                            const TF D = (TF(0.5)*(PL(E0,-1,0) + PL(E0,0,0))*tpri + svisc)*(PL(S0,0,0) - PL(S0,-1,0))*dxi;
+                            gx[3*NGX + gxi] = D - A;
+                        }
                     }
-                    // v at the cell centre j-1.
+                    if (face_y)
                     {
-                        const TF vs = i2(PL(V0,0,-1), PL(V0,0,0));
-                        const TF A = adv6(vs, PL(V0,0,-3), PL(V0,0,-2), PL(V0,0,-1), PL(V0,0,0), PL(V0,0,1), PL(V0,0,2));
-                        const TF D = TF(2)*(PL(E0,0,-1) + visc)*(PL(V0,0,0) - PL(V0,0,-1))*dyi;
-                        gy[1*NGY + gyi] = D - A;
-                    }
-                    // w at (j-1/2, m+1/2).
-                    {
-                        const TF vs = i2(PL(V0,0,0), PL(V1,0,0));
-                        const TF A = adv6(vs, PL(W1,0,-3), PL(W1,0,-2), PL(W1,0,-1), PL(W1,0,0), PL(W1,0,1), PL(W1,0,2));
-                        gy[2*NGY + gyi] = tyz - A;
-                    }
-                    if (SCAL)
-                    {
-                        const TF vs = PL(V0,0,0);
-                        const TF A = LIM ? lim_flux(vs, PL(S0,0,-2), PL(S0,0,-1), PL(S0,0,0), PL(S0,0,1), 0)
-                                         : adv6(vs, PL(S0,0,-3), PL(S0,0,-2), PL(S0,0,-1), PL(S0,0,0), PL(S0,0,1), PL(S0,0,2));
-                        const TF D = (TF(0.5)*(PL(E0,0,-1) + PL(E0,0,0))*tpri + svisc)*(PL(S0,0,0) - PL(S0,0,-1))*dyi;
-                        gy[3*NGY + gyi] = D - A;
+                        // u at (i-1/2, j-1/2).
+                        {
+                            const TF vs = i2(PL(V0,-1,0), PL(V0,0,0));
+                            const TF A = adv6(vs, PL(U0,0,-3), PL(U0,0,-2), PL(U0,0,-1), PL(U0,0,0), PL(U0,0,1), PL(U0,0,2));
+                            gy[0*NGY + gyi] = txy - A;
+                        }
+                        // v at the cell centre j-1.
+                        {
+                            const TF vs = i2(PL(V0,0,-1), PL(V0,0,0));
+                            const TF A = adv6(vs, PL(V0,0,-3), PL(V0,0,-2), PL(V0,0,-1), PL(V0,0,0), PL(V0,0,1), PL(V0,0,2));
+                            const TF D = TF(2)*(PL(E0,0,-1) + visc)*(PL(V0,0,0) - PL(V0,0,-1))*dyi;
+                            gy[1*NGY + gyi] = D - A;
+                        }
+                        // w at (j-1/2, m+1/2).
+                        {
+                            const TF vs = i2(PL(V0,0,0), PL(V1,0,0));
+                            const TF A = adv6(vs, PL(W1,0,-3), PL(W1,0,-2), PL(W1,0,-1), PL(W1,0,0), PL(W1,0,1), PL(W1,0,2));
+                            gy[2*NGY + gyi] = tyz - A;
+                        }
+                        if (SCAL)
+                        {
+                            const TF vs = PL(V0,0,0);
+                            const TF A = LIM ? lim_flux(vs, PL(S0,0,-2), PL(S0,0,-1), PL(S0,0,0), PL(S0,0,1), 0)
+                                             : adv6(vs, PL(S0,0,-3), PL(S0,0,-2), PL(S0,0,-1), PL(S0,0,0), PL(S0,0,1), PL(S0,0,2));
+                            const TF D = (TF(0.5)*(PL(E0,0,-1) + PL(E0,0,0))*tpri + svisc)*(PL(S0,0,0) - PL(S0,0,-1))*dyi;
+                            gy[3*NGY + gyi] = D - A;
+                        }
                     }
                 }
             }
@@ -340,8 +448,17 @@ namespace mhh
                 // face, or the surface model's flux at the walls.
                 const TF du = (SURF && kf == d.kstart) ? -ufb : ((SURF && kf == d.kend) ? -uft : txz);
                 const TF dv = (SURF && kf == d.kstart) ? -vfb : ((SURF && kf == d.kend) ? -vft : tyz);
-                gzu_t = rhoh1*(du - zadv(qu, i2(PL(W1,-1,0), PL(W1,0,0)), ot));
-                gzv_t = rhoh1*(dv - zadv(qv, i2(PL(W1,0,-1), PL(W1,0,0)), ot));
+                if constexpr (sizeof(TF) == 4)
+                {
+                    const float2 A = zadv2(qu, qv, f2(i2(PL(W1,-1,0), PL(W1,0,0)), i2(PL(W1,0,-1), PL(W1,0,0))), ot);
+                    const float2 g = __fmul2_rn(f2(rhoh1, rhoh1), sub2(f2(du, dv), A));
+                    gzu_t = g.x; gzv_t = g.y;
+                }
+                else
+                {
+                    gzu_t = rhoh1*(du - zadv(qu, i2(PL(W1,-1,0), PL(W1,0,0)), ot));
+                    gzv_t = rhoh1*(dv - zadv(qv, i2(PL(W1,0,-1), PL(W1,0,0)), ot));
+                }
                 if (SCAL)
                 {
                     const TF ds = (SURF && kf == d.kstart) ? -sfb : ((SURF && kf == d.kend) ? -sft
@@ -393,10 +510,23 @@ namespace mhh
             {
                 const int gx0 = gxi, gy0 = gyi;
                 const TF zf = prof[5*PLEV + lq - 1];
-                a.ut[c] = tu + (gx[0*NGX + gx0 + 1] - gx[0*NGX + gx0])*dxi
-                             + (gy[0*NGY + gy0 + FTX] - gy[0*NGY + gy0])*dyi + (gzu_t - gzu_b)*zf;
-                a.vt[c] = tv + (gx[1*NGX + gx0 + 1] - gx[1*NGX + gx0])*dxi
-                             + (gy[1*NGY + gy0 + FTX] - gy[1*NGY + gy0])*dyi + (gzv_t - gzv_b)*zf;
+                if constexpr (sizeof(TF) == 4)
+                {
+                    // u and v in one packed pair.
+                    const float2 dgx = sub2(f2(gx[0*NGX + gx0 + 1], gx[1*NGX + gx0 + 1]), f2(gx[0*NGX + gx0], gx[1*NGX + gx0]));
+                    const float2 dgy = sub2(f2(gy[0*NGY + gy0 + FTX], gy[1*NGY + gy0 + FTX]), f2(gy[0*NGY + gy0], gy[1*NGY + gy0]));
+                    const float2 dgz = sub2(f2(gzu_t, gzv_t), f2(gzu_b, gzv_b));
+                    const float2 t = __ffma2_rn(dgz, f2(zf, zf), __ffma2_rn(dgy, f2(dyi, dyi),
+                                                __ffma2_rn(dgx, f2(dxi, dxi), f2(tu, tv))));
+                    a.ut[c] = t.x; a.vt[c] = t.y;
+                }
+                else
+                {
+                    a.ut[c] = tu + (gx[0*NGX + gx0 + 1] - gx[0*NGX + gx0])*dxi
+                                 + (gy[0*NGY + gy0 + FTX] - gy[0*NGY + gy0])*dyi + (gzu_t - gzu_b)*zf;
+                    a.vt[c] = tv + (gx[1*NGX + gx0 + 1] - gx[1*NGX + gx0])*dxi
+                                 + (gy[1*NGY + gy0 + FTX] - gy[1*NGY + gy0])*dyi + (gzv_t - gzv_b)*zf;
+                }
                 if (wlev)
                     a.wt[c + d.ijcells] = tw + (gx[2*NGX + gx0 + 1] - gx[2*NGX + gx0])*dxi
                                              + (gy[2*NGY + gy0 + FTX] - gy[2*NGY + gy0])*dyi
