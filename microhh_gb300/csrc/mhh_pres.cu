@@ -388,16 +388,51 @@ namespace mhh
             // Rows of the pressure right-hand side computed in place of
             // loading them.  Unrolled so that the loads of several elements
             // are in flight together.
+            // RB elements per thread at a time with all their loads issued
+            // before the arithmetic (twelve loads each), so that the
+            // latency of HBM is covered by the loads of several elements.
             const int kgc = fz.d.kgc;
-            #pragma unroll 4
-            for (int e = threadIdx.x; e < tot; e += blockDim.x)
+            constexpr int RB = 4;
+            const long long ii = 1, jj = fz.d.icells, kk = fz.d.ijcells;
+            for (int e0 = threadIdx.x; e0 < tot; e0 += RB*blockDim.x)
             {
-                const int ls = e / n, i = e - ls*n;
-                TF val = TF(0);
-                if (ls < nloc)
-                    val = pres_rhs_at(fz.d, fz.pr, fz.u, fz.v, fz.w, fz.ut, fz.vt, fz.wt, ti.sc[ls] + i,
-                                      ti.sk[ls] + kgc, fz.dti);
-                r1[ls*ns + i] = val;
+                TF vals[RB][12];
+                int kgs[RB];
+                #pragma unroll
+                for (int b=0; b<RB; ++b)
+                {
+                    const int e = e0 + b*blockDim.x;
+                    const int ls = e / n, i = e - ls*n;
+                    const bool ok = e < tot && ls < nloc;
+                    // A masked element reads the first interior cell (a valid
+                    // address) and is stored as zero below.
+                    const long long c = ok ? ti.sc[ls] + i : ti.sc[0];
+                    kgs[b] = (ok ? ti.sk[ls] : ti.sk[0]) + kgc;
+                    vals[b][0] = ld(fz.ut, c+ii); vals[b][1] = ld(fz.u, c+ii);
+                    vals[b][2] = ld(fz.ut, c);    vals[b][3] = ld(fz.u, c);
+                    vals[b][4] = ld(fz.vt, c+jj); vals[b][5] = ld(fz.v, c+jj);
+                    vals[b][6] = ld(fz.vt, c);    vals[b][7] = ld(fz.v, c);
+                    vals[b][8] = ld(fz.wt, c+kk); vals[b][9] = ld(fz.w, c+kk);
+                    vals[b][10] = ld(fz.wt, c);   vals[b][11] = ld(fz.w, c);
+                }
+                #pragma unroll
+                for (int b=0; b<RB; ++b)
+                {
+                    const int e = e0 + b*blockDim.x;
+                    if (e < tot)
+                    {
+                        const int ls = e / n, i = e - ls*n;
+                        const TF* x = vals[b];
+                        const int kg = kgs[b];
+                        const TF rho = ld(fz.pr.rhoref, kg);
+                        const TF dti = fz.dti;
+                        const TF val = rho*((x[0] + x[1]*dti) - (x[2] + x[3]*dti))*dxi_of<TF>(fz.d)
+                                     + rho*((x[4] + x[5]*dti) - (x[6] + x[7]*dti))*dyi_of<TF>(fz.d)
+                                     + (ld(fz.pr.rhorefh, kg+1)*(x[8] + x[9]*dti)
+                                      - ld(fz.pr.rhorefh, kg  )*(x[10] + x[11]*dti))*ld(fz.pr.dzi, kg);
+                        r1[ls*ns + i] = ls < nloc ? val : TF(0);
+                    }
+                }
             }
         }
         else if (L.rows)

@@ -510,6 +510,8 @@ namespace mhh
     // cell of the full ghost layout so that the tendencies' ghost cells are
     // zeroed after the last substep as on the CPU.
     // ---------------------------------------------------------------------
+    constexpr int PRK = 1;
+
     template<typename TF, bool SCAL>
     __global__ void __launch_bounds__(256)
     k_presout_rk3(Dims d, Prof<TF> pr, const TF* __restrict__ p,
@@ -517,33 +519,41 @@ namespace mhh
                   TF* __restrict__ ut, TF* __restrict__ vt, TF* __restrict__ wt, TF* __restrict__ st,
                   TF cbdt, TF ca, int last)
     {
+        // PRK consecutive levels per thread: twice the loads in flight per
+        // thread, and the pressure of level k is reused for level k+1.
         const int i = blockIdx.x*blockDim.x + threadIdx.x;
         const int j = blockIdx.y*blockDim.y + threadIdx.y;
-        const int k = blockIdx.z;
         if (i >= d.icells || j >= d.jcells) return;
-        const long long c = ijk(d, i, j, k);
-        const bool interior = i >= d.istart && i < d.iend && j >= d.jstart && j < d.jend && k >= d.kstart && k < d.kend;
-        if (interior)
+        const bool col_in = i >= d.istart && i < d.iend && j >= d.jstart && j < d.jend;
+        const int kb = blockIdx.z*PRK;
+        #pragma unroll
+        for (int q=0; q<PRK; ++q)
         {
-            const TF pc = ld(p, c);
-            TF tu = ut[c] - (pc - ld(p, c-1))*dxi_of<TF>(d);
-            TF tv = vt[c] - (pc - ld(p, c-d.icells))*dyi_of<TF>(d);
-            TF tw = wt[c] - (pc - ld(p, c-d.ijcells))*ld(pr.dzhi, k);
-            u[c] += cbdt*tu; v[c] += cbdt*tv; w[c] += cbdt*tw;
-            ut[c] = last ? TF(0) : tu*ca;
-            vt[c] = last ? TF(0) : tv*ca;
-            wt[c] = last ? TF(0) : tw*ca;
-            if (SCAL)
+            const int k = kb + q;
+            if (k >= d.kcells) break;
+            const long long c = ijk(d, i, j, k);
+            if (col_in && k >= d.kstart && k < d.kend)
             {
-                const TF ts = st[c];
-                s[c] += cbdt*ts;
-                st[c] = last ? TF(0) : ts*ca;
+                const TF pc = ld(p, c);
+                TF tu = ut[c] - (pc - ld(p, c-1))*dxi_of<TF>(d);
+                TF tv = vt[c] - (pc - ld(p, c-d.icells))*dyi_of<TF>(d);
+                TF tw = wt[c] - (pc - ld(p, c-d.ijcells))*ld(pr.dzhi, k);
+                u[c] += cbdt*tu; v[c] += cbdt*tv; w[c] += cbdt*tw;
+                ut[c] = last ? TF(0) : tu*ca;
+                vt[c] = last ? TF(0) : tv*ca;
+                wt[c] = last ? TF(0) : tw*ca;
+                if (SCAL)
+                {
+                    const TF ts = st[c];
+                    s[c] += cbdt*ts;
+                    st[c] = last ? TF(0) : ts*ca;
+                }
             }
-        }
-        else if (last)
-        {
-            ut[c] = TF(0); vt[c] = TF(0); wt[c] = TF(0);
-            if (SCAL) st[c] = TF(0);
+            else if (last)
+            {
+                ut[c] = TF(0); vt[c] = TF(0); wt[c] = TF(0);
+                if (SCAL) st[c] = TF(0);
+            }
         }
     }
 
@@ -555,7 +565,7 @@ namespace mhh
         const double cB[3] = {1./3., 15./16., 8./15.};
         const int sn = (substep + 1) % 3;
         dim3 block(32, 8);
-        dim3 grid((d.icells + 31)/32, (d.jcells + 7)/8, d.kcells);
+        dim3 grid((d.icells + 31)/32, (d.jcells + 7)/8, (d.kcells + PRK - 1)/PRK);
         if (s)
             k_presout_rk3<TF, true><<<grid, block, 0, strm>>>(d, pr, p, u, v, w, s, ut, vt, wt, st, TF(cB[substep]*dt), TF(cA[sn]), sn == 0);
         else

@@ -181,10 +181,26 @@ namespace mhh
             {
                 const TF dzt = lev[0*VPLEV + lq + 1];
                 exy[b*NXY + ey*VNX + ex] = sq((Q(U0,0,0) - Q(U0,0,-1))*dyi + (Q(V0,0,0) - Q(V0,-1,0))*dxi);
-                if (ey < VTY)
-                    exz[bt*NXZ + ey*VNX + ex] = sq((Q(U1,0,0) - Q(U0,0,0))*dzt + (Q(W1,0,0) - Q(W1,-1,0))*dxi);
-                if (ex < VTX)
-                    eyz[bt*NYZ + ey*VTX + ex] = sq((Q(V1,0,0) - Q(V0,0,0))*dzt + (Q(W1,0,0) - Q(W1,0,-1))*dyi);
+                if constexpr (sizeof(TF) == 4)
+                {
+                    // The xz and yz edges in one packed pair.
+                    const float2 m1 = make_float2(-1.f, -1.f);
+                    const float2 g = __ffma2_rn(__ffma2_rn(make_float2(Q(U0,0,0), Q(V0,0,0)), m1, make_float2(Q(U1,0,0), Q(V1,0,0))),
+                                                make_float2(dzt, dzt),
+                                                __fmul2_rn(__ffma2_rn(make_float2(Q(W1,-1,0), Q(W1,0,-1)), m1,
+                                                                      make_float2(Q(W1,0,0), Q(W1,0,0))),
+                                                           make_float2(dxi, dyi)));
+                    const float2 g2 = __fmul2_rn(g, g);
+                    if (ey < VTY) exz[bt*NXZ + ey*VNX + ex] = g2.x;
+                    if (ex < VTX) eyz[bt*NYZ + ey*VTX + ex] = g2.y;
+                }
+                else
+                {
+                    if (ey < VTY)
+                        exz[bt*NXZ + ey*VNX + ex] = sq((Q(U1,0,0) - Q(U0,0,0))*dzt + (Q(W1,0,0) - Q(W1,-1,0))*dxi);
+                    if (ex < VTX)
+                        eyz[bt*NYZ + ey*VTX + ex] = sq((Q(V1,0,0) - Q(V0,0,0))*dzt + (Q(W1,0,0) - Q(W1,0,-1))*dyi);
+                }
             }
 
             // Normal gradients and, at the surface level, the special terms,
@@ -230,16 +246,30 @@ namespace mhh
             if (write)
             {
                 const TF* xy = exy + b*NXY + ey*VNX + ex;
-                acc += TF(0.125)*(xy[0] + xy[1] + xy[VNX] + xy[VNX+1]);
                 if (!(SURF && m == d.kstart))
                 {
                     const TF* zt = exz + bt*NXZ + ey*VNX + ex;
                     const TF* zb = exz + bb*NXZ + ey*VNX + ex;
                     const TF* yt = eyz + bt*NYZ + ey*VTX + ex;
                     const TF* yb = eyz + bb*NYZ + ey*VTX + ex;
-                    acc += TF(0.125)*(zb[0] + zb[1] + zt[0] + zt[1])
-                         + TF(0.125)*(yb[0] + yb[VTX] + yt[0] + yt[VTX]);
+                    if constexpr (sizeof(TF) == 4)
+                    {
+                        // Sums of the xy / xz / yz edge groups: three of the
+                        // four-term sums in packed pairs.
+                        const float2 s1 = __fadd2_rn(__fadd2_rn(make_float2(xy[0], zb[0]), make_float2(xy[1], zb[1])),
+                                                     __fadd2_rn(make_float2(xy[VNX], zt[0]), make_float2(xy[VNX+1], zt[1])));
+                        const TF sy = (yb[0] + yb[VTX]) + (yt[0] + yt[VTX]);
+                        acc += TF(0.125)*s1.x + (TF(0.125)*s1.y + TF(0.125)*sy);
+                    }
+                    else
+                    {
+                        acc += TF(0.125)*(xy[0] + xy[1] + xy[VNX] + xy[VNX+1]);
+                        acc += TF(0.125)*(zb[0] + zb[1] + zt[0] + zt[1])
+                             + TF(0.125)*(yb[0] + yb[VTX] + yt[0] + yt[VTX]);
+                    }
                 }
+                else
+                    acc += TF(0.125)*(xy[0] + xy[1] + xy[VNX] + xy[VNX+1]);
                 const TF s2 = TF(2)*acc + TF(DSMALL);
                 const TF ml2 = lev[3*VPLEV + lq];
                 TF ev;
