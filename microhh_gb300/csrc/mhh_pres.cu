@@ -672,7 +672,7 @@ namespace mhh
     }
 
     template<typename TF, bool INV, int N, int P, int FUSE, bool ROWS>
-    __global__ void __launch_bounds__(256)
+    __global__ void __launch_bounds__(P == 8 ? 512 : 256)
     k_fftp(TF* __restrict__ data, SeqLayout L, TF scale, FftFuse<TF> fz, const TF* __restrict__ twt, long long ntiles)
     {
         using T2 = typename C2<TF>::T;
@@ -790,6 +790,8 @@ namespace mhh
     static void launch_fftp(const FftPlan& pl, TF* data, SeqLayout L, TF scale, const FftFuse<TF>& fz, cudaStream_t s)
     {
         using T2 = typename C2<TF>::T;
+        // 8 pairs (16 columns, 64-byte rows of a tile) run with 512 threads.
+        constexpr int NT = P == 8 ? 512 : 256;
         const size_t smem = sizeof(T2)*((size_t)3*fftp_buf(N, P, ROWS) + N);
         const long long ntiles = (L.nseq + 2*P - 1) / (2*P);
         // Attribute and residency are set once per kernel, outside any stream
@@ -798,14 +800,14 @@ namespace mhh
         {
             cudaFuncSetAttribute(k_fftp<TF, INV, N, P, FUSE, ROWS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             int per_sm = 0, dev = 0, sms = 0;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fftp<TF, INV, N, P, FUSE, ROWS>, 256, smem);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fftp<TF, INV, N, P, FUSE, ROWS>, NT, smem);
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
             return (per_sm > 0 ? per_sm : 1)*(sms > 0 ? sms : 1);
         }();
         const long long nblk = ntiles < resident ? ntiles : resident;
         const TF* twt = sizeof(TF) == 8 ? reinterpret_cast<const TF*>(pl.tw_d) : reinterpret_cast<const TF*>(pl.tw_f);
-        k_fftp<TF, INV, N, P, FUSE, ROWS><<<(unsigned)nblk, 256, smem, s>>>(data, L, scale, fz, twt, ntiles);
+        k_fftp<TF, INV, N, P, FUSE, ROWS><<<(unsigned)nblk, NT, smem, s>>>(data, L, scale, fz, twt, ntiles);
     }
 
     // Dynamic shared-memory limit of the run-time-plan FFT (two buffers of at
@@ -846,6 +848,7 @@ namespace mhh
         // Pipelined transforms (three buffers) where they fit in 96 KB.
         constexpr bool PIPE_R = sizeof(typename C2<TF>::T)*(3*fftp_buf(NF, PR, true) + NF) <= 96*1024;
         constexpr bool PIPE_C = sizeof(typename C2<TF>::T)*(3*fftp_buf(NF, PR, false) + NF) <= 96*1024;
+        constexpr bool PIPE_C8 = sizeof(TF) == 4 && sizeof(typename C2<TF>::T)*(3*fftp_buf(NF, 8, false) + NF) <= 200*1024;
         const bool pipe = fft_pipeline() != 0;
         if (L.rows)
         {
@@ -863,6 +866,7 @@ namespace mhh
             else launch_fixed<TF, INV, NF, PR, 0>(pl, data, L, scale, fz, s);
         }
         else if (PIPE_C && pipe && fft_column_pairs() == 4) launch_fftp<TF, INV, NF, PR, 0, false>(pl, data, L, scale, fz, s);
+        else if (PIPE_C8 && pipe && fft_column_pairs() == 8) launch_fftp<TF, INV, NF, 8, 0, false>(pl, data, L, scale, fz, s);
         else if (fft_column_pairs() == 4 || PC == PR) launch_fixed<TF, INV, NF, PR, 0>(pl, data, L, scale, fz, s);
         else launch_fixed<TF, INV, NF, PC, 0>(pl, data, L, scale, fz, s);
         return true;

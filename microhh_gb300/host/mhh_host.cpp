@@ -261,6 +261,10 @@ namespace mhh_host
         sd["p"] = make("p");
         if (with_evisc) sd["evisc"] = make("evisc");
         (void)in;
+        // The allocations and their zeroing are ordered on the set-up stream
+        // only; every later use (host copies on the default stream, kernels
+        // on the model's stream) must find them done.
+        cuda_check(cudaStreamSynchronize(setup), "field set-up");
     }
 
     template<typename TF>

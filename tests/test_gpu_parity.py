@@ -371,16 +371,19 @@ def test_fft_pipeline_is_bitwise(mhh, precision):
     for case in (cases.drycbl(64, 48, 20, 6400., 4800., 2000., seed=65, noise_z=600.),
                  cases.drycbl(128, 96, 13, 12800., 9600., 1300., seed=66, noise_z=600.)):
         out = []
-        for pipe in (0, 1):
+        for pipe, pairs in ((0, 4), (1, 4), (1, 8)):
             mhh.set_option("fft_pipeline", pipe)
+            mhh.set_option("fft_column_pairs", pairs)
             try:
                 m = mhh.Model(case, precision=precision)
                 m.run_steps(2)
                 out.append({n: m.get(n) for n in case.prognostic_names() + ["p"]})
             finally:
                 mhh.set_option("fft_pipeline", 1)
-        for n in out[0]:
-            assert np.array_equal(out[0][n], out[1][n]), (case.name, n)
+                mhh.set_option("fft_column_pairs", 4)
+        for q in (1, 2):
+            for n in out[0]:
+                assert np.array_equal(out[0][n], out[q][n]), (case.name, n, q)
 
 
 def buffered_cbl(itot, jtot, ktot, seed):
