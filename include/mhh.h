@@ -143,8 +143,8 @@ int mhh_set_option(const char* name, int value);
 /* "fft_pipeline": 1 (the default) runs the fixed-length FFTs as persistent
    blocks that load their next tile while transforming the current one; 0
    runs one tile per block.  Both give identical results.
-   "fft_column_pairs": complex sequence pairs per block of the y FFT, 4 (the
-   default) or 8 (8 uses the one-tile-per-block kernel).  "pres_fuse": 1 (the default) computes the Poisson
+   "fft_column_pairs": complex sequence pairs per tile of the y FFT, 8 (the
+   default: 16 adjacent columns, 512 threads per block, float fields) or 4.  "pres_fuse": 1 (the default) computes the Poisson
    right-hand side inside the forward x FFT and stores the inverse x FFT into
    the ghost layout of p; 0 runs them as separate kernels. */
 /* "tendency_kchunk" / "viscosity_kchunk": levels per block of the marching

@@ -72,7 +72,7 @@ namespace mhh
     int viscosity_variant() { return g_visc_variant; }
     void set_viscosity_variant(int v) { g_visc_variant = v; }
     static int g_tend_kchunk = 0, g_visc_kchunk = 0;
-    static int g_fft_col_pairs = 4;
+    static int g_fft_col_pairs = 8;
     static int g_pres_fuse = 1;
     int pres_fuse() { return g_pres_fuse; }
     int fft_column_pairs() { return g_fft_col_pairs; }

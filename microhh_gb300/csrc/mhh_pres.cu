@@ -865,8 +865,8 @@ namespace mhh
             if (PIPE_R && pipe) launch_fftp<TF, INV, NF, PR, 0, true>(pl, data, L, scale, fz, s);
             else launch_fixed<TF, INV, NF, PR, 0>(pl, data, L, scale, fz, s);
         }
-        else if (PIPE_C && pipe && fft_column_pairs() == 4) launch_fftp<TF, INV, NF, PR, 0, false>(pl, data, L, scale, fz, s);
         else if (PIPE_C8 && pipe && fft_column_pairs() == 8) launch_fftp<TF, INV, NF, 8, 0, false>(pl, data, L, scale, fz, s);
+        else if (PIPE_C && pipe) launch_fftp<TF, INV, NF, PR, 0, false>(pl, data, L, scale, fz, s);
         else if (fft_column_pairs() == 4 || PC == PR) launch_fixed<TF, INV, NF, PR, 0>(pl, data, L, scale, fz, s);
         else launch_fixed<TF, INV, NF, PC, 0>(pl, data, L, scale, fz, s);
         return true;

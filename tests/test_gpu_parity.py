@@ -380,7 +380,7 @@ def test_fft_pipeline_is_bitwise(mhh, precision):
                 out.append({n: m.get(n) for n in case.prognostic_names() + ["p"]})
             finally:
                 mhh.set_option("fft_pipeline", 1)
-                mhh.set_option("fft_column_pairs", 4)
+                mhh.set_option("fft_column_pairs", 8)
         for q in (1, 2):
             for n in out[0]:
                 assert np.array_equal(out[0][n], out[q][n]), (case.name, n, q)
