@@ -1298,9 +1298,13 @@ namespace mhh
     // transaction.  Four times the threads of k_tdma_scaled, so that the FP64
     // recurrences and the loads of the next levels of other warps overlap.
     constexpr int TDC_KF = 8;
+    constexpr int TDC_KB = 4;
 
+    // At most 64 registers, so that eight blocks (32 warps) fit on an SM:
+    // the loads of one warp's next levels overlap the FP64 recurrences of
+    // the others.
     template<typename TF>
-    __global__ void __launch_bounds__(128)
+    __global__ void __launch_bounds__(128, 8)
     k_tdma_col(int itot, int jtot, int ktot, int niu, int nju, const double* __restrict__ gtab,
                const double* __restrict__ htab, const float* __restrict__ stab, const double* __restrict__ stabd,
                TF* __restrict__ pk, double* __restrict__ work)
@@ -1348,13 +1352,13 @@ namespace mhh
             const double sd = sizeof(TF) == 8 ? __ldg(stabd + base + k*stride) : 0.;
             pk[col + k*kk] = scale_out<TF>(z, s, sd);
         }
-        for (int k0=ktot-2; k0>=0; k0-=TDC_KF)
+        for (int k0=ktot-2; k0>=0; k0-=TDC_KB)
         {
-            const int nk = min(TDC_KF, k0 + 1);
-            double h[TDC_KF], sd[TDC_KF], zv[TDC_KF];
-            float s[TDC_KF];
+            const int nk = min(TDC_KB, k0 + 1);
+            double h[TDC_KB], sd[TDC_KB], zv[TDC_KB];
+            float s[TDC_KB];
             #pragma unroll
-            for (int b=0; b<TDC_KF; ++b)
+            for (int b=0; b<TDC_KB; ++b)
                 if (b < nk)
                 {
                     const long long k = k0 - b;
@@ -1364,7 +1368,7 @@ namespace mhh
                     zv[b] = work[col + k*kk];
                 }
             #pragma unroll
-            for (int b=0; b<TDC_KF; ++b)
+            for (int b=0; b<TDC_KB; ++b)
                 if (b < nk)
                 {
                     z = fma(-h[b], z, zv[b]);
