@@ -154,10 +154,11 @@ def allreduce_sum(x, world):
     return float(t.item())
 
 
-def make_case(size, rank):
+def make_case(size, rank, ktot=None):
     from microhh_gb300 import cases
     n = size
-    return cases.drycbl(n, n, n // 2, 50. * n, 50. * n, 4000., seed=2 + rank, name=f"drycbl_{n}x{n}x{n//2}")
+    kt = ktot or n // 2
+    return cases.drycbl(n, n, kt, 50. * n, 50. * n, 4000. * kt / (n // 2), seed=2 + rank, name=f"drycbl_{n}x{n}x{kt}")
 
 
 def timed_steps(model, steps, world):
@@ -175,12 +176,12 @@ def timed_steps(model, steps, world):
     return e0.elapsed_time(e1) / 1e3
 
 
-def cpu_baseline_sample(size, substeps=3):
+def cpu_baseline_sample(size, kt, substeps=3):
     """The oracle port of the reference's hot-path code on all host cores:
     `substeps` RK3 substeps of the same case (seconds, cores)."""
     from oracle import orcpy
     orcpy.build()
-    case = make_case(size, 0)
+    case = make_case(size, 0, kt)
     m = orcpy.model_from_case(case)
     cores = m.lib.orc_num_threads()
     t0 = time.perf_counter()
@@ -198,8 +199,9 @@ def run_reference(args, world, rank):
     from oracle import orcpy
     orcpy.build()
     size = args.size
-    n = size * size * (size // 2)
-    case = make_case(size, 0)
+    kt = args.ktot or size // 2
+    n = size * size * kt
+    case = make_case(size, 0, kt)
     m = orcpy.model_from_case(case)
     cores = m.lib.orc_num_threads()
     m.run_substeps(args.warmup)
@@ -208,13 +210,13 @@ def run_reference(args, world, rank):
     total = time.perf_counter() - t0
     m.close()
     value = n * (args.steps / 3.0) / total
-    sample = (f"{args.steps} RK3 substeps of drycbl {size}x{size}x{size//2} after {args.warmup} warm-up substeps "
+    sample = (f"{args.steps} RK3 substeps of drycbl {size}x{size}x{kt} after {args.warmup} warm-up substeps "
               "(oracle port of the reference's hot-path code, OpenMP on all host cores)")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / (args.steps / 3.0),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded dry CBL)",
-            "config": {"workload": f"dry CBL LES {size}x{size}x{size//2}, Advec_2i5 + Smagorinsky + MOST + Pres_2, RK3, dt=2 s"},
+            "config": {"workload": f"dry CBL LES {size}x{size}x{kt}, Advec_2i5 + Smagorinsky + MOST + Pres_2, RK3, dt=2 s"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -226,8 +228,9 @@ def run_ours(args, world, rank, local):
     import microhh_gb300 as mhh
 
     size = args.size
-    n = size * size * (size // 2)
-    case = make_case(size, rank)
+    kt = args.ktot or size // 2
+    n = size * size * kt
+    case = make_case(size, rank, kt)
 
     # ---- FP32 form: device-resident throughput -------------------------
     m = mhh.Model(case, precision=mhh.FP32)
@@ -311,16 +314,16 @@ def run_ours(args, world, rank, local):
     # ---- CPU baseline (rank 0, N = 1) ----------------------------------
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        dt, cores = cpu_baseline_sample(size, 3)
+        dt, cores = cpu_baseline_sample(size, kt, 3)
         cpu = {"value": n / dt, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"1 RK3 step of drycbl {size}x{size}x{size//2} (oracle port of the reference's hot-path code, OpenMP)"}
+               "sample": f"1 RK3 step of drycbl {size}x{size}x{kt} (oracle port of the reference's hot-path code, OpenMP)"}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 z-solve and reductions)",
                 "data": "synthetic (seeded dry CBL, theta noise +-0.1 K below 200 m)",
-                "config": {"workload": f"dry CBL LES {size}x{size}x{size//2}, domain {50*size}x{50*size}x4000 m, "
+                "config": {"workload": f"dry CBL LES {size}x{size}x{kt}, domain {50*size}x{50*size}x{case.zsize:g} m, "
                                        "Advec_2i5 + Smagorinsky (cs 0.23) + MOST surface + Boussinesq + Pres_2, RK3, dt=2 s",
                            "precision": "fp32 form", "parallelism": f"replicas x{world}",
                            "l2": "inputs larger than L2 (one field 277 MB)"},
@@ -360,6 +363,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=512)
+    ap.add_argument("--ktot", type=int, default=0, help="vertical levels (default size/2)")
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--form", default="step", choices=["step", "ensemble", "serve"],
