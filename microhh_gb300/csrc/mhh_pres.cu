@@ -349,8 +349,11 @@ namespace mhh
     // pack pairs as complex, FFT, separate into halfcomplex (forward) or take
     // real and imaginary parts (inverse), store.  NFIX > 0 selects the
     // fixed-length path (NFIX = n, PFIX = P); NFIX = 0 the run-time plan.
+    // The float transform with the fused right-hand side keeps five blocks
+    // per SM (at most 51 registers): its batched loads need the residency to
+    // cover the latency of HBM.
     template<typename TF, bool INV, int NFIX, int PFIX, int FUSE>
-    __global__ void __launch_bounds__(256)
+    __global__ void __launch_bounds__(256, (FUSE == 1 && sizeof(TF) == 4) ? 5 : 1)
     k_fft(FftPlan pl, TF* __restrict__ data, SeqLayout L, int Prt, TF scale, FftFuse<TF> fz)
     {
         using T2 = typename C2<TF>::T;
