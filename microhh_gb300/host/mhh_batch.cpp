@@ -400,8 +400,9 @@ namespace mhh_host
                 Input in(j.ini);
                 const std::string swadvec = in.get_item<std::string>("advec", "swadvec", "", "2");
                 const int gc = swadvec == "2i5" ? 3 : 1;
+                const int kgc = swadvec == "2i5" && !in.get_list("advec", "fluxlimit_list", "", {}).empty() ? 2 : 1;
                 const size_t n = size_t(in.get_item<int>("grid", "itot", "") + 2*gc)
-                               * size_t(in.get_item<int>("grid", "jtot", "") + 2*gc) * (j.z.size() + 2);
+                               * size_t(in.get_item<int>("grid", "jtot", "") + 2*gc) * (j.z.size() + 2*kgc);
                 j.init[name] = std::vector<double>(data, data + n);
             }
 
