@@ -134,24 +134,27 @@ def barrier(world):
         dist.barrier()
 
 
-def allreduce_max(x, world):
+def _allreduce(x, world, op):
+    """One float reduced over the ranks (NCCL on the GPUs; gloo on the host
+    when the process group is a gloo one, as in the multi-process tests)."""
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=op)
     return float(t.item())
+
+
+def allreduce_max(x, world):
+    import torch.distributed as dist
+    return _allreduce(x, world, dist.ReduceOp.MAX)
 
 
 def allreduce_sum(x, world):
-    if world == 1:
-        return x
-    import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return float(t.item())
+    return _allreduce(x, world, dist.ReduceOp.SUM)
 
 
 def make_case(size, rank, ktot=None):
