@@ -131,10 +131,10 @@ int mhh_ctx_estimate_bytes(const mhh_grid_desc* desc, int precision, size_t* byt
    reference picks kernel variants through its Kernel Launcher wisdom files):
    "tendency_kernel" 0 = one thread per cell, 1 = tiled planes marching in k,
    2 = flux form (each face flux computed once) marching in k, -1 = automatic
-   (2 for FP32 contexts, 0 for FP64 contexts; the default);
+   (2; the default);
    "viscosity_kernel" 0 = one thread per cell, 1 = shared-memory planes
-   marching in k, -1 = automatic (1 for FP32 contexts, 0 for FP64; the
-   default; the neutral resolved-wall case always runs per cell);
+   marching in k, -1 = automatic (1; the default; the neutral resolved-wall
+   case always runs per cell);
    "tdma_kernel" 0 = the Thomas recurrence in the reference's operation order,
    1 = the rescaled recurrence (two FP64 FMAs per cell) with one column per
    thread, 2 = the same with the four columns of one eigenvalue per thread,

@@ -257,7 +257,9 @@ namespace mhh
     {
         dim3 block(32, 8);
         dim3 grid((d.itot + 31)/32, (d.jtot + 7)/8, d.ktot);
-        const int var = o.visc < 0 ? (sizeof(TF) == 4 ? 1 : 0) : o.visc;
+        // Automatic choice (-1): the plane-staged kernel in both precisions
+        // (in double it keeps the reference's evisc expression).
+        const int var = o.visc < 0 ? 1 : o.visc;
         const bool planes = var == 1 && launch_viscosity_planes<TF>(d, pr, u, v, w, th, evisc, mlen2, dudz, dvdz, dbdz,
                                                                     tpr, surf, thermo, o.visc_kchunk, s);
         if (!planes)
@@ -392,11 +394,13 @@ namespace mhh
     {
         // The LES combination can run in the tiled kernel (mhh_tend_tiled.cu)
         // or in the flux-form kernel (mhh_tend_flux.cu).
-        // Automatic choice (-1): the flux form for float fields, the per-cell
-        // kernel (the reference's operation order) for double fields.
+        // Automatic choice (-1): the flux form in both precisions (in double
+        // it agrees with the per-cell kernel, which keeps the reference's
+        // operation order, to round-off: both are held to 1e-12 against the
+        // reference).
         // The limited scalar (adv == ADVEC_2I5_LIM) runs in the flux-form or
         // the per-cell kernel; the tiled kernel hands it to the flux form.
-        const int var = o.tend < 0 ? (sizeof(TF) == 4 ? 2 : 0) : o.tend;
+        const int var = o.tend < 0 ? 2 : o.tend;
         const bool lim = adv == ADVEC_2I5_LIM && scal;
         if (adv == ADVEC_2I5_LIM && !scal) adv = MHH_ADVEC_2I5;
         if (var >= 1 && (adv == MHH_ADVEC_2I5 || lim) && dif == MHH_DIFF_SMAG2 && !force && d.igc >= 3 && d.jgc >= 3)

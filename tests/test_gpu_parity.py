@@ -123,11 +123,12 @@ def test_against_oracle_fp64(mhh, oracle_lib, name, make):
             assert max_err(a, b) <= 10 * tol, (name, n, nsteps, max_err(a, b))
 
 
-@pytest.mark.parametrize("variant", [1, 2], ids=["tiled", "flux"])
+@pytest.mark.parametrize("variant", [0, 1, 2], ids=["percell", "tiled", "flux"])
 @pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
 def test_tendency_variants_fp64(mhh, path, variant):
-    """The blocked LES tendency kernels (tiled planes; flux form) run on
-    double fields against the golden fixtures at the FP64 tolerance."""
+    """Every LES tendency kernel (per cell in the reference's operation order;
+    tiled planes; flux form, the default) on double fields against the golden
+    fixtures at the FP64 tolerance."""
     name = os.path.basename(path)[:-4]
     g = np.load(path)
     case = golden_case(name)
@@ -144,14 +145,16 @@ def test_tendency_variants_fp64(mhh, path, variant):
         mhh.set_option("tendency_kernel", -1)
 
 
+@pytest.mark.parametrize("variant", [0, 1], ids=["percell", "planes"])
 @pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
-def test_viscosity_planes_fp64(mhh, path):
-    """The plane-staged eddy-viscosity kernel on double fields against the
-    golden fixtures (evisc at its own tolerance, the rest at FP64)."""
+def test_viscosity_planes_fp64(mhh, path, variant):
+    """Both eddy-viscosity kernels (per cell; plane-staged, the default) on
+    double fields against the golden fixtures (evisc at its own tolerance,
+    the rest at FP64)."""
     name = os.path.basename(path)[:-4]
     g = np.load(path)
     case = golden_case(name)
-    mhh.set_option("viscosity_kernel", 1)
+    mhh.set_option("viscosity_kernel", variant)
     try:
         m = mhh.Model(case, precision=mhh.FP64)
         for n in case.prognostic_names():
