@@ -514,8 +514,6 @@ namespace mhh
     // cell of the full ghost layout so that the tendencies' ghost cells are
     // zeroed after the last substep as on the CPU.
     // ---------------------------------------------------------------------
-    constexpr int PRK = 1;
-
     template<typename TF, bool SCAL>
     __global__ void __launch_bounds__(256)
     k_presout_rk3(Dims d, Prof<TF> pr, const TF* __restrict__ p,
@@ -523,41 +521,102 @@ namespace mhh
                   TF* __restrict__ ut, TF* __restrict__ vt, TF* __restrict__ wt, TF* __restrict__ st,
                   TF cbdt, TF ca, int last)
     {
-        // PRK consecutive levels per thread: twice the loads in flight per
-        // thread, and the pressure of level k is reused for level k+1.
         const int i = blockIdx.x*blockDim.x + threadIdx.x;
         const int j = blockIdx.y*blockDim.y + threadIdx.y;
+        const int k = blockIdx.z;
         if (i >= d.icells || j >= d.jcells) return;
-        const bool col_in = i >= d.istart && i < d.iend && j >= d.jstart && j < d.jend;
-        const int kb = blockIdx.z*PRK;
-        #pragma unroll
-        for (int q=0; q<PRK; ++q)
+        const long long c = ijk(d, i, j, k);
+        const bool interior = i >= d.istart && i < d.iend && j >= d.jstart && j < d.jend && k >= d.kstart && k < d.kend;
+        if (interior)
         {
-            const int k = kb + q;
-            if (k >= d.kcells) break;
-            const long long c = ijk(d, i, j, k);
-            if (col_in && k >= d.kstart && k < d.kend)
+            const TF pc = ld(p, c);
+            TF tu = ut[c] - (pc - ld(p, c-1))*dxi_of<TF>(d);
+            TF tv = vt[c] - (pc - ld(p, c-d.icells))*dyi_of<TF>(d);
+            TF tw = wt[c] - (pc - ld(p, c-d.ijcells))*ld(pr.dzhi, k);
+            u[c] += cbdt*tu; v[c] += cbdt*tv; w[c] += cbdt*tw;
+            ut[c] = last ? TF(0) : tu*ca;
+            vt[c] = last ? TF(0) : tv*ca;
+            wt[c] = last ? TF(0) : tw*ca;
+            if (SCAL)
             {
-                const TF pc = ld(p, c);
-                TF tu = ut[c] - (pc - ld(p, c-1))*dxi_of<TF>(d);
-                TF tv = vt[c] - (pc - ld(p, c-d.icells))*dyi_of<TF>(d);
-                TF tw = wt[c] - (pc - ld(p, c-d.ijcells))*ld(pr.dzhi, k);
-                u[c] += cbdt*tu; v[c] += cbdt*tv; w[c] += cbdt*tw;
-                ut[c] = last ? TF(0) : tu*ca;
-                vt[c] = last ? TF(0) : tv*ca;
-                wt[c] = last ? TF(0) : tw*ca;
-                if (SCAL)
-                {
-                    const TF ts = st[c];
-                    s[c] += cbdt*ts;
-                    st[c] = last ? TF(0) : ts*ca;
-                }
+                const TF ts = st[c];
+                s[c] += cbdt*ts;
+                st[c] = last ? TF(0) : ts*ca;
             }
-            else if (last)
+        }
+        else if (last)
+        {
+            ut[c] = TF(0); vt[c] = TF(0); wt[c] = TF(0);
+            if (SCAL) st[c] = TF(0);
+        }
+    }
+
+    // Float fields with an even row length: two adjacent cells (i even) per
+    // thread with 8-byte loads and stores, half the memory instructions of
+    // the per-cell kernel.  A ghost cell of the pair keeps its values (or is
+    // zeroed after the last substep); the arithmetic per cell is that of
+    // k_presout_rk3.
+    template<bool SCAL>
+    __global__ void __launch_bounds__(256)
+    k_presout_rk3_x2(Dims d, Prof<float> pr, const float* __restrict__ p,
+                     float* __restrict__ u, float* __restrict__ v, float* __restrict__ w, float* __restrict__ s,
+                     float* __restrict__ ut, float* __restrict__ vt, float* __restrict__ wt, float* __restrict__ st,
+                     float cbdt, float ca, int last)
+    {
+        const int i = 2*(blockIdx.x*blockDim.x + threadIdx.x);
+        const int j = blockIdx.y*blockDim.y + threadIdx.y;
+        const int k = blockIdx.z;
+        if (i >= d.icells || j >= d.jcells) return;
+        const long long c = ijk(d, i, j, k);
+        const bool row_in = j >= d.jstart && j < d.jend && k >= d.kstart && k < d.kend;
+        const bool in0 = row_in && i >= d.istart && i < d.iend;
+        const bool in1 = row_in && i+1 >= d.istart && i+1 < d.iend;
+        if (!in0 && !in1)
+        {
+            if (last)
             {
-                ut[c] = TF(0); vt[c] = TF(0); wt[c] = TF(0);
-                if (SCAL) st[c] = TF(0);
+                const float2 z = make_float2(0.f, 0.f);
+                *reinterpret_cast<float2*>(ut + c) = z; *reinterpret_cast<float2*>(vt + c) = z;
+                *reinterpret_cast<float2*>(wt + c) = z;
+                if (SCAL) *reinterpret_cast<float2*>(st + c) = z;
             }
+            return;
+        }
+        auto ld2 = [](const float* a, long long n) { return __ldg(reinterpret_cast<const float2*>(a + n)); };
+        const float2 pc = ld2(p, c);
+        const float pw = i > 0 ? __ldg(p + c - 1) : 0.f;
+        const float2 ps = ld2(p, c - d.icells), pb = ld2(p, c - d.ijcells);
+        const float dxi = dxi_of<float>(d), dyi = dyi_of<float>(d), dzhi = __ldg(pr.dzhi + k);
+        float2 tu = *reinterpret_cast<const float2*>(ut + c), tv = *reinterpret_cast<const float2*>(vt + c);
+        float2 tw = *reinterpret_cast<const float2*>(wt + c);
+        float2 uu = *reinterpret_cast<const float2*>(u + c), vv = *reinterpret_cast<const float2*>(v + c);
+        float2 ww = *reinterpret_cast<const float2*>(w + c);
+        // Cell 0 (i) and cell 1 (i+1).
+        const float tu0 = tu.x - (pc.x - pw)*dxi, tu1 = tu.y - (pc.y - pc.x)*dxi;
+        const float tv0 = tv.x - (pc.x - ps.x)*dyi, tv1 = tv.y - (pc.y - ps.y)*dyi;
+        const float tw0 = tw.x - (pc.x - pb.x)*dzhi, tw1 = tw.y - (pc.y - pb.y)*dzhi;
+        if (in0) { uu.x += cbdt*tu0; vv.x += cbdt*tv0; ww.x += cbdt*tw0; }
+        if (in1) { uu.y += cbdt*tu1; vv.y += cbdt*tv1; ww.y += cbdt*tw1; }
+        *reinterpret_cast<float2*>(u + c) = uu; *reinterpret_cast<float2*>(v + c) = vv;
+        *reinterpret_cast<float2*>(w + c) = ww;
+        tu.x = in0 ? (last ? 0.f : tu0*ca) : (last ? 0.f : tu.x);
+        tu.y = in1 ? (last ? 0.f : tu1*ca) : (last ? 0.f : tu.y);
+        tv.x = in0 ? (last ? 0.f : tv0*ca) : (last ? 0.f : tv.x);
+        tv.y = in1 ? (last ? 0.f : tv1*ca) : (last ? 0.f : tv.y);
+        tw.x = in0 ? (last ? 0.f : tw0*ca) : (last ? 0.f : tw.x);
+        tw.y = in1 ? (last ? 0.f : tw1*ca) : (last ? 0.f : tw.y);
+        *reinterpret_cast<float2*>(ut + c) = tu; *reinterpret_cast<float2*>(vt + c) = tv;
+        *reinterpret_cast<float2*>(wt + c) = tw;
+        if (SCAL)
+        {
+            float2 ts = *reinterpret_cast<const float2*>(st + c);
+            float2 ss = *reinterpret_cast<const float2*>(s + c);
+            if (in0) ss.x += cbdt*ts.x;
+            if (in1) ss.y += cbdt*ts.y;
+            *reinterpret_cast<float2*>(s + c) = ss;
+            ts.x = last ? 0.f : (in0 ? ts.x*ca : ts.x);
+            ts.y = last ? 0.f : (in1 ? ts.y*ca : ts.y);
+            *reinterpret_cast<float2*>(st + c) = ts;
         }
     }
 
@@ -569,7 +628,20 @@ namespace mhh
         const double cB[3] = {1./3., 15./16., 8./15.};
         const int sn = (substep + 1) % 3;
         dim3 block(32, 8);
-        dim3 grid((d.icells + 31)/32, (d.jcells + 7)/8, (d.kcells + PRK - 1)/PRK);
+        if constexpr (sizeof(TF) == 4)
+        {
+            if (d.icells % 2 == 0 && d.ijcells % 2 == 0)
+            {
+                dim3 grid((d.icells/2 + 31)/32, (d.jcells + 7)/8, d.kcells);
+                if (s)
+                    k_presout_rk3_x2<true><<<grid, block, 0, strm>>>(d, pr, p, u, v, w, s, ut, vt, wt, st, TF(cB[substep]*dt), TF(cA[sn]), sn == 0);
+                else
+                    k_presout_rk3_x2<false><<<grid, block, 0, strm>>>(d, pr, p, u, v, w, s, ut, vt, wt, st, TF(cB[substep]*dt), TF(cA[sn]), sn == 0);
+                count_launch();
+                return;
+            }
+        }
+        dim3 grid((d.icells + 31)/32, (d.jcells + 7)/8, d.kcells);
         if (s)
             k_presout_rk3<TF, true><<<grid, block, 0, strm>>>(d, pr, p, u, v, w, s, ut, vt, wt, st, TF(cB[substep]*dt), TF(cA[sn]), sn == 0);
         else
