@@ -148,8 +148,9 @@ int mhh_set_option(const char* name, int value);
    right-hand side inside the forward x FFT and stores the inverse x FFT into
    the ghost layout of p; 0 runs them as separate kernels. */
 /* "tendency_kchunk" / "viscosity_kchunk": levels per block of the marching
-   kernels, 4, 8, 16, 32 or 64, or 0 (the default: 32, halved down to 8 while
-   the grid would give fewer than two blocks per SM). */
+   kernels, 4, 8, 16, 32 or 64, or 0 (the default: 64 where the grid gives at
+   least eight blocks per SM, else 32, halved down to 8 while the grid would
+   give fewer than two blocks per SM). */
 /* The same options for one context, overriding the process-wide value;
    -2 returns to it (no counterpart in the reference; used by the ensemble
    autotuner to pick variants and level chunks per grid size). */

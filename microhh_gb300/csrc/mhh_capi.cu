@@ -94,6 +94,9 @@ namespace mhh
             cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
             return n > 0 ? n : 152;
         }();
+        // 64 levels (fewer halo levels per chunk) while the grid still gives
+        // eight blocks per SM; else 32, halved while it gives fewer than two.
+        if (tiles*((ktot + 63)/64) >= 8LL*nsm) return 64;
         int kc = 32;
         while (kc > 8 && tiles*((ktot + kc - 1)/kc) < 2LL*nsm) kc /= 2;
         return kc;

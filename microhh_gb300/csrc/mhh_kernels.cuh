@@ -21,8 +21,9 @@ namespace mhh
     };
 
     // Level-chunk height of a marching kernel with `tiles` blocks per chunk
-    // row: the requested height, or for 0 the largest of 32, 16, 8 that still
-    // gives two blocks per SM (small grids get more, shorter chunks).
+    // row: the requested height, or for 0 64 where that gives eight blocks
+    // per SM, else the largest of 32, 16, 8 that still gives two (small grids
+    // get more, shorter chunks).
     int auto_kchunk(int requested, long long tiles, int ktot);
 
     // Read-only view of a context for kernels in other translation units.
