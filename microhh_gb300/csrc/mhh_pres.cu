@@ -38,6 +38,46 @@ namespace mhh
         typename C2<TF>::T r; r.x = __ldg(t + 2*e); r.y = __ldg(t + 2*e + 1); return r;
     }
 
+    // Radix-R butterfly (R = 5 or 7, a compile-time constant) of one item of
+    // a run-time-plan stage: the inputs x[i + q*T] times the stage twiddles
+    // w^(q*k*step) (an index below n), then a direct DFT whose twiddles
+    // w^(q*r*T) are w^(((q*r) mod R)*T).
+    template<typename TF, int R>
+    __device__ __forceinline__ void radix_gen(const typename C2<TF>::T* __restrict__ x, typename C2<TF>::T* __restrict__ y,
+                                              const TF* __restrict__ tt, int i, int T, int k, int step, int j, int p)
+    {
+        using T2 = typename C2<TF>::T;
+        T2 u[R];
+        u[0] = x[i];
+        #pragma unroll
+        for (int q=1; q<R; ++q) u[q] = cmul(x[i + q*T], tw<TF>(tt, q*k*step));
+        T2 wr[R];
+        #pragma unroll
+        for (int m=0; m<R; ++m) wr[m] = tw<TF>(tt, m*T);
+        #pragma unroll
+        for (int r=0; r<R; ++r)
+        {
+            T2 acc = u[0];
+            #pragma unroll
+            for (int q=1; q<R; ++q) acc = cadd(acc, cmul(u[q], wr[(q*r) % R]));
+            y[j + r*p] = acc;
+        }
+    }
+
+    // Quotient and remainder of a / b for 0 <= a < 2^20 and b >= 1 from a
+    // float reciprocal rb ~ 1/b: the float quotient is within one of the
+    // exact one, and one correction step in either direction makes it exact
+    // (a run-time integer division costs several times more).
+    __device__ __forceinline__ int div_rcp(int a, int b, float rb, int& rem)
+    {
+        int q = __float2int_rz(__int2float_rn(a)*rb);
+        int r = a - q*b;
+        if (r < 0) { --q; r += b; }
+        else if (r >= b) { ++q; r -= b; }
+        rem = r;
+        return q;
+    }
+
     // All Stockham stages for P sequences of length n held in buf[0] (complex,
     // [P][n]); returns the buffer index that holds the natural-order result.
     template<typename TF>
@@ -56,11 +96,12 @@ namespace mhh
             const int T = n / R;
             const int step = n / (p*R);
             const int nitem = P*T;
+            const float rT = 1.f/(float)T, rp = 1.f/(float)p;
             for (int it = threadIdx.x; it < nitem; it += blockDim.x)
             {
-                const int seq = it / T;
-                const int i = it - seq*T;
-                const int k = i % p;
+                int i, k;
+                const int seq = div_rcp(it, T, rT, i);
+                div_rcp(i, p, rp, k);
                 const T2* x = src + seq*n;
                 T2* y = dst + seq*n;
                 const int j = (i - k)*R + k;
@@ -72,10 +113,11 @@ namespace mhh
                 }
                 else if (R == 4)
                 {
+                    // q*k*step < R*p*step = n: no reduction modulo n.
                     T2 u0 = x[i];
-                    T2 u1 = cmul(x[i +   T], tw<TF>(tt, (1*k*step) % n));
-                    T2 u2 = cmul(x[i + 2*T], tw<TF>(tt, (2*k*step) % n));
-                    T2 u3 = cmul(x[i + 3*T], tw<TF>(tt, (3*k*step) % n));
+                    T2 u1 = cmul(x[i +   T], tw<TF>(tt, 1*k*step));
+                    T2 u2 = cmul(x[i + 2*T], tw<TF>(tt, 2*k*step));
+                    T2 u3 = cmul(x[i + 3*T], tw<TF>(tt, 3*k*step));
                     const T2 a = cadd(u0, u2), b = csub(u0, u2);
                     const T2 c = cadd(u1, u3), e = csub(u1, u3);
                     // v_r = sum_q u_q (-i)^(q r)
@@ -90,8 +132,8 @@ namespace mhh
                 else if (R == 3)
                 {
                     T2 u0 = x[i];
-                    T2 u1 = cmul(x[i +   T], tw<TF>(tt, (1*k*step) % n));
-                    T2 u2 = cmul(x[i + 2*T], tw<TF>(tt, (2*k*step) % n));
+                    T2 u1 = cmul(x[i +   T], tw<TF>(tt, 1*k*step));
+                    T2 u2 = cmul(x[i + 2*T], tw<TF>(tt, 2*k*step));
                     const TF s3 = TF(0.86602540378443864676);
                     const T2 t1 = cadd(u1, u2), t4 = csub(u1, u2);
                     T2 t2; t2.x = u0.x - TF(0.5)*t1.x; t2.y = u0.y - TF(0.5)*t1.y;
@@ -103,20 +145,8 @@ namespace mhh
                     y[j + p] = v1;
                     y[j + 2*p] = v2;
                 }
-                else
-                {
-                    // General small radix (5, 7): direct DFT with table twiddles.
-                    T2 u[7];
-                    for (int q=0; q<R; ++q)
-                        u[q] = q ? cmul(x[i + q*T], tw<TF>(tt, (int)(((long long)q*k*step) % n))) : x[i];
-                    for (int r=0; r<R; ++r)
-                    {
-                        T2 acc = u[0];
-                        for (int q=1; q<R; ++q)
-                            acc = cadd(acc, cmul(u[q], tw<TF>(tt, (int)(((long long)q*r*T) % n))));
-                        y[j + r*p] = acc;
-                    }
-                }
+                else if (R == 5) radix_gen<TF, 5>(x, y, tt, i, T, k, step, j, p);
+                else radix_gen<TF, 7>(x, y, tt, i, T, k, step, j, p);
             }
             __syncthreads();
             T2* t = src; src = dst; dst = t;

@@ -237,12 +237,14 @@ def test_fp32_form_against_fp64_oracle(mhh, oracle_lib, variant):
     assert np.abs(case.interior(m.get("th") - o.get("th"))).max() <= 1e-4
 
 
-def test_fft_roundtrip_and_dft(mhh):
+@pytest.mark.parametrize("itot,jtot", [(48, 40), (42, 56), (50, 36), (70, 30)])
+def test_fft_roundtrip_and_dft(mhh, itot, jtot):
     """Forward transforms against numpy's DFT in halfcomplex order, and the
-    inverse pair returns itot*jtot times the input."""
+    inverse pair returns itot*jtot times the input (fixed and run-time-plan
+    lengths with the radices 2, 3, 4, 5, 7, 8)."""
     import ctypes
     import torch
-    itot, jtot, ktot = 48, 40, 3
+    ktot = 3
     desc = mhh.GridDesc(itot, jtot, ktot, 1, 1, 1, 1.0, 1.0, 1.0)
     phys = mhh.Physics(visc=1e-5, svisc=1e-5, cs=0.23, tpr=1/3., dnmax=0.4, swmason=1, cflmax=1.,
                        thref0=300., thermo=0, surface=0, z0m=0.1, z0h=0.1)
