@@ -5,7 +5,8 @@
  * Every entry point returns 0 on success or a negative mhh_status; the text
  * of the last error is available from mhh_last_error().  Nothing allocates
  * device memory except mhh_ctx_create (all scratch of the pressure solver,
- * the reductions and the surface layer lives in the context).
+ * the reductions and the surface layer lives in the context) and the
+ * set-up call mhh_buffer_setup (the buffer layer's profiles).
  *
  * Fields use the reference's ghost-cell layout (include/grid.h:48-138):
  * element (i,j,k) of a 3-D field is at i + j*icells + k*ijcells, with the
