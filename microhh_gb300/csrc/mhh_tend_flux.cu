@@ -459,12 +459,27 @@ namespace mhh
                     gzu_t = rhoh1*(du - zadv(qu, i2(PL(W1,-1,0), PL(W1,0,0)), ot));
                     gzv_t = rhoh1*(dv - zadv(qv, i2(PL(W1,0,-1), PL(W1,0,0)), ot));
                 }
+                // Float form, interior levels: the vertical advective fluxes of
+                // w (through full level kf) and of s (through half level kf),
+                // both 6th/5th order, in one packed pair.
+                bool paired = false;
+                float2 aws = make_float2(0.f, 0.f);
+                if constexpr (sizeof(TF) == 4 && SCAL && !LIM)
+                {
+                    if (ot == 6 && kf < d.kend && face_order_w(d, kf) == 6)
+                    {
+                        aws = adv6x2(f2(i2(qw[2], qw[3]), qw[2]), f2(qw[0], qs[0]), f2(qw[1], qs[1]), f2(qw[2], qs[2]),
+                                     f2(qw[3], qs[3]), f2(qw[4], qs[4]), f2(qw[5], qs[5]));
+                        paired = true;
+                    }
+                }
                 if (SCAL)
                 {
                     const TF ds = (SURF && kf == d.kstart) ? -sfb : ((SURF && kf == d.kend) ? -sft
                                 : (TF(0.5)*(PL(E0,0,0) + PL(E1,0,0))*tpri + svisc)*(qs[3] - qs[2])*dzhi1);
                     TF as;
-                    if (LIM)
+                    if (paired) as = aws.y;
+                    else if (LIM)
                     {
                         const int side = kf == d.kstart+1 ? -1 : (kf == d.kend-1 ? 1 : 0);
                         as = ot ? lim_flux(qw[2], qs[1], qs[2], qs[3], qs[4], side) : TF(0);
@@ -478,7 +493,8 @@ namespace mhh
                     const int ow = face_order_w(d, kf);
                     const TF dw = TF(2)*(PL(E1,0,0) + visc)*(qw[3] - qw[2])*prof[3*PLEV + lq];
                     TF aw;
-                    if (ow == 6) aw = adv6(i2(qw[2], qw[3]), qw[0], qw[1], qw[2], qw[3], qw[4], qw[5]);
+                    if (paired) aw = aws.x;
+                    else if (ow == 6) aw = adv6(i2(qw[2], qw[3]), qw[0], qw[1], qw[2], qw[3], qw[4], qw[5]);
                     else if (ow == 4) aw = i2(qw[2], qw[3])*i4ws(qw[1], qw[2], qw[3], qw[4])
                                          - fabs(i2(qw[2], qw[3]))*i3ws(qw[1], qw[2], qw[3], qw[4]);
                     else aw = i2(qw[2], qw[3])*i2(qw[2], qw[3]);
@@ -527,13 +543,27 @@ namespace mhh
                     a.vt[c] = tv + (gx[1*NGX + gx0 + 1] - gx[1*NGX + gx0])*dxi
                                  + (gy[1*NGY + gy0 + FTX] - gy[1*NGY + gy0])*dyi + (gzv_t - gzv_b)*zf;
                 }
-                if (wlev)
-                    a.wt[c + d.ijcells] = tw + (gx[2*NGX + gx0 + 1] - gx[2*NGX + gx0])*dxi
-                                             + (gy[2*NGY + gy0 + FTX] - gy[2*NGY + gy0])*dyi
-                                             + (gzw_t - gzw_b)*prof[6*PLEV + lq] + buoy;
-                if (SCAL)
-                    a.st[c] = ts + (gx[3*NGX + gx0 + 1] - gx[3*NGX + gx0])*dxi
-                                 + (gy[3*NGY + gy0 + FTX] - gy[3*NGY + gy0])*dyi + (gzs_t - gzs_b)*zf;
+                if constexpr (sizeof(TF) == 4 && SCAL)
+                {
+                    // w and s in one packed pair.
+                    const float2 dgx = sub2(f2(gx[2*NGX + gx0 + 1], gx[3*NGX + gx0 + 1]), f2(gx[2*NGX + gx0], gx[3*NGX + gx0]));
+                    const float2 dgy = sub2(f2(gy[2*NGY + gy0 + FTX], gy[3*NGY + gy0 + FTX]), f2(gy[2*NGY + gy0], gy[3*NGY + gy0]));
+                    const float2 dgz = sub2(f2(gzw_t, gzs_t), f2(gzw_b, gzs_b));
+                    const float2 t = __ffma2_rn(dgz, f2(prof[6*PLEV + lq], zf), __ffma2_rn(dgy, f2(dyi, dyi),
+                                                __ffma2_rn(dgx, f2(dxi, dxi), f2(tw + buoy, ts))));
+                    if (wlev) a.wt[c + d.ijcells] = t.x;
+                    a.st[c] = t.y;
+                }
+                else
+                {
+                    if (wlev)
+                        a.wt[c + d.ijcells] = tw + (gx[2*NGX + gx0 + 1] - gx[2*NGX + gx0])*dxi
+                                                 + (gy[2*NGY + gy0 + FTX] - gy[2*NGY + gy0])*dyi
+                                                 + (gzw_t - gzw_b)*prof[6*PLEV + lq] + buoy;
+                    if (SCAL)
+                        a.st[c] = ts + (gx[3*NGX + gx0 + 1] - gx[3*NGX + gx0])*dxi
+                                     + (gy[3*NGY + gy0 + FTX] - gy[3*NGY + gy0])*dyi + (gzs_t - gzs_b)*zf;
+                }
             }
 
             gzu_b = gzu_t; gzv_b = gzv_t; gzw_b = gzw_t; gzs_b = gzs_t;
