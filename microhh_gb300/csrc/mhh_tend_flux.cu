@@ -143,7 +143,7 @@ namespace mhh
     {
         extern __shared__ __align__(16) unsigned char smem_raw[];
         TF* sm = reinterpret_cast<TF*>(smem_raw);
-        TF* gbase = sm + NSLOT*FPS;     // [2 buffers][4 fields][NGX] then [2][4][NGY]
+        TF* gbase = sm + NSLOT*FPS;     // [2 buffers][NGX][4 fields] then [2][NGY][4]
         TF* prof = gbase + 2*4*(NGX + NGY);   // [NPROF][PLEV]
 
         // Warps 0-8 own the face rows fy = 0..8 (fx = lane); warp 9 owns the
@@ -357,20 +357,14 @@ namespace mhh
                         Ds = __fmul2_rn(__ffma2_rn(__fmul2_rn(__fadd2_rn(eo, f2(PL(E0,0,0), PL(E0,0,0))), f2(0.5f, 0.5f)),
                                                    f2(tpri, tpri), f2(svisc, svisc)),
                                         __fmul2_rn(sub2(f2(PL(S0,0,0), PL(S0,0,0)), f2(PL(S0,-1,0), PL(S0,0,-1))), h2));
+                    // The four fields' fluxes of a face are adjacent: one
+                    // 16-byte store per face.
                     if (face_x)
-                    {
-                        gx[0*NGX + gxi] = Duv.x - Au.x;
-                        gx[1*NGX + gxi] = txy - Av.x;
-                        gx[2*NGX + gxi] = txz - Aw.x;
-                        if (SCAL) gx[3*NGX + gxi] = Ds.x - As.x;
-                    }
+                        reinterpret_cast<float4*>(gx)[gxi] = make_float4(Duv.x - Au.x, txy - Av.x, txz - Aw.x,
+                                                                         SCAL ? Ds.x - As.x : 0.f);
                     if (face_y)
-                    {
-                        gy[0*NGY + gyi] = txy - Au.y;
-                        gy[1*NGY + gyi] = Duv.y - Av.y;
-                        gy[2*NGY + gyi] = tyz - Aw.y;
-                        if (SCAL) gy[3*NGY + gyi] = Ds.y - As.y;
-                    }
+                        reinterpret_cast<float4*>(gy)[gyi] = make_float4(txy - Au.y, Duv.y - Av.y, tyz - Aw.y,
+                                                                         SCAL ? Ds.y - As.y : 0.f);
                 }
                 else
                 {
@@ -381,19 +375,19 @@ namespace mhh
                             const TF uw = i2(PL(U0,-1,0), PL(U0,0,0));
                             const TF A = adv6(uw, PL(U0,-3,0), PL(U0,-2,0), PL(U0,-1,0), PL(U0,0,0), PL(U0,1,0), PL(U0,2,0));
                             const TF D = TF(2)*(PL(E0,-1,0) + visc)*(PL(U0,0,0) - PL(U0,-1,0))*dxi;
-                            gx[0*NGX + gxi] = D - A;
+                            gx[(gxi)*4 + 0] = D - A;
                         }
                         // v at (i-1/2, j-1/2).
                         {
                             const TF uw = i2(PL(U0,0,-1), PL(U0,0,0));
                             const TF A = adv6(uw, PL(V0,-3,0), PL(V0,-2,0), PL(V0,-1,0), PL(V0,0,0), PL(V0,1,0), PL(V0,2,0));
-                            gx[1*NGX + gxi] = txy - A;
+                            gx[(gxi)*4 + 1] = txy - A;
                         }
                         // w at (i-1/2, m+1/2).
                         {
                             const TF uw = i2(PL(U0,0,0), PL(U1,0,0));
                             const TF A = adv6(uw, PL(W1,-3,0), PL(W1,-2,0), PL(W1,-1,0), PL(W1,0,0), PL(W1,1,0), PL(W1,2,0));
-                            gx[2*NGX + gxi] = txz - A;
+                            gx[(gxi)*4 + 2] = txz - A;
                         }
                         if (SCAL)
                         {
@@ -401,7 +395,7 @@ namespace mhh
                             const TF A = LIM ? lim_flux(uw, PL(S0,-2,0), PL(S0,-1,0), PL(S0,0,0), PL(S0,1,0), 0)
                                              : adv6(uw, PL(S0,-3,0), PL(S0,-2,0), PL(S0,-1,0), PL(S0,0,0), PL(S0,1,0), PL(S0,2,0));
                             const TF D = (TF(0.5)*(PL(E0,-1,0) + PL(E0,0,0))*tpri + svisc)*(PL(S0,0,0) - PL(S0,-1,0))*dxi;
-                            gx[3*NGX + gxi] = D - A;
+                            gx[(gxi)*4 + 3] = D - A;
                         }
                     }
                     if (face_y)
@@ -410,20 +404,20 @@ namespace mhh
                         {
                             const TF vs = i2(PL(V0,-1,0), PL(V0,0,0));
                             const TF A = adv6(vs, PL(U0,0,-3), PL(U0,0,-2), PL(U0,0,-1), PL(U0,0,0), PL(U0,0,1), PL(U0,0,2));
-                            gy[0*NGY + gyi] = txy - A;
+                            gy[(gyi)*4 + 0] = txy - A;
                         }
                         // v at the cell centre j-1.
                         {
                             const TF vs = i2(PL(V0,0,-1), PL(V0,0,0));
                             const TF A = adv6(vs, PL(V0,0,-3), PL(V0,0,-2), PL(V0,0,-1), PL(V0,0,0), PL(V0,0,1), PL(V0,0,2));
                             const TF D = TF(2)*(PL(E0,0,-1) + visc)*(PL(V0,0,0) - PL(V0,0,-1))*dyi;
-                            gy[1*NGY + gyi] = D - A;
+                            gy[(gyi)*4 + 1] = D - A;
                         }
                         // w at (j-1/2, m+1/2).
                         {
                             const TF vs = i2(PL(V0,0,0), PL(V1,0,0));
                             const TF A = adv6(vs, PL(W1,0,-3), PL(W1,0,-2), PL(W1,0,-1), PL(W1,0,0), PL(W1,0,1), PL(W1,0,2));
-                            gy[2*NGY + gyi] = tyz - A;
+                            gy[(gyi)*4 + 2] = tyz - A;
                         }
                         if (SCAL)
                         {
@@ -431,7 +425,7 @@ namespace mhh
                             const TF A = LIM ? lim_flux(vs, PL(S0,0,-2), PL(S0,0,-1), PL(S0,0,0), PL(S0,0,1), 0)
                                              : adv6(vs, PL(S0,0,-3), PL(S0,0,-2), PL(S0,0,-1), PL(S0,0,0), PL(S0,0,1), PL(S0,0,2));
                             const TF D = (TF(0.5)*(PL(E0,0,-1) + PL(E0,0,0))*tpri + svisc)*(PL(S0,0,0) - PL(S0,0,-1))*dyi;
-                            gy[3*NGY + gyi] = D - A;
+                            gy[(gyi)*4 + 3] = D - A;
                         }
                     }
                 }
@@ -528,41 +522,47 @@ namespace mhh
                 const TF zf = prof[5*PLEV + lq - 1];
                 if constexpr (sizeof(TF) == 4)
                 {
-                    // u and v in one packed pair.
-                    const float2 dgx = sub2(f2(gx[0*NGX + gx0 + 1], gx[1*NGX + gx0 + 1]), f2(gx[0*NGX + gx0], gx[1*NGX + gx0]));
-                    const float2 dgy = sub2(f2(gy[0*NGY + gy0 + FTX], gy[1*NGY + gy0 + FTX]), f2(gy[0*NGY + gy0], gy[1*NGY + gy0]));
-                    const float2 dgz = sub2(f2(gzu_t, gzv_t), f2(gzu_b, gzv_b));
-                    const float2 t = __ffma2_rn(dgz, f2(zf, zf), __ffma2_rn(dgy, f2(dyi, dyi),
-                                                __ffma2_rn(dgx, f2(dxi, dxi), f2(tu, tv))));
-                    a.ut[c] = t.x; a.vt[c] = t.y;
+                    // The four fields' face fluxes in one 16-byte load per face;
+                    // u/v and w/s in packed pairs.
+                    const float4 xa = reinterpret_cast<const float4*>(gx)[gx0];
+                    const float4 xb = reinterpret_cast<const float4*>(gx)[gx0 + 1];
+                    const float4 ya = reinterpret_cast<const float4*>(gy)[gy0];
+                    const float4 yb = reinterpret_cast<const float4*>(gy)[gy0 + FTX];
+                    {
+                        const float2 dgx = sub2(f2(xb.x, xb.y), f2(xa.x, xa.y));
+                        const float2 dgy = sub2(f2(yb.x, yb.y), f2(ya.x, ya.y));
+                        const float2 dgz = sub2(f2(gzu_t, gzv_t), f2(gzu_b, gzv_b));
+                        const float2 t = __ffma2_rn(dgz, f2(zf, zf), __ffma2_rn(dgy, f2(dyi, dyi),
+                                                    __ffma2_rn(dgx, f2(dxi, dxi), f2(tu, tv))));
+                        a.ut[c] = t.x; a.vt[c] = t.y;
+                    }
+                    if constexpr (SCAL)
+                    {
+                        const float2 dgx = sub2(f2(xb.z, xb.w), f2(xa.z, xa.w));
+                        const float2 dgy = sub2(f2(yb.z, yb.w), f2(ya.z, ya.w));
+                        const float2 dgz = sub2(f2(gzw_t, gzs_t), f2(gzw_b, gzs_b));
+                        const float2 t = __ffma2_rn(dgz, f2(prof[6*PLEV + lq], zf), __ffma2_rn(dgy, f2(dyi, dyi),
+                                                    __ffma2_rn(dgx, f2(dxi, dxi), f2(tw + buoy, ts))));
+                        if (wlev) a.wt[c + d.ijcells] = t.x;
+                        a.st[c] = t.y;
+                    }
+                    else if (wlev)
+                        a.wt[c + d.ijcells] = tw + (xb.z - xa.z)*dxi + (yb.z - ya.z)*dyi
+                                                 + (gzw_t - gzw_b)*prof[6*PLEV + lq] + buoy;
                 }
                 else
                 {
-                    a.ut[c] = tu + (gx[0*NGX + gx0 + 1] - gx[0*NGX + gx0])*dxi
-                                 + (gy[0*NGY + gy0 + FTX] - gy[0*NGY + gy0])*dyi + (gzu_t - gzu_b)*zf;
-                    a.vt[c] = tv + (gx[1*NGX + gx0 + 1] - gx[1*NGX + gx0])*dxi
-                                 + (gy[1*NGY + gy0 + FTX] - gy[1*NGY + gy0])*dyi + (gzv_t - gzv_b)*zf;
-                }
-                if constexpr (sizeof(TF) == 4 && SCAL)
-                {
-                    // w and s in one packed pair.
-                    const float2 dgx = sub2(f2(gx[2*NGX + gx0 + 1], gx[3*NGX + gx0 + 1]), f2(gx[2*NGX + gx0], gx[3*NGX + gx0]));
-                    const float2 dgy = sub2(f2(gy[2*NGY + gy0 + FTX], gy[3*NGY + gy0 + FTX]), f2(gy[2*NGY + gy0], gy[3*NGY + gy0]));
-                    const float2 dgz = sub2(f2(gzw_t, gzs_t), f2(gzw_b, gzs_b));
-                    const float2 t = __ffma2_rn(dgz, f2(prof[6*PLEV + lq], zf), __ffma2_rn(dgy, f2(dyi, dyi),
-                                                __ffma2_rn(dgx, f2(dxi, dxi), f2(tw + buoy, ts))));
-                    if (wlev) a.wt[c + d.ijcells] = t.x;
-                    a.st[c] = t.y;
-                }
-                else
-                {
+                    a.ut[c] = tu + (gx[(gx0 + 1)*4 + 0] - gx[(gx0)*4 + 0])*dxi
+                                 + (gy[(gy0 + FTX)*4 + 0] - gy[(gy0)*4 + 0])*dyi + (gzu_t - gzu_b)*zf;
+                    a.vt[c] = tv + (gx[(gx0 + 1)*4 + 1] - gx[(gx0)*4 + 1])*dxi
+                                 + (gy[(gy0 + FTX)*4 + 1] - gy[(gy0)*4 + 1])*dyi + (gzv_t - gzv_b)*zf;
                     if (wlev)
-                        a.wt[c + d.ijcells] = tw + (gx[2*NGX + gx0 + 1] - gx[2*NGX + gx0])*dxi
-                                                 + (gy[2*NGY + gy0 + FTX] - gy[2*NGY + gy0])*dyi
+                        a.wt[c + d.ijcells] = tw + (gx[(gx0 + 1)*4 + 2] - gx[(gx0)*4 + 2])*dxi
+                                                 + (gy[(gy0 + FTX)*4 + 2] - gy[(gy0)*4 + 2])*dyi
                                                  + (gzw_t - gzw_b)*prof[6*PLEV + lq] + buoy;
                     if (SCAL)
-                        a.st[c] = ts + (gx[3*NGX + gx0 + 1] - gx[3*NGX + gx0])*dxi
-                                     + (gy[3*NGY + gy0 + FTX] - gy[3*NGY + gy0])*dyi + (gzs_t - gzs_b)*zf;
+                        a.st[c] = ts + (gx[(gx0 + 1)*4 + 3] - gx[(gx0)*4 + 3])*dxi
+                                     + (gy[(gy0 + FTX)*4 + 3] - gy[(gy0)*4 + 3])*dyi + (gzs_t - gzs_b)*zf;
                 }
             }
 
