@@ -1040,8 +1040,10 @@ namespace mhh
     // lambda = bmati[i] + bmatj[j], and bmati, bmatj are mirror-symmetric
     // (i and itot - i share a wave number), so the columns form groups of up
     // to four with identical coefficients.  1/den_k of every group is computed
-    // once at set-up (k_tdma_table); the solve then needs three FP64 operations
-    // per cell, and one thread solves the four columns of a group together.
+    // once at set-up (k_tdma_table).  The reference-order solve (k_tdma) then
+    // needs three FP64 operations per cell with one thread for the four columns
+    // of a group; the rescaled solve (k_tdma_col) two, with one thread per
+    // column (k_tdma_scaled: the same with four columns per thread).
     // ---------------------------------------------------------------------
     __global__ void k_tdma_table(int niu, int nju, int ktot, const double* __restrict__ bmati,
                                  const double* __restrict__ bmatj, const double* __restrict__ a,
