@@ -6,7 +6,7 @@
  * Diff_2, Thermo_dry buoyancy, Pres_2 with x/y real FFTs and a Thomas solve
  * in z, the low-storage RK3 and the CFL / diffusion-number / divergence
  * reductions).  It is used by the tests, by __graft_entry__.smoke() and by
- * bench.py's CPU-baseline leg as the checker.  The product path never links,
+ * bench.py's CPU-baseline leg to compare against.  The product path never links,
  * loads or calls it.
  *
  * The same C API is exported by oracle/_ref/libmhh_ref.so, which is built

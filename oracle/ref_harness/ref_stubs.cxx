@@ -263,7 +263,7 @@ template<> Soil_grid<TF>::~Soil_grid() {}
 template<> const Soil_grid_data<TF>& Soil_grid<TF>::get_grid_data() { return empty_soil_grid; }
 
 // ---------------------------------------------------------------------------
-// Fields: storage only; the driver registers u, v, w, th, p, evisc.
+// Fields: storage only; ref_driver.cxx registers u, v, w, th, p, evisc.
 // ---------------------------------------------------------------------------
 template<>
 Fields<TF>::Fields(Master& m, Grid<TF>& g, Soil_grid<TF>& sg, Input& input) :
