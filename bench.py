@@ -164,6 +164,14 @@ def make_case(size, rank, ktot=None):
     return cases.drycbl(n, n, kt, 50. * n, 50. * n, 4000. * kt / (n // 2), seed=2 + rank, name=f"drycbl_{n}x{n}x{kt}")
 
 
+def bench_config(size, kt, world):
+    """The `config` of both arms' lines (the same workload)."""
+    return {"workload": f"dry CBL LES {size}x{size}x{kt}, domain {50*size}x{50*size}x{4000. * kt / (size // 2):g} m, "
+                        "Advec_2i5 + Smagorinsky (cs 0.23) + MOST surface + Boussinesq + Pres_2, RK3, dt=2 s",
+            "parallelism": f"replicas x{world}",
+            "l2": "inputs larger than L2 (one field 277 MB), no flush"}
+
+
 def timed_steps(model, steps, world):
     """Device time of `steps` RK3 steps (CUDA events on the model's stream)."""
     import torch
@@ -195,8 +203,9 @@ def cpu_baseline_sample(size, kt, substeps=3):
 
 
 def run_reference(args, world, rank):
-    """Each bench step is one RK3 substep (a third of a time step) of the full
-    case; `value` counts cell-steps as cells x substeps / 3."""
+    """The reference algorithm's CPU implementation on the same case: each
+    bench step is one full RK3 step (three substeps) of the whole grid, after
+    the warm-up steps; rank 0 alone runs."""
     if rank != 0:
         return
     from oracle import orcpy
@@ -207,19 +216,19 @@ def run_reference(args, world, rank):
     case = make_case(size, 0, kt)
     m = orcpy.model_from_case(case)
     cores = m.lib.orc_num_threads()
-    m.run_substeps(args.warmup)
+    m.run_substeps(3 * args.warmup)
     t0 = time.perf_counter()
-    m.run_substeps(args.steps)
+    m.run_substeps(3 * args.steps)
     total = time.perf_counter() - t0
     m.close()
-    value = n * (args.steps / 3.0) / total
-    sample = (f"{args.steps} RK3 substeps of drycbl {size}x{size}x{kt} after {args.warmup} warm-up substeps "
-              "(oracle port of the reference's hot-path code, OpenMP on all host cores)")
+    value = n * args.steps / total
+    sample = (f"{args.steps} RK3 steps of drycbl {size}x{size}x{kt} after {args.warmup} warm-up steps "
+              "(oracle port of the reference's hot-path code, FP64, OpenMP on all host cores)")
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / (args.steps / 3.0),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded dry CBL)",
-            "config": {"workload": f"dry CBL LES {size}x{size}x{kt}, Advec_2i5 + Smagorinsky + MOST + Pres_2, RK3, dt=2 s"},
+            "data": "synthetic (seeded dry CBL, theta noise +-0.1 K below 200 m)",
+            "config": bench_config(size, kt, world),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -292,7 +301,8 @@ def run_ours(args, world, rank, local):
         s64 = allreduce_max(timed_steps(m64, args.fp64_steps, world), world)
         v64 = allreduce_sum(n * args.fp64_steps / s64, world)
         fp64 = {"value": v64, "unit": UNIT, "ms_per_step": 1e3 * s64 / args.fp64_steps,
-                "steps": args.fp64_steps, "fp32_over_fp64": value / v64}
+                "steps": args.fp64_steps, "fp32_over_fp64": value / v64,
+                "note": "plain FP64 path, same case and kernels' FP64 builds, device-resident"}
         del m64
 
     # ---- roofline of the dominant kernel --------------------------------
@@ -319,17 +329,19 @@ def run_ours(args, world, rank, local):
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         dt, cores = cpu_baseline_sample(size, kt, 3)
         cpu = {"value": n / dt, "unit": UNIT, "cores": cores, "kind": "port",
-               "sample": f"1 RK3 step of drycbl {size}x{size}x{kt} (oracle port of the reference's hot-path code, OpenMP)"}
+               "sample": f"1 RK3 step of drycbl {size}x{size}x{kt} (oracle port of the reference's hot-path code, "
+                         "FP64, OpenMP)"}
+        if fp64:
+            # Like for like: the FP64 GPU path against the FP64 CPU code.
+            cpu["fp64_gpu_over_cpu"] = fp64["value"] / cpu["value"]
+            cpu["fp32_gpu_over_cpu"] = value / cpu["value"]
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 z-solve and reductions)",
                 "data": "synthetic (seeded dry CBL, theta noise +-0.1 K below 200 m)",
-                "config": {"workload": f"dry CBL LES {size}x{size}x{kt}, domain {50*size}x{50*size}x{case.zsize:g} m, "
-                                       "Advec_2i5 + Smagorinsky (cs 0.23) + MOST surface + Boussinesq + Pres_2, RK3, dt=2 s",
-                           "precision": "fp32 form", "parallelism": f"replicas x{world}",
-                           "l2": "inputs larger than L2 (one field 277 MB)"},
+                "config": bench_config(size, kt, world),
                 "fp64": fp64, "e2e": e2e, "roofline": roof, "step_roofline": step_roof,
                 "cpu_baseline": cpu, "clocks": clk, "gpu_launches": launches, "kernels": kernels,
                 "diagnostics": {"cfl": cfl, "div": div}}
@@ -367,7 +379,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=512)
     ap.add_argument("--ktot", type=int, default=0, help="vertical levels (default size/2)")
-    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--fp64-steps", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--form", default="step", choices=["step", "ensemble", "serve"],
                     help="step: the time-step throughput (default); ensemble / serve: the batching and "

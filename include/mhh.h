@@ -35,7 +35,7 @@ enum mhh_status
     MHH_ERR_ARG = -1,         /* invalid argument (NULL pointer, bad size, bad switch) */
     MHH_ERR_CUDA = -2,        /* a CUDA call failed */
     MHH_ERR_UNSUPPORTED = -3, /* e.g. an FFT length with a prime factor above 7 */
-    MHH_ERR_NONFINITE = -4,   /* a reduction returned NaN or inf */
+    MHH_ERR_NONFINITE = -4,   /* a reduction returned NaN or inf; a model run with non-finite numbers */
     MHH_ERR_TIMEOUT = -5      /* a bounded device wait ran out */
 };
 
@@ -265,9 +265,12 @@ int mhh_pres_2_get_divergence(mhh_ctx* ctx, const mhh_fields* f, double* div, cu
    memory after set-up, e.g. a host that charges every device allocation
    against a fixed HBM budget.  The scratch is a file-scope device array of
    the library: jtot*ktot <= 262144 (2 MiB of row maxima), larger grids return
-   MHH_ERR_ARG.  The first call on each device looks up the array's address;
-   make it before any stream capture.  Calls on one device share the array,
-   so calls that overlap in time race and must be serialised by the caller.
+   MHH_ERR_ARG.  The first call on each device looks up the array's address
+   and, as CUDA loads kernels lazily, may load the module that holds the
+   array (2 MiB of device memory, possibly a device synchronisation): make
+   one warm-up call during set-up, before any stream capture.  Calls on one
+   device share the array, so calls that overlap in time race and must be
+   serialised by the caller.  A NaN in u, v or w returns MHH_ERR_NONFINITE.
    Synchronises the stream. */
 int mhh_pres_2_get_divergence_noalloc(mhh_ctx* ctx, const mhh_fields* f, double* div, cudaStream_t stream);
 /* Halfcomplex x/y transforms of a packed itot*jtot*ktot array in place

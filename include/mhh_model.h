@@ -34,7 +34,11 @@ int mhh_model_get_field_native(mhh_model* m, const char* name, void* data);
 
 /* The time loop of src/model.cxx:356-505: n RK3 steps or substeps.
    fused = 1: one fused tendency kernel and a fused pressure-gradient + RK3
-   kernel per substep; fused = 0: the module-by-module call sequence. */
+   kernel per substep; fused = 0: the module-by-module call sequence.
+   Every [time] outputiter iterations (default 20; 0 = every substep) the
+   status check of src/model.cxx:842-872 computes the CFL number at the start
+   of a step and stops with MHH_ERR_NONFINITE ("Simulation has non-finite
+   numbers") when it is NaN, inf or outside [0, 10). */
 int mhh_model_run_steps(mhh_model* m, int n, int fused);
 int mhh_model_run_substeps(mhh_model* m, int n, int fused);
 

@@ -17,12 +17,19 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 LIBDIR = os.path.join(PKG, "lib")
 
 FP64, FP32 = 64, 32
+# mhh_status codes of include/mhh.h used by callers.
+ERR_ARG, ERR_NONFINITE = -1, -4
 ADVEC_2, ADVEC_2I5 = 2, 25
 DIFF_NONE, DIFF_2, DIFF_SMAG2 = 0, 2, 7
 
 
 class MhhError(RuntimeError):
-    pass
+    """A failed entry point; ``status`` is its mhh_status code (include/mhh.h),
+    e.g. -4 (MHH_ERR_NONFINITE) for a run with non-finite numbers."""
+
+    def __init__(self, msg, status=None):
+        super().__init__(msg)
+        self.status = status
 
 
 class GridDesc(ctypes.Structure):
@@ -204,7 +211,7 @@ def check(rc, what="mhh"):
         else:
             msg = kern.mhh_last_error()
         msg = msg or b""
-        raise MhhError(f"{what} failed ({rc}): {msg.decode(errors='replace')}")
+        raise MhhError(f"{what} failed ({rc}): {msg.decode(errors='replace')}", rc)
 
 
 def set_option(name, value):

@@ -112,9 +112,9 @@ namespace mhh
         if (i >= d.iend || j >= d.jend) return;
         const long long c = ijk(d, i, j, k);
         const TF pc = ld(p, c);
-        ut[c] -= (pc - ld(p, c-1))*dxi_of<TF>(d);
-        vt[c] -= (pc - ld(p, c-d.icells))*dyi_of<TF>(d);
-        wt[c] -= (pc - ld(p, c-d.ijcells))*ld(pr.dzhi, k);
+        ut[c] -= mulx(pc - ld(p, c-1), dxi_of<TF>(d));
+        vt[c] -= mulx(pc - ld(p, c-d.icells), dyi_of<TF>(d));
+        wt[c] -= mulx(pc - ld(p, c-d.ijcells), ld(pr.dzhi, k));
     }
 }
 
@@ -310,6 +310,7 @@ namespace
         const size_t tfb = c->prec == MHH_FP64 ? 8 : 4;
         if (cudaMallocAsync(&c->pw.pk, tfb*n, c->setup) != cudaSuccess) return fail(MHH_ERR_CUDA, "cudaMallocAsync pressure");
         if ((rc = dalloc(&c->pw.work, (size_t)n, false))) return rc;
+        if (cudaMallocAsync(&c->pw.dcm, sizeof(double)*d.ktot, c->setup) != cudaSuccess) return fail(MHH_ERR_CUDA, "cudaMallocAsync pressure");
         if ((rc = dalloc(&c->pw.bmati, d.itot)) || (rc = dalloc(&c->pw.bmatj, d.jtot))) return rc;
         if ((rc = dalloc(&c->pw.a, d.ktot)) || (rc = dalloc(&c->pw.c, d.ktot))) return rc;
         if ((rc = dalloc(&c->pw.dz2, d.ktot)) || (rc = dalloc(&c->pw.dz2rho, d.ktot))) return rc;
@@ -451,6 +452,7 @@ namespace
             fz.ut = CT<TF>(f->ut); fz.vt = CT<TF>(f->vt); fz.wt = CT<TF>(f->wt);
             fz.dti = TF(1./sub_dt);
             fz.p = T<TF>(f->p);
+            fz.dcm = static_cast<const TF*>(c->pw.dcm);
             fz.mode = 1;
             { Timed t("fft_x", s); launch_fft_x<TF>(c->pw.px, pk, d.jtot*d.ktot, false, 1., s, &fz); }
             { Timed t("fft_y", s); launch_fft_y<TF>(c->pw.py, pk, d.itot, d.jtot, d.ktot, false, 1., s); }
@@ -479,7 +481,7 @@ namespace
         { Timed t("fft_x", s); launch_fft_x<TF>(c->pw.px, pk, d.jtot*d.ktot, true, 1./d.itot, s); }
         {
             Timed t("pres_scatter", s);
-            launch_pres_scatter<TF>(d, pk, T<TF>(f->p), s);
+            launch_pres_scatter<TF>(d, pk, static_cast<const TF*>(c->pw.dcm), T<TF>(f->p), s);
             fl.p[0] = T<TF>(f->p); launch_cyclic(fl, d, MHH_EDGE_BOTH, s);
         }
         }
@@ -863,8 +865,8 @@ int mhh_ctx_estimate_bytes(const mhh_grid_desc* g, int precision, size_t* bytes)
     const double groups = double(g->itot/2 + 1)*(g->jtot/2 + 1)*g->ktot;
     double b = 0.;
     b += 12.*kcells*tf;                         // profiles
-    b += n*tf + n*8.;                           // packed pressure + work
-    b += groups*(8. + 8. + 8. + 4. + 8.);      // elimination tables
+    b += n*tf + n*8. + g->ktot*8.;              // packed pressure + work + level means
+    b += groups*(8. + 8. + 8. + 8. + 4. + 8.); // elimination tables
     b += 2.*(g->itot + g->jtot)*(16. + 8.);    // twiddles
     b += 12.*ij*8. + ij*4. + 2.*10000*4.;      // surface layer
     b += 2.*kcells*8.;                          // mixing length
@@ -881,7 +883,7 @@ int mhh_ctx_destroy(mhh_ctx* c)
     // stream reaches it; the caller has finished its own work on the fields.
     for (auto& p : c->dprof) if (p) cudaFreeAsync(p, c->setup);
     fft_plan_free(&c->pw.px, c->setup); fft_plan_free(&c->pw.py, c->setup);
-    void* ptrs[] = {c->pw.pk, c->pw.work, c->pw.rtab, c->pw.gtab, c->pw.htab, c->pw.stab, c->pw.stabd, c->pw.bmati, c->pw.bmatj, c->pw.a, c->pw.c, c->pw.dz2, c->pw.dz2rho,
+    void* ptrs[] = {c->pw.pk, c->pw.work, c->pw.dcm, c->pw.rtab, c->pw.wtab, c->pw.gtab, c->pw.htab, c->pw.stab, c->pw.stabd, c->pw.bmati, c->pw.bmatj, c->pw.a, c->pw.c, c->pw.dz2, c->pw.dz2rho,
                     c->red, c->statbuf, c->bufprof, c->sw.fm, c->sw.fh, c->sw.phim, c->sw.phih, c->sw.ustar, c->sw.obuk, c->sw.dudz, c->sw.dvdz, c->sw.dbdz, c->sw.dutot,
                     c->sw.nobuk, c->sw.zL, c->sw.f, c->sw.mlen2, c->sw.mlen2f};
     for (void* p : ptrs) if (p) cudaFreeAsync(p, c->setup);

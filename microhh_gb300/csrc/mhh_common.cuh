@@ -75,9 +75,28 @@ namespace mhh
 
     // Monotone max of non-negative doubles through their bit patterns
     // (a NaN, bit pattern above +inf, wins, so a blow-up is reported).
+    // A product rounded on its own in double, never contracted with a
+    // following addition into an FMA.  The FP64 path uses it where the
+    // reference's CPU build rounds large elementwise terms separately (u/dt
+    // in the pressure right-hand side, the pressure gradient, the RK3
+    // update): the level sums of the right-hand side feed the mean-mode
+    // pressure solve, whose conditioning amplifies any difference in their
+    // round-off.  In float the compiler may contract as usual.
+    __device__ __forceinline__ double mulx(double a, double b) { return __dmul_rn(a, b); }
+    __device__ __forceinline__ float mulx(float a, float b) { return a*b; }
+
+    // Maximum that keeps a NaN of either operand.  fmax returns the other
+    // operand when one is NaN, which would turn a blown-up field into a
+    // finite CFL, diffusion number or divergence.
+    template<typename T> __device__ __forceinline__ T max_nan(T a, T b) { return (a != a || a > b) ? a : b; }
+
+    // Maximum of non-negative doubles on their bit patterns, which order like
+    // the values.  A NaN is stored as the positive quiet NaN, whose pattern
+    // is above that of +inf, so it survives every later maximum.
     __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* dst, double v)
     {
-        atomicMax(dst, (unsigned long long)__double_as_longlong(v));
+        const unsigned long long bits = v != v ? 0x7ff8000000000000ull : (unsigned long long)__double_as_longlong(v);
+        atomicMax(dst, bits);
     }
 
     // Exact float <-> double conversions on the integer pipe (IEEE 754

@@ -135,11 +135,13 @@ namespace mhh
         double* dz2;          // ktot: dz^2
         double* dz2rho;       // ktot: dz^2 * rhoref
         double* work;         // itot*jtot*ktot doubles: forward-swept right-hand side
-        double* rtab;         // (itot/2+1)*(jtot/2+1)*ktot: 1/den per column group and level
+        double* rtab;         // (itot/2+1)*(jtot/2+1)*ktot: den per column group and level
+        double* wtab;         // same shape: c_k/den_k, the back-substitution factor
         double* gtab;         // same shape: forward coefficient of the rescaled recurrence
         double* htab;         // same shape: backward coefficient of the rescaled recurrence
         float* stab;          // same shape: output scale dz^2/den in float
         double* stabd;        // same shape: output scale dz^2/den
+        void* dcm;            // ktot values (TF): each level's mean, (X_00/jtot)/itot
         int niu, nju;
     };
 
@@ -163,6 +165,8 @@ namespace mhh
     // Work fused into the row (x) FFT: mode 1 computes the pressure
     // right-hand side in place of loading the forward transform's input;
     // mode 2 stores the inverse transform's output into the ghost layout of p.
+    // With mode 2, dcm (if set) holds each level's mean, which the tridiagonal
+    // solve took out of the mean mode; it is added to every stored point.
     template<typename TF>
     struct FftFuse
     {
@@ -172,13 +176,14 @@ namespace mhh
         const TF *u, *v, *w, *ut, *vt, *wt;
         TF dti;
         TF* p;
+        const TF* dcm;
     };
     template<typename TF> void launch_fft_x(const FftPlan& pl, TF* data, int nrows, bool inverse, double scale, cudaStream_t s,
                                             const FftFuse<TF>* fuse = nullptr);
     template<typename TF> void launch_fft_y(const FftPlan& pl, TF* data, int itot, int jtot, int ktot, bool inverse,
                                             double scale, cudaStream_t s);
     template<typename TF> void launch_tdma(const Dims& d, const PresWork& pw, TF* pk, const KernelOpts& o, cudaStream_t s);
-    template<typename TF> void launch_pres_scatter(const Dims& d, const TF* pk, TF* p, cudaStream_t s);
+    template<typename TF> void launch_pres_scatter(const Dims& d, const TF* pk, const TF* dcm, TF* p, cudaStream_t s);
 
     // ---- surface layer (mhh_surface.cu) ----
     struct SurfWork

@@ -20,11 +20,16 @@
 // the previous call's values until they are overwritten.
 //
 // The first call on each device looks up the array's device address
-// (cudaGetSymbolAddress, with that device current) and keeps it; make that
-// first call before any stream capture.  All calls on one device share the
-// array: calls that overlap in time (other host threads, or other streams
-// whose work is not ordered with this call) race on it and must be
-// serialised by the caller.
+// (cudaGetSymbolAddress, with that device current) and keeps it.  CUDA loads
+// a library's kernels lazily by default, so that first call can also load
+// this file's module, which places the 2 MiB array in device memory and may
+// synchronise the device.  Callers therefore make one warm-up call during
+// their own set-up, before any stream capture; later calls allocate nothing
+// and do not load anything.  All calls on one device share the array: calls
+// that overlap in time (other host threads, or other streams whose work is
+// not ordered with this call) race on it and must be serialised by the
+// caller.  A NaN anywhere in u, v or w gives a NaN maximum, reported as
+// MHH_ERR_NONFINITE.
 #include <cmath>
 #include <mutex>
 
@@ -80,16 +85,16 @@ namespace mhh
             const long long c = ijk(d, i, j, k);
             const double div = double(ld(pr.rhoref, k))*(double(ld(u, c+ii)-ld(u, c))*d.dxi + double(ld(v, c+jj)-ld(v, c))*d.dyi)
                              + (double(ld(pr.rhorefh, k+1))*double(ld(w, c+kk)) - double(ld(pr.rhorefh, k))*double(ld(w, c)))*double(ld(pr.dzi, k));
-            val = fmax(val, fabs(div));
+            val = max_nan(val, fabs(div));
         }
         for (int o=16; o>0; o>>=1)
-            val = fmax(val, __shfl_xor_sync(0xffffffffu, val, o));
+            val = max_nan(val, __shfl_xor_sync(0xffffffffu, val, o));
         __shared__ double sm[4];
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
         if (lane == 0) sm[warp] = val;
         __syncthreads();
         if (threadIdx.x == 0)
-            rows[blockIdx.x + (long long)blockIdx.y*gridDim.x] = fmax(fmax(sm[0], sm[1]), fmax(sm[2], sm[3]));
+            rows[blockIdx.x + (long long)blockIdx.y*gridDim.x] = max_nan(max_nan(sm[0], sm[1]), max_nan(sm[2], sm[3]));
     }
 
     // One block: the maximum of n row maxima into *out.
@@ -98,9 +103,9 @@ namespace mhh
     {
         double val = 0.;
         for (int q = threadIdx.x; q < n; q += blockDim.x)
-            val = fmax(val, rows[q]);
+            val = max_nan(val, rows[q]);
         for (int o=16; o>0; o>>=1)
-            val = fmax(val, __shfl_xor_sync(0xffffffffu, val, o));
+            val = max_nan(val, __shfl_xor_sync(0xffffffffu, val, o));
         __shared__ double sm[32];
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
         if (lane == 0) sm[warp] = val;
@@ -109,7 +114,7 @@ namespace mhh
         {
             val = sm[lane];
             for (int o=16; o>0; o>>=1)
-                val = fmax(val, __shfl_xor_sync(0xffffffffu, val, o));
+                val = max_nan(val, __shfl_xor_sync(0xffffffffu, val, o));
             if (lane == 0) *out = val;
         }
     }

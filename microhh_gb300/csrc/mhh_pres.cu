@@ -21,6 +21,10 @@ namespace mhh
     template<> struct C2<double> { using T = double2; };
     template<> struct C2<float> { using T = float2; };
 
+    // a + b rounded once and never contracted with a preceding product.
+    __device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+    __device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+
     template<typename T2> __device__ __forceinline__ T2 cmul(T2 a, T2 b)
     {
         T2 r; r.x = a.x*b.x - a.y*b.y; r.y = a.x*b.y + a.y*b.x; return r;
@@ -302,10 +306,11 @@ namespace mhh
     {
         const long long ii = 1, jj = d.icells, kk = d.ijcells;
         const TF rho = ld(pr.rhoref, kg);
-        return rho*((ld(ut, c+ii) + ld(u, c+ii)*dti) - (ld(ut, c) + ld(u, c)*dti))*dxi_of<TF>(d)
-             + rho*((ld(vt, c+jj) + ld(v, c+jj)*dti) - (ld(vt, c) + ld(v, c)*dti))*dyi_of<TF>(d)
-             + (ld(pr.rhorefh, kg+1)*(ld(wt, c+kk) + ld(w, c+kk)*dti)
-              - ld(pr.rhorefh, kg  )*(ld(wt, c   ) + ld(w, c   )*dti))*ld(pr.dzi, kg);
+        const TF du = (ld(ut, c+ii) + mulx(ld(u, c+ii), dti)) - (ld(ut, c) + mulx(ld(u, c), dti));
+        const TF dv = (ld(vt, c+jj) + mulx(ld(v, c+jj), dti)) - (ld(vt, c) + mulx(ld(v, c), dti));
+        const TF dw = mulx(ld(pr.rhorefh, kg+1), ld(wt, c+kk) + mulx(ld(w, c+kk), dti))
+                    - mulx(ld(pr.rhorefh, kg  ), ld(wt, c   ) + mulx(ld(w, c   ), dti));
+        return mulx(mulx(rho, du), dxi_of<TF>(d)) + mulx(mulx(rho, dv), dyi_of<TF>(d)) + mulx(dw, ld(pr.dzi, kg));
     }
 
     template<typename TF>
@@ -459,10 +464,14 @@ namespace mhh
                         const int kg = kgs[b];
                         const TF rho = ld(fz.pr.rhoref, kg);
                         const TF dti = fz.dti;
-                        const TF val = rho*((x[0] + x[1]*dti) - (x[2] + x[3]*dti))*dxi_of<TF>(fz.d)
-                                     + rho*((x[4] + x[5]*dti) - (x[6] + x[7]*dti))*dyi_of<TF>(fz.d)
-                                     + (ld(fz.pr.rhorefh, kg+1)*(x[8] + x[9]*dti)
-                                      - ld(fz.pr.rhorefh, kg  )*(x[10] + x[11]*dti))*ld(fz.pr.dzi, kg);
+                        // The operation order of src/pres_2.cxx:184-191
+                        // (products not contracted in double).
+                        const TF du = (x[0] + mulx(x[1], dti)) - (x[2] + mulx(x[3], dti));
+                        const TF dv = (x[4] + mulx(x[5], dti)) - (x[6] + mulx(x[7], dti));
+                        const TF dw = mulx(ld(fz.pr.rhorefh, kg+1), x[8] + mulx(x[9], dti))
+                                    - mulx(ld(fz.pr.rhorefh, kg  ), x[10] + mulx(x[11], dti));
+                        const TF val = mulx(mulx(rho, du), dxi_of<TF>(fz.d)) + mulx(mulx(rho, dv), dyi_of<TF>(fz.d))
+                                     + mulx(dw, ld(fz.pr.dzi, kg));
                         r1[ls*ns + i] = ls < nloc ? val : TF(0);
                     }
                 }
@@ -581,7 +590,7 @@ namespace mhh
                 const int ls = e / n, i = e - ls*n;
                 if (ls < nloc)
                 {
-                    const TF val = rout[ls*ns + i];
+                    const TF val = fz.dcm ? add_rn(rout[ls*ns + i], fz.dcm[ti.sk[ls]]) : rout[ls*ns + i];
                     const long long c = ti.sc[ls] + i;
                     fz.p[c] = val;
                     if (ti.sk[ls] == 0) fz.p[c - fz.d.ijcells] = val;
@@ -788,7 +797,8 @@ namespace mhh
                     const int ls = e / N, i = e - ls*N;
                     if (ls < nloc)
                     {
-                        const TF val = fft_real_out<TF, INV, N, SS, ROWS>(res, ls, i, scale);
+                        TF val = fft_real_out<TF, INV, N, SS, ROWS>(res, ls, i, scale);
+                        if (fz.dcm) val = add_rn(val, fz.dcm[x.sk[ls]]);
                         const long long c = x.sc[ls] + i;
                         fz.p[c] = val;
                         if (x.sk[ls] == 0) fz.p[c - fz.d.ijcells] = val;
@@ -1039,17 +1049,21 @@ namespace mhh
     // The elimination coefficients depend on the column only through
     // lambda = bmati[i] + bmatj[j], and bmati, bmatj are mirror-symmetric
     // (i and itot - i share a wave number), so the columns form groups of up
-    // to four with identical coefficients.  1/den_k of every group is computed
-    // once at set-up (k_tdma_table).  The reference-order solve (k_tdma) then
-    // needs three FP64 operations per cell with one thread for the four columns
-    // of a group; the rescaled solve (k_tdma_col) two, with one thread per
-    // column (k_tdma_scaled: the same with four columns per thread).
+    // to four with identical coefficients.  den_k and c_k/den_k of every group
+    // are computed once at set-up (k_tdma_table), rounded as the reference
+    // rounds them.  The reference-order solve (k_tdma) then repeats the
+    // reference's per-cell operations (a product, a difference and a division
+    // forward, a product and a difference back) with one thread for the four
+    // columns of a group: the mean mode's solve is ill-conditioned, so its
+    // result follows every rounding of the sweep.  The rescaled solve
+    // (k_tdma_col) needs two FMAs per cell, with one thread per column
+    // (k_tdma_scaled: the same with four columns per thread).
     // ---------------------------------------------------------------------
     __global__ void k_tdma_table(int niu, int nju, int ktot, const double* __restrict__ bmati,
                                  const double* __restrict__ bmatj, const double* __restrict__ a,
                                  const double* __restrict__ c, const double* __restrict__ dz2rho,
                                  const double* __restrict__ dz2, double* __restrict__ rtab,
-                                 double* __restrict__ gtab, double* __restrict__ htab,
+                                 double* __restrict__ wtab, double* __restrict__ gtab, double* __restrict__ htab,
                                  float* __restrict__ stab, double* __restrict__ stabd)
     {
         const int iu = blockIdx.x*blockDim.x + threadIdx.x;
@@ -1059,19 +1073,22 @@ namespace mhh
         const long long base = iu + (long long)ju*niu;
         const double lam = bmati[iu] + bmatj[ju];
         const bool mean_mode = (iu == 0 && ju == 0);
-        double b = dz2rho[0]*lam - (a[0] + c[0]);
+        // src/pres_2.cxx:266-326 and :200-263, products not contracted.
+        double b = mulx(dz2rho[0], lam) - (a[0] + c[0]);
         b += a[0];
         if (ktot == 1) b += mean_mode ? -c[0] : c[0];
         double den = b;
-        rtab[base] = 1.0/den;
+        rtab[base] = den;
         for (int k=1; k<ktot; ++k)
         {
-            double bk = dz2rho[k]*lam - (a[k] + c[k]);
+            double bk = mulx(dz2rho[k], lam) - (a[k] + c[k]);
             if (k == ktot-1) bk += mean_mode ? -c[k] : c[k];
             const double w3 = c[k-1]/den;
-            den = bk - a[k]*w3;
-            rtab[base + k*stride] = 1.0/den;
+            wtab[base + (k-1)*stride] = w3;
+            den = bk - mulx(a[k], w3);
+            rtab[base + k*stride] = den;
         }
+        wtab[base + (ktot-1)*stride] = 0.;
         // Rescaled recurrence: with s_k = dz2_k/den_k, y_k = s_k z_k and
         // x_k = s_k xi_k the sweeps become
         //   z_k = p_k - g_k z_{k-1},      g_k = a_k s_{k-1}/dz2_k,
@@ -1079,11 +1096,11 @@ namespace mhh
         // and x_k = s_k xi_k: one FMA per cell and sweep.
         for (int k=0; k<ktot; ++k)
         {
-            const double sk = dz2[k]*rtab[base + k*stride];
+            const double sk = dz2[k]/rtab[base + k*stride];
             stabd[base + k*stride] = sk;
             stab[base + k*stride] = float(sk);
-            gtab[base + k*stride] = k ? a[k]*(dz2[k-1]*rtab[base + (k-1)*stride])/dz2[k] : 0.;
-            htab[base + k*stride] = k < ktot-1 ? c[k]*(dz2[k+1]*rtab[base + (k+1)*stride])/dz2[k] : 0.;
+            gtab[base + k*stride] = k ? a[k]*(dz2[k-1]/rtab[base + (k-1)*stride])/dz2[k] : 0.;
+            htab[base + k*stride] = k < ktot-1 ? c[k]*(dz2[k+1]/rtab[base + (k+1)*stride])/dz2[k] : 0.;
         }
     }
 
@@ -1095,11 +1112,24 @@ namespace mhh
     constexpr int TDMA_KF = 8;
     constexpr int TDMA_KBK = 4;
 
+    // Output of column col at level k.  The mean mode (col 0) is not stored:
+    // its level mean (X_00/jtot)/itot goes to dcm[k] and the column gets
+    // zero, so that the inverse transforms carry only the other modes and the
+    // large hydrostatic part of p stays out of their round-off; the inverse
+    // x transform (or the scatter) adds the mean to every point.
+    template<typename TF>
+    __device__ __forceinline__ TF dc_out(TF val, int col, int k, int itot, int jtot, TF* __restrict__ dcm)
+    {
+        if (col != 0) return val;
+        dcm[k] = TF((double(val) / jtot) / itot);
+        return TF(0);
+    }
+
     template<typename TF>
     __global__ void __launch_bounds__(128)
     k_tdma(int itot, int jtot, int ktot, int niu, int nju, const double* __restrict__ rtab,
-           const double* __restrict__ a, const double* __restrict__ c, const double* __restrict__ dz2,
-           TF* __restrict__ pk, double* __restrict__ work)
+           const double* __restrict__ wtab, const double* __restrict__ a, const double* __restrict__ dz2,
+           TF* __restrict__ pk, double* __restrict__ work, TF* __restrict__ dcm)
     {
         const int iu = blockIdx.x*blockDim.x + threadIdx.x;
         const int ju = blockIdx.y;
@@ -1118,7 +1148,8 @@ namespace mhh
         const int ja = ju*itot, jb = (j1 >= 0 ? j1 : ju)*itot;
         const int col[4] = {ia + ja, ib + ja, ia + jb, ib + jb};
 
-        // Forward sweep: y_k = (dz2_k p_k - a_k y_{k-1}) / den_k.
+        // Forward sweep: y_k = (dz2_k p_k - a_k y_{k-1}) / den_k, rounded
+        // after each operation as in src/pres_2.cxx:200-263.
         double y[4] = {0., 0., 0., 0.};
         for (int k0=0; k0<ktot; k0+=TDMA_KF)
         {
@@ -1144,27 +1175,29 @@ namespace mhh
                 if (b < nk)
                 {
                     const int k = k0 + b;
-                    const double dr = dz2[k]*r[b];
-                    const double ar = k ? a[k]*r[b] : 0.;
+                    const double dzk = dz2[k];
+                    const double ak = a[k];
                     double* wrow = work + (long long)k*kk;
                     #pragma unroll
                     for (int q=0; q<4; ++q)
                     {
                         if (use[q])
                         {
-                            y[q] = double(pv[b][q])*dr - ar*y[q];
+                            double x = mulx(dzk, double(pv[b][q]));
+                            if (k) x = x - mulx(ak, y[q]);
+                            y[q] = x / r[b];
                             wrow[col[q]] = y[q];
                         }
                     }
                 }
             }
         }
-        // Back substitution: x_k = y_k - c_k/den_k x_{k+1}.
+        // Back substitution: x_k = y_k - (c_k/den_k) x_{k+1}.
         {
             TF* row = pk + (long long)(ktot-1)*kk;
             #pragma unroll
             for (int q=0; q<4; ++q)
-                if (use[q]) row[col[q]] = TF(y[q]);
+                if (use[q]) row[col[q]] = dc_out<TF>(TF(y[q]), col[q], ktot-1, itot, jtot, dcm);
         }
         for (int k0=ktot-2; k0>=0; k0-=TDMA_KBK)
         {
@@ -1177,7 +1210,7 @@ namespace mhh
                 if (b < nk)
                 {
                     const long long k = k0 - b;
-                    r[b] = __ldg(&rtab[base + k*stride]);
+                    r[b] = __ldg(&wtab[base + k*stride]);
                     const double* wrow = work + k*kk;
                     #pragma unroll
                     for (int q=0; q<4; ++q)
@@ -1190,15 +1223,15 @@ namespace mhh
                 if (b < nk)
                 {
                     const int k = k0 - b;
-                    const double w3 = c[k]*r[b];
+                    const double w3 = r[b];
                     TF* row = pk + (long long)k*kk;
                     #pragma unroll
                     for (int q=0; q<4; ++q)
                     {
                         if (use[q])
                         {
-                            y[q] = wv[b][q] - w3*y[q];
-                            row[col[q]] = TF(y[q]);
+                            y[q] = wv[b][q] - mulx(w3, y[q]);
+                            row[col[q]] = dc_out<TF>(TF(y[q]), col[q], k, itot, jtot, dcm);
                         }
                     }
                 }
@@ -1223,7 +1256,7 @@ namespace mhh
     __global__ void __launch_bounds__(128)
     k_tdma_scaled(int itot, int jtot, int ktot, int niu, int nju, const double* __restrict__ gtab,
                   const double* __restrict__ htab, const float* __restrict__ stab, const double* __restrict__ stabd,
-                  TF* __restrict__ pk, double* __restrict__ work)
+                  TF* __restrict__ pk, double* __restrict__ work, TF* __restrict__ dcm)
     {
         const int iu = blockIdx.x*blockDim.x + threadIdx.x;
         const int ju = blockIdx.y;
@@ -1284,7 +1317,7 @@ namespace mhh
             TF* row = pk + k*kk;
             #pragma unroll
             for (int q=0; q<4; ++q)
-                if (use[q]) row[col[q]] = scale_out<TF>(z[q], s, sd);
+                if (use[q]) row[col[q]] = dc_out<TF>(scale_out<TF>(z[q], s, sd), col[q], (int)k, itot, jtot, dcm);
         }
         for (int k0=ktot-2; k0>=0; k0-=TDMA_KBK)
         {
@@ -1319,7 +1352,7 @@ namespace mhh
                         if (use[q])
                         {
                             z[q] = fma(-h[b], z[q], zv[b][q]);
-                            row[col[q]] = scale_out<TF>(z[q], s[b], sd[b]);
+                            row[col[q]] = dc_out<TF>(scale_out<TF>(z[q], s[b], sd[b]), col[q], k0 - b, itot, jtot, dcm);
                         }
                     }
                 }
@@ -1342,7 +1375,7 @@ namespace mhh
     __global__ void __launch_bounds__(128, 8)
     k_tdma_col(int itot, int jtot, int ktot, int niu, int nju, const double* __restrict__ gtab,
                const double* __restrict__ htab, const float* __restrict__ stab, const double* __restrict__ stabd,
-               TF* __restrict__ pk, double* __restrict__ work)
+               TF* __restrict__ pk, double* __restrict__ work, TF* __restrict__ dcm)
     {
         const int t = blockIdx.x*blockDim.x + threadIdx.x;
         const int iu = t >> 2, q = t & 3;
@@ -1385,7 +1418,7 @@ namespace mhh
             const long long k = ktot - 1;
             const float s = __ldg(stab + base + k*stride);
             const double sd = sizeof(TF) == 8 ? __ldg(stabd + base + k*stride) : 0.;
-            pk[col + k*kk] = scale_out<TF>(z, s, sd);
+            pk[col + k*kk] = dc_out<TF>(scale_out<TF>(z, s, sd), col, (int)k, itot, jtot, dcm);
         }
         for (int k0=ktot-2; k0>=0; k0-=TDC_KB)
         {
@@ -1407,7 +1440,7 @@ namespace mhh
                 if (b < nk)
                 {
                     z = fma(-h[b], z, zv[b]);
-                    pk[col + (long long)(k0 - b)*kk] = scale_out<TF>(z, s[b], sd[b]);
+                    pk[col + (long long)(k0 - b)*kk] = dc_out<TF>(scale_out<TF>(z, s[b], sd[b]), col, k0 - b, itot, jtot, dcm);
                 }
         }
     }
@@ -1418,13 +1451,14 @@ namespace mhh
         pw.nju = jtot/2 + 1;
         const size_t n = (size_t)pw.niu*pw.nju*ktot;
         if (cudaMallocAsync((void**)&pw.rtab, sizeof(double)*n, s) != cudaSuccess) return MHH_ERR_CUDA;
+        if (cudaMallocAsync((void**)&pw.wtab, sizeof(double)*n, s) != cudaSuccess) return MHH_ERR_CUDA;
         if (cudaMallocAsync((void**)&pw.gtab, sizeof(double)*n, s) != cudaSuccess) return MHH_ERR_CUDA;
         if (cudaMallocAsync((void**)&pw.htab, sizeof(double)*n, s) != cudaSuccess) return MHH_ERR_CUDA;
         if (cudaMallocAsync((void**)&pw.stab, sizeof(float)*n, s) != cudaSuccess) return MHH_ERR_CUDA;
         if (cudaMallocAsync((void**)&pw.stabd, sizeof(double)*n, s) != cudaSuccess) return MHH_ERR_CUDA;
         dim3 grid((pw.niu + 127)/128, pw.nju);
         k_tdma_table<<<grid, 128, 0, s>>>(pw.niu, pw.nju, ktot, pw.bmati, pw.bmatj, pw.a, pw.c, pw.dz2rho, pw.dz2,
-                                    pw.rtab, pw.gtab, pw.htab, pw.stab, pw.stabd);
+                                    pw.rtab, pw.wtab, pw.gtab, pw.htab, pw.stab, pw.stabd);
         count_launch();
         return cudaStreamSynchronize(s) == cudaSuccess ? MHH_OK : MHH_ERR_CUDA;
     }
@@ -1433,18 +1467,19 @@ namespace mhh
     void launch_tdma(const Dims& d, const PresWork& pw, TF* pk, const KernelOpts& o, cudaStream_t s)
     {
         dim3 grid((pw.niu + 127)/128, pw.nju);
+        TF* dcm = static_cast<TF*>(pw.dcm);
         const int v = o.tdma < 0 ? (sizeof(TF) == 4 ? 1 : 0) : o.tdma;
         if (v == 1)
         {
             dim3 gridc((4*pw.niu + 127)/128, pw.nju);
             k_tdma_col<TF><<<gridc, 128, 0, s>>>(d.itot, d.jtot, d.ktot, pw.niu, pw.nju, pw.gtab, pw.htab,
-                                                 pw.stab, pw.stabd, pk, pw.work);
+                                                 pw.stab, pw.stabd, pk, pw.work, dcm);
         }
         else if (v == 2)
             k_tdma_scaled<TF><<<grid, 128, 0, s>>>(d.itot, d.jtot, d.ktot, pw.niu, pw.nju, pw.gtab, pw.htab,
-                                                   pw.stab, pw.stabd, pk, pw.work);
+                                                   pw.stab, pw.stabd, pk, pw.work, dcm);
         else
-            k_tdma<TF><<<grid, 128, 0, s>>>(d.itot, d.jtot, d.ktot, pw.niu, pw.nju, pw.rtab, pw.a, pw.c, pw.dz2, pk, pw.work);
+            k_tdma<TF><<<grid, 128, 0, s>>>(d.itot, d.jtot, d.ktot, pw.niu, pw.nju, pw.rtab, pw.wtab, pw.a, pw.dz2, pk, pw.work, dcm);
         count_launch();
     }
 
@@ -1452,24 +1487,24 @@ namespace mhh
     // p[kstart-1] = p[kstart], src/pres_2.cxx:330-358 (the periodic fill
     // follows separately).
     template<typename TF>
-    __global__ void k_pres_scatter(Dims d, const TF* __restrict__ pk, TF* __restrict__ p)
+    __global__ void k_pres_scatter(Dims d, const TF* __restrict__ pk, const TF* __restrict__ dcm, TF* __restrict__ p)
     {
         const int i = blockIdx.x*blockDim.x + threadIdx.x;
         const int j = blockIdx.y*blockDim.y + threadIdx.y;
         const int k = blockIdx.z;
         if (i >= d.itot || j >= d.jtot) return;
-        const TF val = pk[i + (long long)j*d.itot + (long long)k*d.itot*d.jtot];
+        const TF val = add_rn(pk[i + (long long)j*d.itot + (long long)k*d.itot*d.jtot], dcm[k]);
         const long long c = ijk(d, i + d.igc, j + d.jgc, k + d.kgc);
         p[c] = val;
         if (k == 0) p[c - d.ijcells] = val;
     }
 
     template<typename TF>
-    void launch_pres_scatter(const Dims& d, const TF* pk, TF* p, cudaStream_t s)
+    void launch_pres_scatter(const Dims& d, const TF* pk, const TF* dcm, TF* p, cudaStream_t s)
     {
         dim3 block(32, 8);
         dim3 grid((d.itot + 31)/32, (d.jtot + 7)/8, d.ktot);
-        k_pres_scatter<TF><<<grid, block, 0, s>>>(d, pk, p);
+        k_pres_scatter<TF><<<grid, block, 0, s>>>(d, pk, dcm, p);
         count_launch();
     }
 
@@ -1478,7 +1513,7 @@ namespace mhh
     template void launch_fft_x<TF>(const FftPlan&, TF*, int, bool, double, cudaStream_t, const FftFuse<TF>*); \
     template void launch_fft_y<TF>(const FftPlan&, TF*, int, int, int, bool, double, cudaStream_t); \
     template void launch_tdma<TF>(const Dims&, const PresWork&, TF*, const KernelOpts&, cudaStream_t); \
-    template void launch_pres_scatter<TF>(const Dims&, const TF*, TF*, cudaStream_t);
+    template void launch_pres_scatter<TF>(const Dims&, const TF*, const TF*, TF*, cudaStream_t);
 
     MHH_PRES_INST(double)
     MHH_PRES_INST(float)

@@ -454,7 +454,7 @@ namespace mhh
         if (interior)
         {
             const TF t = at[n];
-            a[n] += cbdt*t;
+            a[n] = a[n] + mulx(cbdt, t);
             at[n] = last ? TF(0) : t*ca;
         }
         else if (last)
@@ -530,17 +530,19 @@ namespace mhh
         if (interior)
         {
             const TF pc = ld(p, c);
-            TF tu = ut[c] - (pc - ld(p, c-1))*dxi_of<TF>(d);
-            TF tv = vt[c] - (pc - ld(p, c-d.icells))*dyi_of<TF>(d);
-            TF tw = wt[c] - (pc - ld(p, c-d.ijcells))*ld(pr.dzhi, k);
-            u[c] += cbdt*tu; v[c] += cbdt*tv; w[c] += cbdt*tw;
+            // src/pres_2.cxx:380-382 and src/timeloop.cxx:264 (products not
+            // contracted in double).
+            TF tu = ut[c] - mulx(pc - ld(p, c-1), dxi_of<TF>(d));
+            TF tv = vt[c] - mulx(pc - ld(p, c-d.icells), dyi_of<TF>(d));
+            TF tw = wt[c] - mulx(pc - ld(p, c-d.ijcells), ld(pr.dzhi, k));
+            u[c] = u[c] + mulx(cbdt, tu); v[c] = v[c] + mulx(cbdt, tv); w[c] = w[c] + mulx(cbdt, tw);
             ut[c] = last ? TF(0) : tu*ca;
             vt[c] = last ? TF(0) : tv*ca;
             wt[c] = last ? TF(0) : tw*ca;
             if (SCAL)
             {
                 const TF ts = st[c];
-                s[c] += cbdt*ts;
+                s[c] = s[c] + mulx(cbdt, ts);
                 st[c] = last ? TF(0) : ts*ca;
             }
         }
@@ -699,9 +701,9 @@ namespace mhh
                 val = fabs(div);
             }
         }
-        // Block max, then one atomic per block.
+        // Block max (NaN kept), then one atomic per block.
         for (int o=16; o>0; o>>=1)
-            val = fmax(val, __shfl_xor_sync(0xffffffffu, val, o));
+            val = max_nan(val, __shfl_xor_sync(0xffffffffu, val, o));
         __shared__ RT sm[8];
         const int lane = (threadIdx.x + threadIdx.y*blockDim.x) & 31;
         const int warp = (threadIdx.x + threadIdx.y*blockDim.x) >> 5;
@@ -711,7 +713,7 @@ namespace mhh
         {
             val = lane < (int)(blockDim.x*blockDim.y/32) ? sm[lane] : RT(0);
             for (int o=16; o>0; o>>=1)
-                val = fmax(val, __shfl_xor_sync(0xffffffffu, val, o));
+                val = max_nan(val, __shfl_xor_sync(0xffffffffu, val, o));
             if (lane == 0) atomic_max_nonneg(out, double(val));
         }
     }

@@ -15,6 +15,8 @@ namespace mhh_host
 {
     void check(int rc, const char* what)
     {
+        if (rc == MHH_ERR_NONFINITE)
+            throw Nonfinite_error(std::string(what) + ": " + mhh_last_error());
         if (rc != MHH_OK)
             throw std::runtime_error(std::string(what) + ": " + mhh_last_error());
     }
@@ -730,6 +732,8 @@ namespace mhh_host
         idt = to_itime(dt); idtmax = to_itime(dtmax); idtlim = idt;
         const int iotimeprec = in.get_item<int>("time", "iotimeprec", "", 0);
         iiotimeprec = to_itime(std::pow(10., iotimeprec));
+        outputiter = in.get_item<int>("time", "outputiter", "", 20);
+        if (outputiter < 0) throw std::runtime_error("outputiter must be >= 0");
     }
 
     template<typename TF>
@@ -894,10 +898,24 @@ namespace mhh_host
     }
 
     template<typename TF>
+    void Model<TF>::check_status()
+    {
+        if (!timeloop->do_check()) return;
+        boundary->set_prognostic_cyclic_bcs(stream);
+        mhh_fields f = fields->dev();
+        double cfl = 0.;
+        const int rc = mhh_advec_get_cfl(grid->ctx(), advec->get_switch(), &f, timeloop->get_dt(), &cfl, stream);
+        if (rc == MHH_ERR_NONFINITE || (rc == MHH_OK && !(cfl >= 0. && cfl < 10.)))
+            throw Nonfinite_error("Simulation has non-finite numbers");
+        check(rc, "get_cfl");
+    }
+
+    template<typename TF>
     void Model<TF>::run_substeps(int n, bool fused)
     {
         for (int q=0; q<n; ++q)
         {
+            check_status();
             if (fused) substep_fused();
             else substep_modules();
         }
@@ -1154,6 +1172,7 @@ namespace
     int guard(F&& f)
     {
         try { f(); return MHH_OK; }
+        catch (mhh_host::Nonfinite_error& e) { g_model_error = e.what(); return MHH_ERR_NONFINITE; }
         catch (std::exception& e) { g_model_error = e.what(); return MHH_ERR_ARG; }
     }
 }

@@ -37,6 +37,14 @@ namespace mhh_host
 
     void check(int rc, const char* what);
 
+    // A run that has produced non-finite numbers (a reduction returned NaN or
+    // inf, or the status check found the CFL number out of range).  The C
+    // entry points return MHH_ERR_NONFINITE for it.
+    struct Nonfinite_error : std::runtime_error
+    {
+        using std::runtime_error::runtime_error;
+    };
+
     template<typename TF> class Grid;
     template<typename TF> class Fields;
 
@@ -291,6 +299,9 @@ namespace mhh_host
             void set_time_step_limit(unsigned long lim) { idtlim = std::min(idtlim, lim); }
             void set_time_step();
             bool in_substep() const { return substep > 0; }
+            // src/timeloop.cxx:179-188: status every outputiter iterations at
+            // the start of a step (every substep with outputiter = 0).
+            bool do_check() const { return outputiter == 0 || (iteration % outputiter == 0 && !in_substep()); }
             void step_time();
             double get_dt() const { return dt; }
             unsigned long get_idt() const { return idt; }
@@ -309,7 +320,7 @@ namespace mhh_host
             bool adaptivestep;
             double dt, dtmax, time;
             unsigned long itime, idt, idtmax, idtlim, iiotimeprec;
-            int substep, iteration;
+            int substep, iteration, outputiter;
     };
 
     // ---- Model, src/model.cxx:327-581 -------------------------------------
@@ -354,6 +365,11 @@ namespace mhh_host
             const std::string& ini() const { return ini_text; }
             const std::vector<double>& levels() const { return z_full; }
             cudaStream_t stream = 0;
+            // The status check of src/model.cxx:842-872 (when the time loop's
+            // do_check is due): the CFL number of the current fields; NaN, inf
+            // or a value outside [0, 10) throws Nonfinite_error ("Simulation
+            // has non-finite numbers").  Synchronises the stream.
+            void check_status();
         private:
             void set_time_step();
             void substep_modules();

@@ -371,6 +371,14 @@ template<> Thermo_type Thermo<TF>::get_switch() { return swthermo; }
 // FFT: the serial branch of src/fft.cxx:337-452 (x transforms of all rows,
 // then y transforms with stride iblock; inverse y then /jtot, inverse x then
 // /itot into tmp1), with the oracle's halfcomplex transforms in place of FFTW.
+//
+// The inverse evaluates the mean mode (kx = ky = 0) of each level apart: the
+// mode is set aside and zeroed, the other modes are transformed, and the
+// level's mean (X_00/jtot)/itot is added to every point at the end.  That is
+// the same unnormalised inverse transform; it only keeps the large
+// hydrostatic part of the pressure out of the butterflies, whose round-off
+// (eps times the mean, at every point) would otherwise depend on the order
+// of the radix passes.  FFTW's own rounding is not reproducible here anyway.
 // ---------------------------------------------------------------------------
 template<> FFT<TF>::FFT(Master& m, Grid<TF>& g) : master(m), grid(g), transpose(m, g)
 {
@@ -396,11 +404,18 @@ void FFT<TF>::exec_backward(TF* const restrict data, TF* const restrict tmp1)
 {
     auto& gd = grid.get_grid_data();
     const long n = (long)gd.itot*gd.jtot*gd.ktot;
+    const long nlev = (long)gd.iblock*gd.jtot;
+    std::vector<TF> mean(gd.kblock);
     for (int k=0; k<gd.kblock; ++k)
-        orcfft_hc2r(gd.jtot, gd.iblock, data + (long)k*gd.iblock*gd.jtot, gd.iblock, 1);
+    {
+        mean[k] = (data[k*nlev] / gd.jtot) / gd.itot;
+        data[k*nlev] = TF(0);
+    }
+    for (int k=0; k<gd.kblock; ++k)
+        orcfft_hc2r(gd.jtot, gd.iblock, data + (long)k*nlev, gd.iblock, 1);
     for (long q=0; q<n; ++q) data[q] = data[q] / gd.jtot;
     orcfft_hc2r(gd.itot, gd.jmax*gd.kblock, data, 1, gd.itot);
-    for (long q=0; q<n; ++q) tmp1[q] = data[q] / gd.itot;
+    for (long q=0; q<n; ++q) tmp1[q] = data[q] / gd.itot + mean[q / nlev];
 }
 
 // ---------------------------------------------------------------------------

@@ -70,6 +70,41 @@ def test_noalloc_divergence_matches(mhh, precision):
     assert abs(got - ref) <= TOL * scale(case, m), (got, ref)
 
 
+def test_noalloc_divergence_at_the_size_limit(mhh):
+    """jtot*ktot = 262144 row maxima exactly (the largest accepted use of
+    the scratch array, with the row index spanning the whole grid of
+    blocks), two calls in a row, against mhh_pres_2_get_divergence."""
+    case = cases.drycbl(8, 512, 512, 800., 51200., 5120., seed=43, noise_z=200.)
+    m = mhh.Model(case, precision=mhh.FP64)
+    rng = np.random.default_rng(8)
+    shape = m.get("u").shape
+    for call in range(2):
+        for n in ("u", "v", "w"):
+            m.set(n, rng.standard_normal(shape))
+        ref, got = both(mhh, m)
+        assert ref > 0
+        assert abs(got - ref) <= TOL * ref, (call, got, ref)
+    m.close()
+
+
+@pytest.mark.parametrize("precision", [64, 32], ids=["fp64", "fp32"])
+def test_noalloc_divergence_reports_nan(mhh, precision):
+    """One NaN in u gives MHH_ERR_NONFINITE from both divergence entry
+    points (a maximum that dropped the NaN would report a finite value)."""
+    kern, _ = mhh.load()
+    case = cases.drycbl(32, 24, 16, 3200., 2400., 1600., seed=44, noise_z=400.)
+    m = mhh.Model(case, precision=precision)
+    u = m.get("u")
+    u[5, 10, 11] = np.nan
+    m.set("u", u)
+    fl, _ = m.device_fields()
+    out = ctypes.c_double()
+    assert kern.mhh_pres_2_get_divergence(m.ctx(), ctypes.byref(fl), ctypes.byref(out), None) == mhh.ERR_NONFINITE
+    assert kern.mhh_pres_2_get_divergence_noalloc(m.ctx(), ctypes.byref(fl), ctypes.byref(out), None) == mhh.ERR_NONFINITE
+    assert np.isnan(out.value)
+    m.close()
+
+
 def test_noalloc_divergence_rejects_large_grid(mhh):
     """jtot*ktot above the 262144 row maxima of the scratch array is an
     argument error (no launch, no allocation)."""
