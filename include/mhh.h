@@ -252,6 +252,19 @@ int mhh_force_dpdx_exec(mhh_ctx* ctx, const mhh_fields* f, double dpdx, cudaStre
 /* Pressure                                                                */
 /* ---------------------------------------------------------------------- */
 
+/* Storage offset of the scalar (potential temperature).  FP32 contexts with
+   thermodynamics store theta - thref0 (the Boussinesq reference, so that the
+   float keeps 1e-8 K of a boundary-layer fluctuation instead of 3e-5 K of
+   300 K); FP64 contexts store theta itself (offset 0).  The 3-D scalar field
+   and its boundary values passed to the entry points are in these storage
+   units; profiles passed by name (mhh_buffer_set_profile) are physical.  No
+   counterpart in the reference (its fields hold theta). */
+int mhh_ctx_scalar_offset(const mhh_ctx* ctx, double* offset);
+/* Adds delta to every cell (ghost cells included) of a 3-D field in the
+   field precision; used to move the scalar between physical and storage
+   units on the device. */
+int mhh_field_shift(mhh_ctx* ctx, void* field, double delta, cudaStream_t stream);
+
 /* Pres_2<TF>::exec (src/pres_2.cxx:65-94): divergence of the predicted
    velocity, x/y real FFTs (hand-written, no cuFFT), tridiagonal solve in z in
    double, inverse FFTs and the pressure gradient into ut, vt, wt. */

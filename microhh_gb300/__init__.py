@@ -192,6 +192,8 @@ def load():
     _declare(host, "mhh_server_destroy", I, [P])
     _declare(kern, "mhh_ctx_set_option", I, [P, ctypes.c_char_p, I])
     _declare(kern, "mhh_stats_profile", I, [P, P, dp, dp, S])
+    _declare(kern, "mhh_ctx_scalar_offset", I, [P, dp])
+    _declare(kern, "mhh_field_shift", I, [P, P, ctypes.c_double, S])
     _declare(kern, "mhh_ctx_device_bytes", I, [P, ctypes.POINTER(ctypes.c_size_t)])
     _declare(kern, "mhh_launch_count_add", I, [ctypes.c_longlong])
     _kern, _host = kern, host
@@ -377,7 +379,16 @@ class Model:
         mean = np.empty(self.grid.kcells)
         var = np.empty(self.grid.kcells)
         check(self.kern.mhh_stats_profile(self.ctx(), ptr, _dptr(mean), _dptr(var), None), "stats_profile")
+        if name == "th":
+            mean += self.scalar_offset()
         return mean, var
+
+    def scalar_offset(self):
+        """The offset the scalar th is stored with on the device (thref0 in
+        FP32 contexts with thermodynamics, else 0); host values are physical."""
+        off = ctypes.c_double()
+        check(self.kern.mhh_ctx_scalar_offset(self.ctx(), ctypes.byref(off)), "scalar_offset")
+        return off.value
 
     def device_fields(self):
         f, b = Fields(), BcFields()

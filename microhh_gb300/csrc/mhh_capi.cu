@@ -102,6 +102,14 @@ namespace mhh
         return kc;
     }
 
+    // a += delta over a whole 3-D field (mhh_field_shift).
+    template<typename TF>
+    __global__ void k_shift(TF* __restrict__ a, long long n, TF delta)
+    {
+        for (long long q = blockIdx.x*(long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x*blockDim.x)
+            a[q] += delta;
+    }
+
     template<typename TF>
     __global__ void k_pres_out(Dims d, Prof<TF> pr, const TF* __restrict__ p,
                                TF* __restrict__ ut, TF* __restrict__ vt, TF* __restrict__ wt)
@@ -128,10 +136,13 @@ struct mhh_ctx
     mhh_physics phys;
 
     // Host profiles (double), device profiles (one precision).
-    std::vector<double> h[12];
-    void* dprof[12];
+    std::vector<double> h[14];
+    void* dprof[14];
     Prof<double> pd;
     Prof<float> pf;
+    // Storage offset of the scalar theta: FP32 contexts with thermodynamics
+    // store theta - thref0 (0 elsewhere).
+    double th0;
 
     PresWork pw;
     SurfWork sw;
@@ -164,9 +175,9 @@ namespace mhh
 
 namespace
 {
-    enum { P_Z, P_ZH, P_DZ, P_DZH, P_DZI, P_DZHI, P_RHO, P_RHOH, P_TH, P_THH, P_ZF, P_ZFH };
-    const char* prof_names[12] = {"z", "zh", "dz", "dzh", "dzi", "dzhi", "rhoref", "rhorefh", "thref", "threfh",
-                                  "zfac", "zfach"};
+    enum { P_Z, P_ZH, P_DZ, P_DZH, P_DZI, P_DZHI, P_RHO, P_RHOH, P_TH, P_THH, P_ZF, P_ZFH, P_THB, P_THBH, NPROF };
+    const char* prof_names[NPROF] = {"z", "zh", "dz", "dzh", "dzi", "dzhi", "rhoref", "rhorefh", "thref", "threfh",
+                                     "zfac", "zfach", "thb", "thbh"};
 
     int fail(int code, const char* msg) { mhh_set_last_error(msg); return code; }
 
@@ -217,6 +228,13 @@ namespace
             c->h[P_ZF][k] = dzi[k]/c->h[P_RHO][k];
             c->h[P_ZFH][k] = dzhi[k]/c->h[P_RHOH][k];
         }
+        // Reference profile in the scalar's storage units: the buoyancy
+        // g/thref (theta - thref) becomes g/thref (theta_stored - thb).
+        for (int k=0; k<kc; ++k)
+        {
+            c->h[P_THB][k] = c->h[P_TH][k] - c->th0;
+            c->h[P_THBH][k] = c->h[P_THH][k] - c->th0;
+        }
     }
 
     // Squared Smagorinsky mixing length per level: src/diff_smag2.cxx:176-180
@@ -247,7 +265,7 @@ namespace
     {
         const int kc = c->d.kcells;
         std::vector<TF> tmp(kc);
-        for (int q=0; q<12; ++q)
+        for (int q=0; q<NPROF; ++q)
         {
             if (cudaMallocAsync(&c->dprof[q], sizeof(TF)*kc, c->setup) != cudaSuccess)
                 return fail(MHH_ERR_CUDA, "cudaMallocAsync profiles");
@@ -262,6 +280,7 @@ namespace
         p.rhoref = (const TF*)c->dprof[P_RHO]; p.rhorefh = (const TF*)c->dprof[P_RHOH];
         p.thref = (const TF*)c->dprof[P_TH]; p.threfh = (const TF*)c->dprof[P_THH];
         p.zfac = (const TF*)c->dprof[P_ZF]; p.zfach = (const TF*)c->dprof[P_ZFH];
+        p.thb = (const TF*)c->dprof[P_THB]; p.thbh = (const TF*)c->dprof[P_THBH];
         if constexpr (sizeof(TF) == 8) c->pd = *reinterpret_cast<Prof<double>*>(&p);
         else c->pf = *reinterpret_cast<Prof<float>*>(&p);
         return MHH_OK;
@@ -768,6 +787,11 @@ int mhh_ctx_create(const mhh_grid_desc* desc, const double* z, int precision, co
     std::memset(&c->sw, 0, sizeof(c->sw));
     c->prec = precision;
     c->phys = *phys;
+    // Theta near 300 K keeps about 3e-5 K in float; stored as its difference
+    // from the Boussinesq reference it keeps 1e-8 K in the boundary layer.
+    // The buoyancy of the dry thermodynamics only needs theta - thref, so
+    // the kernels see the offset through the thb profiles alone.
+    c->th0 = (precision == MHH_FP32 && phys->thermo) ? phys->thref0 : 0.;
     Dims& d = c->d;
     d.itot = desc->itot; d.jtot = desc->jtot; d.ktot = desc->ktot;
     d.igc = desc->igc; d.jgc = desc->jgc; d.kgc = desc->kgc;
@@ -826,6 +850,8 @@ int mhh_ctx_create(const mhh_grid_desc* desc, const double* z, int precision, co
     c->sw.zsl = c->h[P_Z][d.kstart];
     c->sw.thref_s = c->h[P_TH][d.kstart];
     c->sw.threfh_s = c->h[P_THH][d.kstart];
+    c->sw.thb_s = c->h[P_THB][d.kstart];
+    c->sw.thbh_s = c->h[P_THBH][d.kstart];
     // Diff_2 multiplier, src/diff_2.cxx:143-155.
     {
         const double viscmax = phys->thermo ? std::max(phys->visc, phys->svisc) : phys->visc;
@@ -864,7 +890,7 @@ int mhh_ctx_estimate_bytes(const mhh_grid_desc* g, int precision, size_t* bytes)
     const double n = double(g->itot)*g->jtot*g->ktot;
     const double groups = double(g->itot/2 + 1)*(g->jtot/2 + 1)*g->ktot;
     double b = 0.;
-    b += 12.*kcells*tf;                         // profiles
+    b += 14.*kcells*tf;                         // profiles
     b += n*tf + n*8. + g->ktot*8.;              // packed pressure + work + level means
     b += groups*(8. + 8. + 8. + 8. + 4. + 8.); // elimination tables
     b += 2.*(g->itot + g->jtot)*(16. + 8.);    // twiddles
@@ -911,6 +937,24 @@ int mhh_ctx_get_profile(const mhh_ctx* c, const char* name, double* out)
             return MHH_OK;
         }
     return fail(MHH_ERR_ARG, "unknown profile");
+}
+
+int mhh_ctx_scalar_offset(const mhh_ctx* c, double* offset)
+{
+    if (!c || !offset) return fail(MHH_ERR_ARG, "NULL argument");
+    *offset = c->th0;
+    return MHH_OK;
+}
+
+int mhh_field_shift(mhh_ctx* c, void* field, double delta, cudaStream_t s)
+{
+    if (!c || !field) return fail(MHH_ERR_ARG, "NULL argument");
+    const long long n = c->d.ncells;
+    const unsigned nb = (unsigned)std::min<long long>((n + 255)/256, 8LL*152);
+    if (c->prec == MHH_FP64) k_shift<double><<<nb, 256, 0, s>>>((double*)field, n, delta);
+    else k_shift<float><<<nb, 256, 0, s>>>((float*)field, n, float(delta));
+    count_launch();
+    return check_cuda("field_shift");
 }
 
 int mhh_boundary_cyclic(mhh_ctx* c, void* data, int edges, cudaStream_t s)
@@ -1237,7 +1281,9 @@ int mhh_buffer_set_profile(mhh_ctx* c, const char* name, const double* prof)
     else if (!std::strcmp(name, "th")) q = 4;
     if (q < 0) return fail(MHH_ERR_ARG, "buffer profiles are u, v and th");
     const int kc = c->d.kcells;
-    std::copy(prof, prof + kc, c->hbuf.begin() + (size_t)q*kc);
+    // Profiles are physical values; theta's is stored with the scalar's offset.
+    const double off = q == 4 ? c->th0 : 0.;
+    for (int k=0; k<kc; ++k) c->hbuf[(size_t)q*kc + k] = prof[k] - off;
     c->buf_set |= 1 << (q - 2);
     return upload_buffer(c);
 }

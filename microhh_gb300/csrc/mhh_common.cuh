@@ -39,6 +39,9 @@ namespace mhh
         const TF *rhoref, *rhorefh;
         const TF *thref, *threfh;
         const TF *zfac, *zfach;     // dzi/rhoref and dzhi/rhorefh
+        // The reference potential temperature in the units the scalar is
+        // stored in (thref minus the context's storage offset of theta).
+        const TF *thb, *thbh;
     };
 
     __host__ __device__ inline long long ijk(const Dims& d, int i, int j, int k)

@@ -197,6 +197,7 @@ namespace mhh
         float *mlen2f;   // the same in float
         double zsl;      // height of the first full level
         double thref_s, threfh_s;  // reference potential temperature at kstart (full, half)
+        double thb_s, thbh_s;      // the same in the scalar's storage units
     };
 
     template<typename TF> void launch_surface(const Dims& d, const Prof<TF>& pr, const SurfWork& sw,

@@ -325,7 +325,7 @@ namespace mhh
         if (k > d.kstart)
         {
             TF t = TF(0);
-            if (BUOY) t += TF(GRAV)/ld(pr.threfh, k)*(i2(ld(a.s, c-d.ijcells), ld(a.s, c)) - ld(pr.threfh, k));
+            if (BUOY) t += TF(GRAV)/ld(pr.threfh, k)*(i2(ld(a.s, c-d.ijcells), ld(a.s, c)) - ld(pr.thbh, k));
             if (A2I5) t += advec_2i5_w(d, pr, u, v, w, c, k, dxi, dyi);
             else if (ADV == MHH_ADVEC_2) t += advec_2_w(d, pr, u, v, w, c, k, dxi, dyi);
             if (DIF == MHH_DIFF_SMAG2) t += diff_smag2_w(d, pr, u, v, w, a.evisc, c, k, dxi, dyi, a.visc);

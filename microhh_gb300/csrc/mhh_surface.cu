@@ -113,7 +113,7 @@ namespace mhh
     template<typename TF>
     __global__ void k_stability(Dims d, SurfWork sw, const TF* __restrict__ s, const TF* __restrict__ s_bot,
                                 const TF* __restrict__ s_flux, double zsl, double z0m, double thref_s, double threfh_s,
-                                int thermo, int thermo_bc)
+                                double thb_s, double thbh_s, int thermo, int thermo_bc)
     {
         const int n = blockIdx.x*blockDim.x + threadIdx.x;
         if (n >= d.ijcells) return;
@@ -131,8 +131,9 @@ namespace mhh
         }
         else
         {
-            const CT b = CT(GRAV)/CT(thref_s)*(CT(s[n + (long long)d.kstart*d.ijcells]) - CT(thref_s));
-            const CT bbot = CT(GRAV)/CT(threfh_s)*(CT(s_bot[n]) - CT(threfh_s));
+            // theta - thref in the scalar's storage units (thb = thref - offset).
+            const CT b = CT(GRAV)/CT(thref_s)*(CT(s[n + (long long)d.kstart*d.ijcells]) - CT(thb_s));
+            const CT bbot = CT(GRAV)/CT(threfh_s)*(CT(s_bot[n]) - CT(thbh_s));
             const CT db_ref = CT(GRAV)/CT(thref_s)*(CT(thref_s) - CT(threfh_s));
             const CT db = b - bbot + db_ref;
             const float Ri = (float)(CT(KAPPA)*db*zs/(du*du));
@@ -240,7 +241,8 @@ namespace mhh
         const int nb = (d.ijcells + 255)/256;
         k_dutot<TF><<<g2, b2, 0, st>>>(d, u, v, u_bot, v_bot, sw.dutot);
         launch_cyclic2d<double>(sw.dutot, d, st);
-        k_stability<TF><<<nb, 256, 0, st>>>(d, sw, s, s_bot, s_flux, zsl, z0m, thref_s, threfh_s, thermo, thermo_bc);
+        k_stability<TF><<<nb, 256, 0, st>>>(d, sw, s, s_bot, s_flux, zsl, z0m, thref_s, threfh_s, sw.thb_s, sw.thbh_s,
+                                            thermo, thermo_bc);
         k_surfm<TF><<<g2, b2, 0, st>>>(d, sw, u, v, u_bot, v_bot, u_flux, v_flux, zsl, z0m);
         launch_cyclic2d<TF>(u_flux, d, st);
         launch_cyclic2d<TF>(v_flux, d, st);

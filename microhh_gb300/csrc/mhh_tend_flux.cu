@@ -212,7 +212,7 @@ namespace mhh
             prof[2*PLEV + q] = pr.rhoref[l];
             prof[3*PLEV + q] = pr.dzi[l];
             prof[4*PLEV + q] = TF(GRAV)/pr.threfh[l];
-            prof[7*PLEV + q] = pr.threfh[l];
+            prof[7*PLEV + q] = pr.thbh[l];
             prof[5*PLEV + q] = pr.zfac[l];
             prof[6*PLEV + q] = pr.zfach[l];
         }

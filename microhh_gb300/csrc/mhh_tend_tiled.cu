@@ -236,7 +236,7 @@ namespace mhh
                 {
                     const TF rhom = pr.rhoref[k-1];
                     TF t = TF(0);
-                    if (BUOY) t += TF(GRAV)/pr.threfh[k]*(i2(qs[2], qs[3]) - pr.threfh[k]);
+                    if (BUOY) t += TF(GRAV)/pr.threfh[k]*(i2(qs[2], qs[3]) - pr.thbh[k]);
                     t += hadv(W0, i2(X(Um,1,0), X(U,1,0)), i2(X(Um,0,0), X(U,0,0)),
                                   i2(X(Vm,0,1), X(V,0,1)), i2(X(Vm,0,0), X(V,0,0)));
                     const TF ftop = rho *qflux<4>(qw, i2(qw[3], qw[4]), face_order_w(d, k));

@@ -328,15 +328,27 @@ namespace mhh_host
     }
 
     template<typename TF>
+    double Fields<TF>::offset(const std::string& name) const
+    {
+        if (name != "th") return 0.;
+        double off = 0.;
+        check(mhh_ctx_scalar_offset(grid.ctx(), &off), "scalar_offset");
+        return off;
+    }
+
+    template<typename TF>
     void Fields<TF>::set_from_host(const std::string& name, const double* data)
     {
         Field3d<TF>* f = by_name(name);
         const long long n = grid.get_grid_data().ncells;
-        if (sizeof(TF) == 8)
+        const double off = offset(name);
+        if (sizeof(TF) == 8 && off == 0.)
             cuda_check(cudaMemcpy(f->fld_g, data, sizeof(double)*n, cudaMemcpyHostToDevice), "set field");
         else
         {
-            std::vector<TF> tmp(data, data + n);
+            // The difference is taken in double and rounded once.
+            std::vector<TF> tmp(n);
+            for (long long q=0; q<n; ++q) tmp[q] = TF(data[q] - off);
             cuda_check(cudaMemcpy(f->fld_g, tmp.data(), sizeof(TF)*n, cudaMemcpyHostToDevice), "set field");
         }
     }
@@ -346,13 +358,14 @@ namespace mhh_host
     {
         Field3d<TF>* f = by_name(name);
         const long long n = grid.get_grid_data().ncells;
-        if (sizeof(TF) == 8)
+        const double off = offset(name);
+        if (sizeof(TF) == 8 && off == 0.)
             cuda_check(cudaMemcpy(data, f->fld_g, sizeof(double)*n, cudaMemcpyDeviceToHost), "get field");
         else
         {
             std::vector<TF> tmp(n);
             cuda_check(cudaMemcpy(tmp.data(), f->fld_g, sizeof(TF)*n, cudaMemcpyDeviceToHost), "get field");
-            std::copy(tmp.begin(), tmp.end(), data);
+            for (long long q=0; q<n; ++q) data[q] = double(tmp[q]) + off;
         }
     }
 
@@ -362,14 +375,26 @@ namespace mhh_host
         Field3d<TF>* f = by_name(name);
         cuda_check(cudaMemcpyAsync(f->fld_g, data, sizeof(TF)*grid.get_grid_data().ncells, cudaMemcpyHostToDevice, s),
                    "set field");
+        const double off = offset(name);
+        if (off != 0.) check(mhh_field_shift(grid.ctx(), f->fld_g, -off, s), "field_shift");
     }
 
     template<typename TF>
     void Fields<TF>::get_native(const std::string& name, void* data, cudaStream_t s) const
     {
         Field3d<TF>* f = by_name(name);
-        cuda_check(cudaMemcpyAsync(data, f->fld_g, sizeof(TF)*grid.get_grid_data().ncells, cudaMemcpyDeviceToHost, s),
-                   "get field");
+        const long long n = grid.get_grid_data().ncells;
+        cuda_check(cudaMemcpyAsync(data, f->fld_g, sizeof(TF)*n, cudaMemcpyDeviceToHost, s), "get field");
+        const double off = offset(name);
+        if (off != 0.)
+        {
+            // Native values are physical: the offset is added on the host,
+            // rounded to the field precision.
+            cuda_check(cudaStreamSynchronize(s), "get field");
+            TF* out = static_cast<TF*>(data);
+            const TF o = TF(off);
+            for (long long q=0; q<n; ++q) out[q] += o;
+        }
     }
 
     // ---------------------------------------------------------------------
@@ -416,8 +441,13 @@ namespace mhh_host
         if (fields.sp.count("th"))
         {
             auto& s = *fields.sp.at("th");
-            check(mhh_boundary_set_bc(c, s.fld_bot_g, s.grad_bot_g, s.flux_bot_g, sbcbot, sbot, s.visc, sfg, 0), "set_bc");
-            check(mhh_boundary_set_bc(c, s.fld_top_g, s.grad_top_g, s.flux_top_g, sbctop, stop, s.visc, sfg, 0), "set_bc");
+            // A Dirichlet value is a temperature, stored with the scalar's
+            // offset; gradients and fluxes are unchanged by it.
+            const double off = fields.offset("th");
+            const double vb = sbcbot == MHH_BC_DIRICHLET ? sbot - off : sbot;
+            const double vt = sbctop == MHH_BC_DIRICHLET ? stop - off : stop;
+            check(mhh_boundary_set_bc(c, s.fld_bot_g, s.grad_bot_g, s.flux_bot_g, sbcbot, vb, s.visc, sfg, 0), "set_bc");
+            check(mhh_boundary_set_bc(c, s.fld_top_g, s.grad_top_g, s.flux_top_g, sbctop, vt, s.visc, sfg, 0), "set_bc");
         }
         if (swboundary == "surface")
         {
@@ -997,16 +1027,35 @@ namespace mhh_host
         for (const auto& n : names)
         {
             fields->get_to_host(n, full.data());
-            const std::string path = restart_name(dir, n, iotime);
-            FILE* f = create_exclusive(path);
-            std::vector<TF> row(g.itot);
-            for (int k=g.kstart; k<g.kend; ++k)
-                for (int j=g.jstart; j<g.jend; ++j)
-                {
-                    for (int i=0; i<g.itot; ++i) row[i] = TF(full[g.istart + i + (size_t)j*g.icells + (size_t)k*g.ijcells]);
-                    write_all(f, row.data(), row.size(), path);
-                }
-            std::fclose(f);
+            {
+                const std::string path = restart_name(dir, n, iotime);
+                FILE* f = create_exclusive(path);
+                std::vector<TF> row(g.itot);
+                for (int k=g.kstart; k<g.kend; ++k)
+                    for (int j=g.jstart; j<g.jend; ++j)
+                    {
+                        for (int i=0; i<g.itot; ++i) row[i] = TF(full[g.istart + i + (size_t)j*g.icells + (size_t)k*g.ijcells]);
+                        write_all(f, row.data(), row.size(), path);
+                    }
+                std::fclose(f);
+            }
+            // The reference's file holds the physical field; a scalar stored
+            // with an offset also gets <name>_stored.%07d with the stored
+            // values as they are on the device (a physical value in double
+            // cannot hold every bit of a small stored anomaly), so that a
+            // restart continues bit for bit.
+            if (fields->offset(n) != 0.)
+            {
+                std::vector<TF> raw(g.ncells);
+                cuda_check(cudaMemcpy(raw.data(), fields->by_name(n)->fld_g, sizeof(TF)*g.ncells, cudaMemcpyDeviceToHost),
+                           "copy");
+                const std::string path = restart_name(dir, n + "_stored", iotime);
+                FILE* f = create_exclusive(path);
+                for (int k=g.kstart; k<g.kend; ++k)
+                    for (int j=g.jstart; j<g.jend; ++j)
+                        write_all(f, raw.data() + g.istart + (size_t)j*g.icells + (size_t)k*g.ijcells, (size_t)g.itot, path);
+                std::fclose(f);
+            }
         }
         // The integer time.
         {
@@ -1068,6 +1117,26 @@ namespace mhh_host
         std::vector<double> full(g.ncells, 0.);
         for (const auto& n : names)
         {
+            // The stored values where this implementation wrote them (exact),
+            // else the reference's file of physical values.
+            if (fields->offset(n) != 0.)
+            {
+                const std::string stored = restart_name(dir, n + "_stored", iotime);
+                if (FILE* t = std::fopen(stored.c_str(), "rb"))
+                {
+                    std::fclose(t);
+                    read_all(stored, buf.data(), nint);
+                    std::vector<TF> raw(g.ncells, TF(0));
+                    for (int k=0; k<g.ktot; ++k)
+                        for (int j=0; j<g.jtot; ++j)
+                            std::copy(buf.data() + (size_t)j*g.itot + (size_t)k*g.itot*g.jtot,
+                                      buf.data() + (size_t)j*g.itot + (size_t)k*g.itot*g.jtot + g.itot,
+                                      raw.data() + g.istart + (size_t)(j + g.jstart)*g.icells + (size_t)(k + g.kstart)*g.ijcells);
+                    cuda_check(cudaMemcpy(fields->by_name(n)->fld_g, raw.data(), sizeof(TF)*g.ncells,
+                                          cudaMemcpyHostToDevice), "copy");
+                    continue;
+                }
+            }
             read_all(restart_name(dir, n, iotime), buf.data(), nint);
             std::fill(full.begin(), full.end(), 0.);
             for (int k=0; k<g.ktot; ++k)

@@ -94,16 +94,21 @@ namespace mhh_host
             std::map<std::string, std::shared_ptr<Field3d<TF>>> mp, mt, sp, st, sd;
             double visc, svisc;
             mhh_fields dev() const;          // device pointers for the C-ABI
+            // Storage offset of field `name` (theta in FP32 contexts), else 0.
+            double offset(const std::string& name) const;
             mhh_bcfields bc() const;
+            // Host copies are physical values; the scalar th is stored on the
+            // device with the context's offset (mhh_ctx_scalar_offset), which
+            // these conversions add or remove.
             void set_from_host(const std::string& name, const double* data);
             void get_to_host(const std::string& name, double* data) const;
             // Host buffers already in the model precision (TF), copied on the
             // given stream (asynchronous for page-locked buffers).
             void set_native(const std::string& name, const void* data, cudaStream_t s);
             void get_native(const std::string& name, void* data, cudaStream_t s) const;
+            Field3d<TF>* by_name(const std::string& name) const;
         private:
             Grid<TF>& grid;
-            Field3d<TF>* by_name(const std::string& name) const;
     };
 
     // ---- Boundary, src/boundary.cxx + src/boundary_surface.cxx -----------
