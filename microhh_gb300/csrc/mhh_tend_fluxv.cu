@@ -96,13 +96,19 @@ namespace mhh
         const float* __restrict__ ev = a.evisc;
 
         // Interleaved-plane copies of this thread: field cf of the points
-        // cp0 + 80 c, i.e. plane rows cpj + 2 c at column cpi.
+        // cp0 + 80 c, i.e. plane rows cpj + 2 c at column cpi.  In a tile
+        // whose halo lies inside the field (all but the last tiles in x and
+        // y) every copy is valid and needs no predicate; the others check
+        // each point.
         const int cf = tid & 3, cp0 = tid >> 2;
         const int cpj = cp0 / VPW, cpi = cp0 - cpj*VPW;
         const int cgi = i0 - VH + cpi, cgj = j0 - VH + cpj;
-        const bool ccol = cgi < d.icells && (cf != 3 || SCAL);
+        const bool full = i0 - VH + VPW <= d.icells && j0 - VH + VPH <= d.jcells;
+        const bool cuse = cf != 3 || SCAL;
         const float* csrc = cf == 0 ? u : cf == 1 ? v : cf == 2 ? w : (SCAL ? s : u);
-        const long long cgo = ccol ? cgi + (long long)cgj*d.icells : 0;
+        const float* cbase = csrc + (cgi < d.icells ? cgi + cgj*d.icells : 0);
+        const int cstep = 2*d.icells;
+        float* cdst = reinterpret_cast<float*>(P) + 4*cp0 + cf;
         // Viscosity-plane copies: points tid and tid + VNTHR.
         int go0, go1;
         bool v0, v1;
@@ -124,22 +130,32 @@ namespace mhh
         {
             if (l > d.kcells - 1) return;
             const int lf = cf == 2 ? l + 1 : l;
-            const bool lok = ccol && lf <= d.kcells - 1;
-            const float* src = csrc + (long long)lf*d.ijcells + cgo;
-            float* dst = reinterpret_cast<float*>(P + slot*VPS) + 4*cp0 + cf;
-            if (cf != 3 || SCAL)
+            // w of the level above the top reads as zero (never used).
+            const bool lok = cuse && lf <= d.kcells - 1;
+            const float* src = cbase + (long long)lf*d.ijcells;
+            float* dst = cdst + slot*4*VPS;
+            float* de = E + slot*VPS;
+            const float* se = ev + (long long)l*d.ijcells;
+            if (full)
             {
                 #pragma unroll
                 for (int c=0; c<VCOPY; ++c)
-                {
-                    const bool ok = lok && cgj + 2*c < d.jcells;
-                    cp_async_el(dst + 4*(VNTHR/4)*c, ok ? src + 2LL*c*d.icells : csrc, ok);
-                }
+                    cp_async_el(dst + 4*(VNTHR/4)*c, lok ? src + c*cstep : csrc, lok);
+                cp_async_el(de + tid, se + go0, true);
+                if (tid < VNEL1) cp_async_el(de + tid + VNTHR, se + go1, true);
             }
-            float* de = E + slot*VPS;
-            const float* se = ev + (long long)l*d.ijcells;
-            cp_async_el(de + tid, v0 ? se + go0 : ev, v0);
-            if (tid < VNEL1) cp_async_el(de + tid + VNTHR, v1 ? se + go1 : ev, v1);
+            else
+            {
+                const bool lc = lok && cgi < d.icells;
+                #pragma unroll
+                for (int c=0; c<VCOPY; ++c)
+                {
+                    const bool ok = lc && cgj + 2*c < d.jcells;
+                    cp_async_el(dst + 4*(VNTHR/4)*c, ok ? src + c*cstep : csrc, ok);
+                }
+                cp_async_el(de + tid, v0 ? se + go0 : ev, v0);
+                if (tid < VNEL1) cp_async_el(de + tid + VNTHR, v1 ? se + go1 : ev, v1);
+            }
         };
 
         const long long col = cell ? (long long)i + (long long)j*d.icells : 0;
