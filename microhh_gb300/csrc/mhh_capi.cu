@@ -629,7 +629,7 @@ int mhh_set_option(const char* name, int value)
     if (!name) return fail(MHH_ERR_ARG, "NULL option");
     if (!std::strcmp(name, "tendency_kernel"))
     {
-        if (value < -1 || value > 3) return fail(MHH_ERR_ARG, "tendency_kernel is -1, 0, 1, 2 or 3");
+        if (value < -1 || value > 2) return fail(MHH_ERR_ARG, "tendency_kernel is -1, 0, 1 or 2");
         set_tendency_variant(value);
         return MHH_OK;
     }
@@ -679,7 +679,7 @@ int mhh_ctx_set_option(mhh_ctx* c, const char* name, int value)
     const bool reset = value == -2;
     if (!std::strcmp(name, "tendency_kernel"))
     {
-        if (!reset && (value < -1 || value > 3)) return fail(MHH_ERR_ARG, "tendency_kernel is -2, -1, 0, 1, 2 or 3");
+        if (!reset && (value < -1 || value > 2)) return fail(MHH_ERR_ARG, "tendency_kernel is -2, -1, 0, 1 or 2");
         c->opt_tend = value;
     }
     else if (!std::strcmp(name, "viscosity_kernel"))

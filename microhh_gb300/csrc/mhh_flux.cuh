@@ -1,5 +1,5 @@
 // mhh_flux.cuh -- device helpers shared by the flux-form tendency kernels
-// (mhh_tend_flux.cu, mhh_tend_fluxv.cu): asynchronous plane copies and the
+// (mhh_tend_flux.cu): asynchronous plane copies and the
 // advective face fluxes of src/advec_2i5.cxx:150-728 (6th-order
 // interpolation with 5th-order upwind dissipation, lower orders next to the
 // walls) and of the flux limiter (include/advec_monotonic.h:28-219).

@@ -91,10 +91,6 @@ namespace mhh
                                                cudaStream_t s);
     template<typename TF> void launch_tendency_les(const Dims& d, const Prof<TF>& pr, const TendArgs<TF>& a,
                                                    bool surf, bool scal, bool buoy, cudaStream_t s);
-    // The same on float fields with the four fields' planes interleaved
-    // (mhh_tend_fluxv.cu).
-    void launch_tendency_fluxv(const Dims& d, const Prof<float>& pr, const TendArgs<float>& a, bool surf, bool scal,
-                               bool buoy, bool lim, int kchunk, cudaStream_t s);
     // lim: the scalar is advected with the flux limiter.
     template<typename TF> void launch_tendency_flux(const Dims& d, const Prof<TF>& pr, const TendArgs<TF>& a,
                                                     bool surf, bool scal, bool buoy, bool lim, int kchunk,

@@ -393,29 +393,19 @@ namespace mhh
                          bool surf, bool scal, bool buoy, bool force, const KernelOpts& o, cudaStream_t s)
     {
         // The LES combination can run in the tiled kernel (mhh_tend_tiled.cu)
-        // or in the flux-form kernels (mhh_tend_flux.cu; for float fields
-        // also with interleaved planes, mhh_tend_fluxv.cu).
-        // Automatic choice (-1): the flux form in both precisions, with
-        // interleaved planes in float (in double it agrees with the per-cell
-        // kernel, which keeps the reference's operation order, to round-off:
-        // both are held to 1e-12 against the reference).  Variant 3 on
-        // double fields runs variant 2.
+        // or in the flux-form kernel (mhh_tend_flux.cu).
+        // Automatic choice (-1): the flux form in both precisions (in double
+        // it agrees with the per-cell kernel, which keeps the reference's
+        // operation order, to round-off: both are held to 1e-12 against the
+        // reference).
         // The limited scalar (adv == ADVEC_2I5_LIM) runs in the flux-form or
         // the per-cell kernel; the tiled kernel hands it to the flux form.
-        const int var = o.tend < 0 ? (sizeof(TF) == 4 ? 3 : 2) : o.tend;
+        const int var = o.tend < 0 ? 2 : o.tend;
         const bool lim = adv == ADVEC_2I5_LIM && scal;
         if (adv == ADVEC_2I5_LIM && !scal) adv = MHH_ADVEC_2I5;
         if (var >= 1 && (adv == MHH_ADVEC_2I5 || lim) && dif == MHH_DIFF_SMAG2 && !force && d.igc >= 3 && d.jgc >= 3)
         {
-            if constexpr (sizeof(TF) == 4)
-            {
-                if (var == 3)
-                {
-                    launch_tendency_fluxv(d, pr, a, surf, scal, buoy, lim, o.tend_kchunk, s);
-                    return;
-                }
-            }
-            if (var >= 2 || lim) launch_tendency_flux<TF>(d, pr, a, surf, scal, buoy, lim, o.tend_kchunk, s);
+            if (var == 2 || lim) launch_tendency_flux<TF>(d, pr, a, surf, scal, buoy, lim, o.tend_kchunk, s);
             else launch_tendency_les<TF>(d, pr, a, surf, scal, buoy, s);
             return;
         }
