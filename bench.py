@@ -358,7 +358,7 @@ def run_form(args):
     from microhh_gb300 import forms
     if args.form == "ensemble":
         r = forms.ensemble_workload(mhh)
-        line = {"metric": "ensemble member-cell RK3 steps/s", "value": r["graphs"], "unit": "cell-steps/s",
+        line = {"metric": "ensemble member-cell RK3 steps/s", "value": max(r["graphs"], r["batched"]), "unit": "cell-steps/s",
                 "n_gpus": 1, "higher_is_better": True, "form": "ensemble", "dtype": "f32 (FP64 z-solve)",
                 "data": "synthetic (seeded dry CBL members)", "config": {"workload": r["workload"]},
                 "detail": r}

@@ -343,6 +343,28 @@ int mhh_substep_begin(mhh_ctx* ctx, const mhh_substep_config* cfg, const mhh_fie
 int mhh_substep_end(mhh_ctx* ctx, const mhh_substep_config* cfg, const mhh_fields* f,
                     const mhh_bcfields* bc, int substep, double dt, cudaStream_t stream);
 
+/* Batched substeps (no counterpart in the reference, which runs one
+   simulation per process): n contexts of one precision -- ensemble members
+   or served jobs, of uneven grid sizes -- advance a fused substep together
+   with one kernel launch per stage over all of them (per group of contexts
+   whose stage runs the same kernel, e.g. one group per FFT length).  Each
+   context keeps its own fields; cfg, f, bc and dt are per context (dt is the
+   fixed full time step).  Every context gets the kernels and parameters of
+   its own mhh_substep_begin/end, so its results are the same bit for bit.
+   mhh_batch_create records the contexts' substeps without running them and
+   allocates the launch tables; call it after one ordinary substep of every
+   context (kernel attributes are set on first use) and outside any stream
+   capture.  A configuration with a kernel that cannot run batched (the
+   buffer layer, the per-cell kernel variants) returns MHH_ERR_UNSUPPORTED.
+   mhh_batch_substep launches substep 0, 1 or 2 of all contexts on the
+   stream; mhh_batch_launches gives its number of launches. */
+typedef struct mhh_batch mhh_batch;
+int mhh_batch_create(int n, mhh_ctx* const* ctx, const mhh_substep_config* cfg, const mhh_fields* f,
+                     const mhh_bcfields* bc, const double* dt, mhh_batch** out);
+int mhh_batch_substep(mhh_batch* b, int substep, cudaStream_t stream);
+int mhh_batch_launches(const mhh_batch* b, int substep, int* nlaunch);
+int mhh_batch_destroy(mhh_batch* b);
+
 #ifdef __cplusplus
 }
 #endif

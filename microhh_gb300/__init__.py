@@ -399,7 +399,7 @@ class Model:
         return self.host.mhh_model_get_ctx(self.h)
 
 
-ENS_SEQUENTIAL, ENS_STREAMS, ENS_GRAPHS = 0, 1, 2
+ENS_SEQUENTIAL, ENS_STREAMS, ENS_GRAPHS, ENS_BATCHED = 0, 1, 2, 3
 SERVE_FIFO, SERVE_CONTINUOUS = 0, 1
 
 

@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "mhh_kernels.cuh"
+#include "mhh_batchable.cuh"
 
 namespace
 {
@@ -1389,6 +1390,194 @@ int mhh_substep_end(mhh_ctx* c, const mhh_substep_config* cfg, const mhh_fields*
     if (c->buf_on && !buffer_ready(c, f)) return fail(MHH_ERR_ARG, "buffer profiles of u, v (and th) not set");
     return c->prec == MHH_FP64 ? substep_end<double>(c, cfg, f, bc, substep, dt, s)
                                : substep_end<float>(c, cfg, f, bc, substep, dt, s);
+}
+
+}
+
+// ---------------------------------------------------------------------------
+// Batched substeps: many contexts, one launch per stage.
+//
+// The plan records, for every context and substep, the launches of
+// mhh_substep_begin/end (launch_body appends them instead of launching,
+// mhh_batchable.cuh).  Stage i of a substep is the i-th launch of every
+// context; equal kernels (the same k_many entry point and block shape) of a
+// stage form one launch over all their contexts, with the contexts' grids
+// laid end to end.  Each context's kernels run with the same parameters and
+// block positions as in its own substep, so the results are the same bit for
+// bit.  The recording runs inside a stream capture on a scratch stream that
+// is then discarded: a launch that cannot be batched (it does not go through
+// launch_body) is caught by the launch count and the plan is refused.
+// ---------------------------------------------------------------------------
+namespace mhh
+{
+    BatchRecorder*& batch_recorder()
+    {
+        thread_local BatchRecorder* r = nullptr;
+        return r;
+    }
+}
+
+struct mhh_batch
+{
+    struct Group
+    {
+        const void* fn;
+        dim3 block;
+        size_t smem;
+        int nmem, nblocks;
+        void* params;          // device: nmem parameter structs
+        int* start;            // device: nmem + 1 block offsets
+        int4* grid;            // device: nmem grids
+    };
+    int n;
+    std::vector<Group> groups[3];
+    std::vector<void*> mem;
+};
+
+namespace
+{
+    void batch_free(mhh_batch* b)
+    {
+        for (void* p : b->mem) cudaFree(p);
+        delete b;
+    }
+
+    // The launches of one substep of context c (nothing runs).
+    int record_substep(mhh_ctx* c, const mhh_substep_config* cfg, const mhh_fields* f, const mhh_bcfields* bc,
+                       int substep, double dt, cudaStream_t scratch, std::vector<mhh::RecordedLaunch>& out)
+    {
+        mhh::BatchRecorder rec;
+        const bool timing = g_timing;
+        g_timing = false;
+        const long long n0 = launch_count();
+        if (cudaStreamBeginCapture(scratch, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+        {
+            g_timing = timing;
+            return fail(MHH_ERR_CUDA, "batch: stream capture");
+        }
+        mhh::batch_recorder() = &rec;
+        int rc = mhh_substep_begin(c, cfg, f, bc, scratch);
+        if (!rc) rc = mhh_substep_end(c, cfg, f, bc, substep, dt, scratch);
+        mhh::batch_recorder() = nullptr;
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(scratch, &g);
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        g_timing = timing;
+        const long long counted = launch_count() - n0;
+        mhh_launch_count_add(-counted);
+        if (rc) return rc;
+        if (counted != (long long)rec.launches.size())
+            return fail(MHH_ERR_UNSUPPORTED, "batch: a kernel of this configuration cannot run batched");
+        out = std::move(rec.launches);
+        return MHH_OK;
+    }
+}
+
+extern "C" {
+
+int mhh_batch_create(int n, mhh_ctx* const* ctx, const mhh_substep_config* cfg, const mhh_fields* f,
+                     const mhh_bcfields* bc, const double* dt, mhh_batch** out)
+{
+    if (n < 1 || !ctx || !cfg || !f || !bc || !dt || !out) return fail(MHH_ERR_ARG, "NULL argument");
+    for (int m=0; m<n; ++m)
+        if (!ctx[m] || ctx[m]->prec != ctx[0]->prec) return fail(MHH_ERR_ARG, "batch: contexts of one precision");
+    cudaStream_t scratch = nullptr;
+    if (cudaStreamCreateWithFlags(&scratch, cudaStreamNonBlocking) != cudaSuccess) return fail(MHH_ERR_CUDA, "stream");
+    mhh_batch* b = new mhh_batch();
+    b->n = n;
+    int rc = MHH_OK;
+    for (int q=0; q<3 && !rc; ++q)
+    {
+        std::vector<std::vector<mhh::RecordedLaunch>> rec(n);
+        for (int m=0; m<n && !rc; ++m)
+            rc = record_substep(ctx[m], &cfg[m], &f[m], &bc[m], q, dt[m], scratch, rec[m]);
+        if (rc) break;
+        const size_t nstage = rec[0].size();
+        for (int m=1; m<n; ++m)
+            if (rec[m].size() != nstage) { rc = fail(MHH_ERR_UNSUPPORTED, "batch: contexts with different stages"); break; }
+        for (size_t st=0; st<nstage && !rc; ++st)
+        {
+            // Contexts of this stage grouped by entry point and block shape.
+            std::vector<int> done(n, 0);
+            for (int m0=0; m0<n && !rc; ++m0)
+            {
+                if (done[m0]) continue;
+                const mhh::RecordedLaunch& L0 = rec[m0][st];
+                std::vector<int> mem;
+                for (int m=m0; m<n; ++m)
+                {
+                    const mhh::RecordedLaunch& L = rec[m][st];
+                    if (!done[m] && L.fn == L0.fn && L.block.x == L0.block.x && L.block.y == L0.block.y
+                        && L.block.z == L0.block.z && L.params.size() == L0.params.size())
+                    { mem.push_back(m); done[m] = 1; }
+                }
+                mhh_batch::Group g{};
+                g.fn = L0.fn; g.block = L0.block; g.nmem = (int)mem.size();
+                const size_t psz = L0.params.size();
+                std::vector<unsigned char> params(psz*mem.size());
+                std::vector<int> start(mem.size() + 1, 0);
+                std::vector<int4> grid(mem.size());
+                long long total = 0;
+                for (size_t q2=0; q2<mem.size(); ++q2)
+                {
+                    const mhh::RecordedLaunch& L = rec[mem[q2]][st];
+                    std::memcpy(params.data() + q2*psz, L.params.data(), psz);
+                    grid[q2] = make_int4((int)L.grid.x, (int)L.grid.y, (int)L.grid.z, 0);
+                    start[q2] = (int)total;
+                    total += (long long)L.grid.x*L.grid.y*L.grid.z;
+                    g.smem = std::max(g.smem, L.smem);
+                }
+                start[mem.size()] = (int)total;
+                if (total <= 0 || total > 0x7fffffffLL) { rc = fail(MHH_ERR_UNSUPPORTED, "batch: grid too large"); break; }
+                g.nblocks = (int)total;
+                if (cudaMalloc(&g.params, params.size()) != cudaSuccess ||
+                    cudaMalloc((void**)&g.start, sizeof(int)*start.size()) != cudaSuccess ||
+                    cudaMalloc((void**)&g.grid, sizeof(int4)*grid.size()) != cudaSuccess)
+                { rc = fail(MHH_ERR_CUDA, "batch: cudaMalloc"); break; }
+                b->mem.push_back(g.params); b->mem.push_back(g.start); b->mem.push_back(g.grid);
+                cudaMemcpy(g.params, params.data(), params.size(), cudaMemcpyHostToDevice);
+                cudaMemcpy(g.start, start.data(), sizeof(int)*start.size(), cudaMemcpyHostToDevice);
+                cudaMemcpy(g.grid, grid.data(), sizeof(int4)*grid.size(), cudaMemcpyHostToDevice);
+                b->groups[q].push_back(g);
+            }
+        }
+    }
+    cudaStreamDestroy(scratch);
+    if (!rc && cudaDeviceSynchronize() != cudaSuccess) rc = fail(MHH_ERR_CUDA, "batch: set-up");
+    if (rc) { batch_free(b); return rc; }
+    *out = b;
+    return MHH_OK;
+}
+
+int mhh_batch_substep(mhh_batch* b, int substep, cudaStream_t s)
+{
+    if (!b || substep < 0 || substep > 2) return fail(MHH_ERR_ARG, "bad argument");
+    for (const auto& g : b->groups[substep])
+    {
+        mhh::BatchMap map{g.start, g.grid, g.nmem};
+        const void* params = g.params;
+        void* args[] = {(void*)&params, (void*)&map};
+        if (cudaLaunchKernel(g.fn, dim3(g.nblocks), g.block, args, g.smem, s) != cudaSuccess)
+            return fail(MHH_ERR_CUDA, "batch: launch");
+    }
+    count_launch((int)b->groups[substep].size());
+    return check_cuda("batch substep");
+}
+
+int mhh_batch_launches(const mhh_batch* b, int substep, int* nlaunch)
+{
+    if (!b || !nlaunch || substep < 0 || substep > 2) return fail(MHH_ERR_ARG, "bad argument");
+    *nlaunch = (int)b->groups[substep].size();
+    return MHH_OK;
+}
+
+int mhh_batch_destroy(mhh_batch* b)
+{
+    if (!b) return MHH_OK;
+    cudaDeviceSynchronize();
+    batch_free(b);
+    return MHH_OK;
 }
 
 }

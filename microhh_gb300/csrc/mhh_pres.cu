@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "mhh_kernels.cuh"
+#include "mhh_batchable.cuh"
 
 namespace mhh
 {
@@ -387,10 +388,18 @@ namespace mhh
     // The float transform with the fused right-hand side keeps five blocks
     // per SM (at most 51 registers): its batched loads need the residency to
     // cover the latency of HBM.
+    template<typename TF> struct FftP { FftPlan pl; TF* data; SeqLayout L; int Prt; TF scale; FftFuse<TF> fz; };
+    template<typename TF, int FUSE> struct FftOcc { static constexpr int v = (FUSE == 1 && sizeof(TF) == 4) ? 5 : 1; };
+
     template<typename TF, bool INV, int NFIX, int PFIX, int FUSE>
-    __global__ void __launch_bounds__(256, (FUSE == 1 && sizeof(TF) == 4) ? 5 : 1)
-    k_fft(FftPlan pl, TF* __restrict__ data, SeqLayout L, int Prt, TF scale, FftFuse<TF> fz)
+    __device__ __forceinline__ void fft_body(const FftP<TF>& A, const VBlock& vb)
     {
+        const FftPlan& pl = A.pl;
+        TF* __restrict__ data = A.data;
+        const SeqLayout& L = A.L;
+        const int Prt = A.Prt;
+        const TF scale = A.scale;
+        const FftFuse<TF>& fz = A.fz;
         using T2 = typename C2<TF>::T;
         extern __shared__ __align__(16) unsigned char smem_raw[];
         const int n = NFIX ? NFIX : pl.n;
@@ -403,7 +412,7 @@ namespace mhh
         T2* buf1 = buf0 + (size_t)P*n + P;
         T2* tws = buf1 + (size_t)P*n + P;  // twiddle table (fixed path)
         const int ns = L.rows ? n : n + 1;  // real-sequence stride in shared memory
-        const long long s0 = (long long)blockIdx.x*2*P;
+        const long long s0 = (long long)vb.x*2*P;
         const int nloc = (int)min((long long)2*P, L.nseq - s0);
 
         if (NFIX)
@@ -638,7 +647,7 @@ namespace mhh
     // Shared memory: two input buffers and one work buffer of P*SS + P
     // complex elements, plus the twiddle table.  Tile t's input buffer also
     // serves as the second stage buffer; the other input buffer receives
-    // tile t + gridDim.x.
+    // tile t + (the number of blocks).
 
     // Complex elements of one buffer of the pipelined kernel: P sequences at
     // stride SS (N for rows, N + 4 for columns) with the swizzle padding, and
@@ -713,10 +722,17 @@ namespace mhh
         return yseq ? TF(-0.5)*(a.x - b.x) : TF(0.5)*(a.y - b.y);
     }
 
+    template<typename TF> struct FftpP { TF* data; SeqLayout L; TF scale; FftFuse<TF> fz; const TF* twt; long long ntiles; };
+
     template<typename TF, bool INV, int N, int P, int FUSE, bool ROWS>
-    __global__ void __launch_bounds__(P == 8 ? 512 : 256)
-    k_fftp(TF* __restrict__ data, SeqLayout L, TF scale, FftFuse<TF> fz, const TF* __restrict__ twt, long long ntiles)
+    __device__ __forceinline__ void fftp_body(const FftpP<TF>& A, const VBlock& vb)
     {
+        TF* __restrict__ data = A.data;
+        const SeqLayout& L = A.L;
+        const TF scale = A.scale;
+        const FftFuse<TF>& fz = A.fz;
+        const TF* __restrict__ twt = A.twt;
+        const long long ntiles = A.ntiles;
         using T2 = typename C2<TF>::T;
         constexpr int NS = ROWS ? N : N + 1;      // real stride of the input view
         constexpr int SS = ROWS ? N : N + 4;      // complex stride of the stages
@@ -761,17 +777,17 @@ namespace mhh
         // after the barriers of the stages.
         __shared__ TileIdx x;
 
-        long long t = blockIdx.x;
+        long long t = vb.x;
         int cur = 0;
         if (t < ntiles) issue(t, bufs);
-        for (; t < ntiles; t += gridDim.x)
+        for (; t < ntiles; t += vb.gx)
         {
             T2* in = cur ? bufs + 2*BUF : bufs;
             asm volatile("cp.async.wait_group 0;\n" ::: "memory");
             __syncthreads();
             // The other input buffer was last read by the previous tile,
             // which every thread has finished (barrier above).
-            if (t + gridDim.x < ntiles) issue(t + gridDim.x, cur ? bufs : bufs + 2*BUF);
+            if (t + vb.gx < ntiles) issue(t + vb.gx, cur ? bufs : bufs + 2*BUF);
             if (FUSE == 2)
             {
                 const long long s0 = t*2*P;
@@ -839,18 +855,20 @@ namespace mhh
         const long long ntiles = (L.nseq + 2*P - 1) / (2*P);
         // Attribute and residency are set once per kernel, outside any stream
         // capture that a later call may be part of.
+        using B = FftpP<TF>;
+        constexpr auto body = fftp_body<TF, INV, N, P, FUSE, ROWS>;
         static const int resident = [&]
         {
-            cudaFuncSetAttribute(k_fftp<TF, INV, N, P, FUSE, ROWS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            set_smem_limit<B, body, NT, 1>(smem);
             int per_sm = 0, dev = 0, sms = 0;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fftp<TF, INV, N, P, FUSE, ROWS>, NT, smem);
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_one<B, body, NT, 1>, NT, smem);
             cudaGetDevice(&dev);
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
             return (per_sm > 0 ? per_sm : 1)*(sms > 0 ? sms : 1);
         }();
         const long long nblk = ntiles < resident ? ntiles : resident;
         const TF* twt = sizeof(TF) == 8 ? reinterpret_cast<const TF*>(pl.tw_d) : reinterpret_cast<const TF*>(pl.tw_f);
-        k_fftp<TF, INV, N, P, FUSE, ROWS><<<(unsigned)nblk, NT, smem, s>>>(data, L, scale, fz, twt, ntiles);
+        launch_body<B, body, NT, 1>(dim3((unsigned)nblk), dim3(NT), smem, s, B{data, L, scale, fz, twt, ntiles});
     }
 
     // Dynamic shared-memory limit of the run-time-plan FFT (two buffers of at
@@ -875,10 +893,8 @@ namespace mhh
     {
         const size_t smem = sizeof(typename C2<TF>::T)*((size_t)2*(PF*NF + PF) + NF);
         const long long nblk = (L.nseq + 2*PF - 1) / (2*PF);
-        static const bool attr = cudaFuncSetAttribute(k_fft<TF, INV, NF, PF, FUSE>,
-            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess;
-        (void)attr;
-        k_fft<TF, INV, NF, PF, FUSE><<<(unsigned)nblk, 256, smem, s>>>(pl, data, L, PF, scale, fz);
+        launch_body<FftP<TF>, fft_body<TF, INV, NF, PF, FUSE>, 256, FftOcc<TF, FUSE>::v>(
+            dim3((unsigned)nblk), dim3(256), smem, s, FftP<TF>{pl, data, L, PF, scale, fz});
     }
 
     template<typename TF, bool INV, int NF>
@@ -933,10 +949,10 @@ namespace mhh
         const int P = pairs_per_block<TF>(n, L.rows != 0);
         const size_t smem = 2*sizeof(typename C2<TF>::T)*((size_t)P*n + P);
         const long long nblk = (L.nseq + 2*P - 1) / (2*P);
-        static const bool attr = cudaFuncSetAttribute(k_fft<TF, INV, 0, 0, FUSE>,
-            cudaFuncAttributeMaxDynamicSharedMemorySize, FFT_GENERIC_SMEM) == cudaSuccess;
-        (void)attr;
-        k_fft<TF, INV, 0, 0, FUSE><<<(unsigned)nblk, 256, smem, s>>>(pl, data, L, P, scale, fz);
+        // The shared memory depends on n: the limit is set to the largest.
+        set_smem_limit<FftP<TF>, fft_body<TF, INV, 0, 0, FUSE>, 256, FftOcc<TF, FUSE>::v>(FFT_GENERIC_SMEM);
+        launch_body<FftP<TF>, fft_body<TF, INV, 0, 0, FUSE>, 256, FftOcc<TF, FUSE>::v>(
+            dim3((unsigned)nblk), dim3(256), smem, s, FftP<TF>{pl, data, L, P, scale, fz});
     }
 
     template<typename TF>
@@ -1125,14 +1141,24 @@ namespace mhh
         return TF(0);
     }
 
-    template<typename TF>
-    __global__ void __launch_bounds__(128)
-    k_tdma(int itot, int jtot, int ktot, int niu, int nju, const double* __restrict__ rtab,
-           const double* __restrict__ wtab, const double* __restrict__ a, const double* __restrict__ dz2,
-           TF* __restrict__ pk, double* __restrict__ work, TF* __restrict__ dcm)
+    template<typename TF> struct TdmaP
     {
-        const int iu = blockIdx.x*blockDim.x + threadIdx.x;
-        const int ju = blockIdx.y;
+        int itot, jtot, ktot, niu, nju;
+        const double *rtab, *wtab, *a, *dz2, *gtab, *htab;
+        const float* stab;
+        const double* stabd;
+        TF* pk; double* work; TF* dcm;
+    };
+
+    template<typename TF>
+    __device__ __forceinline__ void tdma_body(const TdmaP<TF>& A, const VBlock& vb)
+    {
+        const int itot = A.itot, jtot = A.jtot, ktot = A.ktot, niu = A.niu, nju = A.nju;
+        const double* __restrict__ rtab = A.rtab; const double* __restrict__ wtab = A.wtab;
+        const double* __restrict__ a = A.a; const double* __restrict__ dz2 = A.dz2;
+        TF* __restrict__ pk = A.pk; double* __restrict__ work = A.work; TF* __restrict__ dcm = A.dcm;
+        const int iu = vb.x*blockDim.x + threadIdx.x;
+        const int ju = vb.y;
         if (iu >= niu) return;
         const long long stride = (long long)niu*nju;
         const long long base = iu + (long long)ju*niu;
@@ -1253,13 +1279,14 @@ namespace mhh
     // k_tdma_table): in the float form the whole solve costs two FP64 FMAs
     // per cell, the elimination itself staying in double.
     template<typename TF>
-    __global__ void __launch_bounds__(128)
-    k_tdma_scaled(int itot, int jtot, int ktot, int niu, int nju, const double* __restrict__ gtab,
-                  const double* __restrict__ htab, const float* __restrict__ stab, const double* __restrict__ stabd,
-                  TF* __restrict__ pk, double* __restrict__ work, TF* __restrict__ dcm)
+    __device__ __forceinline__ void tdma_scaled_body(const TdmaP<TF>& A, const VBlock& vb)
     {
-        const int iu = blockIdx.x*blockDim.x + threadIdx.x;
-        const int ju = blockIdx.y;
+        const int itot = A.itot, jtot = A.jtot, ktot = A.ktot, niu = A.niu, nju = A.nju;
+        const double* __restrict__ gtab = A.gtab; const double* __restrict__ htab = A.htab;
+        const float* __restrict__ stab = A.stab; const double* __restrict__ stabd = A.stabd;
+        TF* __restrict__ pk = A.pk; double* __restrict__ work = A.work; TF* __restrict__ dcm = A.dcm;
+        const int iu = vb.x*blockDim.x + threadIdx.x;
+        const int ju = vb.y;
         if (iu >= niu) return;
         const long long stride = (long long)niu*nju;
         const long long base = iu + (long long)ju*niu;
@@ -1372,14 +1399,15 @@ namespace mhh
     // the loads of one warp's next levels overlap the FP64 recurrences of
     // the others.
     template<typename TF>
-    __global__ void __launch_bounds__(128, 8)
-    k_tdma_col(int itot, int jtot, int ktot, int niu, int nju, const double* __restrict__ gtab,
-               const double* __restrict__ htab, const float* __restrict__ stab, const double* __restrict__ stabd,
-               TF* __restrict__ pk, double* __restrict__ work, TF* __restrict__ dcm)
+    __device__ __forceinline__ void tdma_col_body(const TdmaP<TF>& A, const VBlock& vb)
     {
-        const int t = blockIdx.x*blockDim.x + threadIdx.x;
+        const int itot = A.itot, jtot = A.jtot, ktot = A.ktot, niu = A.niu, nju = A.nju;
+        const double* __restrict__ gtab = A.gtab; const double* __restrict__ htab = A.htab;
+        const float* __restrict__ stab = A.stab; const double* __restrict__ stabd = A.stabd;
+        TF* __restrict__ pk = A.pk; double* __restrict__ work = A.work; TF* __restrict__ dcm = A.dcm;
+        const int t = vb.x*blockDim.x + threadIdx.x;
         const int iu = t >> 2, q = t & 3;
-        const int ju = blockIdx.y;
+        const int ju = vb.y;
         if (iu >= niu) return;
         const int i1 = (iu == 0 || 2*iu == itot) ? -1 : itot - iu;
         const int j1 = (ju == 0 || 2*ju == jtot) ? -1 : jtot - ju;
@@ -1469,17 +1497,17 @@ namespace mhh
         dim3 grid((pw.niu + 127)/128, pw.nju);
         TF* dcm = static_cast<TF*>(pw.dcm);
         const int v = o.tdma < 0 ? (sizeof(TF) == 4 ? 1 : 0) : o.tdma;
+        const TdmaP<TF> A{d.itot, d.jtot, d.ktot, pw.niu, pw.nju, pw.rtab, pw.wtab, pw.a, pw.dz2, pw.gtab, pw.htab,
+                          pw.stab, pw.stabd, pk, pw.work, dcm};
         if (v == 1)
         {
             dim3 gridc((4*pw.niu + 127)/128, pw.nju);
-            k_tdma_col<TF><<<gridc, 128, 0, s>>>(d.itot, d.jtot, d.ktot, pw.niu, pw.nju, pw.gtab, pw.htab,
-                                                 pw.stab, pw.stabd, pk, pw.work, dcm);
+            launch_body<TdmaP<TF>, tdma_col_body<TF>, 128, 8>(gridc, dim3(128), 0, s, A);
         }
         else if (v == 2)
-            k_tdma_scaled<TF><<<grid, 128, 0, s>>>(d.itot, d.jtot, d.ktot, pw.niu, pw.nju, pw.gtab, pw.htab,
-                                                   pw.stab, pw.stabd, pk, pw.work, dcm);
+            launch_body<TdmaP<TF>, tdma_scaled_body<TF>, 128>(grid, dim3(128), 0, s, A);
         else
-            k_tdma<TF><<<grid, 128, 0, s>>>(d.itot, d.jtot, d.ktot, pw.niu, pw.nju, pw.rtab, pw.wtab, pw.a, pw.dz2, pk, pw.work, dcm);
+            launch_body<TdmaP<TF>, tdma_body<TF>, 128>(grid, dim3(128), 0, s, A);
         count_launch();
     }
 

@@ -5,6 +5,7 @@
 #include <type_traits>
 
 #include "mhh_kernels.cuh"
+#include "mhh_batchable.cuh"
 #include "mhh_stencil.cuh"
 
 namespace mhh
@@ -15,9 +16,14 @@ namespace mhh
     // equals the reference's east-west-then-north-south copy, corners
     // included, and reads interior cells only.
     // ---------------------------------------------------------------------
+    template<typename TF> struct CyclicP { FieldList<TF> fl; Dims d; int edges; };
+
     template<typename TF>
-    __global__ void k_cyclic(FieldList<TF> fl, Dims d, int edges)
+    __device__ __forceinline__ void cyclic_body(const CyclicP<TF>& P, const VBlock& vb)
     {
+        const FieldList<TF>& fl = P.fl;
+        const Dims& d = P.d;
+        const int edges = P.edges;
         const int nghost_i = 2*d.igc, nghost_j = 2*d.jgc;
         // Work items: the ghost columns (all j) and the ghost rows: interior i
         // when the columns are filled too, every i for a north-south-only fill
@@ -27,8 +33,8 @@ namespace mhh
         const long long ncol = (long long)nghost_i*d.jcells;
         const long long nrow = (long long)nghost_j*rowlen;
         const long long nitem = ((edges & 1) ? ncol : 0) + ((edges & 2) ? nrow : 0);
-        const int k = blockIdx.y;
-        for (long long n = blockIdx.x*(long long)blockDim.x + threadIdx.x; n < nitem; n += (long long)gridDim.x*blockDim.x)
+        const int k = vb.y;
+        for (long long n = vb.x*(long long)blockDim.x + threadIdx.x; n < nitem; n += (long long)vb.gx*blockDim.x)
         {
             int i, j;
             long long m = n;
@@ -70,15 +76,19 @@ namespace mhh
         int bx = (int)((nitem + threads - 1) / threads);
         if (bx > 64) bx = 64;
         dim3 grid(bx, d.kcells);
-        k_cyclic<TF><<<grid, threads, 0, s>>>(fl, d, edges);
+        launch_body<CyclicP<TF>, cyclic_body<TF>, 128>(grid, dim3(threads), 0, s, CyclicP<TF>{fl, d, edges});
         count_launch();
     }
 
     // Periodic fill of a 2-D array (icells*jcells).
+    template<typename TF> struct Cyclic2P { TF* a; Dims d; };
+
     template<typename TF>
-    __global__ void k_cyclic2d(TF* a, Dims d)
+    __device__ __forceinline__ void cyclic2d_body(const Cyclic2P<TF>& P, const VBlock& vb)
     {
-        const int n = blockIdx.x*blockDim.x + threadIdx.x;
+        TF* a = P.a;
+        const Dims& d = P.d;
+        const int n = vb.x*blockDim.x + threadIdx.x;
         if (n >= d.ijcells) return;
         const int i = n % d.icells, j = n / d.icells;
         if (i >= d.istart && i < d.iend && j >= d.jstart && j < d.jend) return;
@@ -91,7 +101,7 @@ namespace mhh
     template<typename TF>
     void launch_cyclic2d(TF* a, const Dims& d, cudaStream_t s)
     {
-        k_cyclic2d<TF><<<(d.ijcells + 255)/256, 256, 0, s>>>(a, d);
+        launch_body<Cyclic2P<TF>, cyclic2d_body<TF>, 256>(dim3((d.ijcells + 255)/256), dim3(256), 0, s, Cyclic2P<TF>{a, d});
         count_launch();
     }
 
@@ -118,10 +128,15 @@ namespace mhh
     // ---------------------------------------------------------------------
     // Wall ghost levels, 2nd order, src/boundary.cxx:700-760.
     // ---------------------------------------------------------------------
+    template<typename TF> struct GhostP { GhostList<TF> gl; Dims d; const TF* dzh; };
+
     template<typename TF>
-    __global__ void k_ghost(GhostList<TF> gl, Dims d, const TF* dzh)
+    __device__ __forceinline__ void ghost_body(const GhostP<TF>& P, const VBlock& vb)
     {
-        const int n = blockIdx.x*blockDim.x + threadIdx.x;
+        const GhostList<TF>& gl = P.gl;
+        const Dims& d = P.d;
+        const TF* dzh = P.dzh;
+        const int n = vb.x*blockDim.x + threadIdx.x;
         if (n >= d.ijcells) return;
         const TF dzhb = dzh[d.kstart], dzht = dzh[d.kend];
         for (int f=0; f<gl.n; ++f)
@@ -143,7 +158,7 @@ namespace mhh
     template<typename TF>
     void launch_ghost(const GhostList<TF>& gl, const Dims& d, const TF* dzh, cudaStream_t s)
     {
-        k_ghost<TF><<<(d.ijcells + 255)/256, 256, 0, s>>>(gl, d, dzh);
+        launch_body<GhostP<TF>, ghost_body<TF>, 256>(dim3((d.ijcells + 255)/256), dim3(256), 0, s, GhostP<TF>{gl, d, dzh});
         count_launch();
     }
 
@@ -239,9 +254,14 @@ namespace mhh
 
     // Mirror of the eddy viscosity over resolved walls, src/diff_smag2.cxx:195-207.
     template<typename TF>
-    __global__ void k_evisc_mirror(TF* evisc, Dims d)
+    struct MirrorP { TF* evisc; Dims d; };
+
+    template<typename TF>
+    __device__ __forceinline__ void evisc_mirror_body(const MirrorP<TF>& P, const VBlock& vb)
     {
-        const int n = blockIdx.x*blockDim.x + threadIdx.x;
+        TF* evisc = P.evisc;
+        const Dims& d = P.d;
+        const int n = vb.x*blockDim.x + threadIdx.x;
         if (n >= d.ijcells) return;
         const long long cb = n + (long long)d.kstart*d.ijcells;
         const long long ct = n + (long long)(d.kend-1)*d.ijcells;
@@ -276,7 +296,8 @@ namespace mhh
         }
         if (!surf)
         {
-            k_evisc_mirror<TF><<<(d.ijcells + 255)/256, 256, 0, s>>>(evisc, d);
+            launch_body<MirrorP<TF>, evisc_mirror_body<TF>, 256>(dim3((d.ijcells + 255)/256), dim3(256), 0, s,
+                                                               MirrorP<TF>{evisc, d});
             count_launch();
         }
         FieldList<TF> fl; fl.n = 1; fl.p[0] = evisc;
@@ -514,16 +535,26 @@ namespace mhh
     // cell of the full ghost layout so that the tendencies' ghost cells are
     // zeroed after the last substep as on the CPU.
     // ---------------------------------------------------------------------
-    template<typename TF, bool SCAL>
-    __global__ void __launch_bounds__(256)
-    k_presout_rk3(Dims d, Prof<TF> pr, const TF* __restrict__ p,
-                  TF* __restrict__ u, TF* __restrict__ v, TF* __restrict__ w, TF* __restrict__ s,
-                  TF* __restrict__ ut, TF* __restrict__ vt, TF* __restrict__ wt, TF* __restrict__ st,
-                  TF cbdt, TF ca, int last)
+    template<typename TF> struct PresoutP
     {
-        const int i = blockIdx.x*blockDim.x + threadIdx.x;
-        const int j = blockIdx.y*blockDim.y + threadIdx.y;
-        const int k = blockIdx.z;
+        Dims d; Prof<TF> pr; const TF* p;
+        TF *u, *v, *w, *s, *ut, *vt, *wt, *st;
+        TF cbdt, ca; int last;
+    };
+
+    template<typename TF, bool SCAL>
+    __device__ __forceinline__ void presout_rk3_body(const PresoutP<TF>& P, const VBlock& vb)
+    {
+        const Dims& d = P.d;
+        const Prof<TF>& pr = P.pr;
+        const TF* __restrict__ p = P.p;
+        TF* __restrict__ u = P.u; TF* __restrict__ v = P.v; TF* __restrict__ w = P.w; TF* __restrict__ s = P.s;
+        TF* __restrict__ ut = P.ut; TF* __restrict__ vt = P.vt; TF* __restrict__ wt = P.wt; TF* __restrict__ st = P.st;
+        const TF cbdt = P.cbdt, ca = P.ca;
+        const int last = P.last;
+        const int i = vb.x*blockDim.x + threadIdx.x;
+        const int j = vb.y*blockDim.y + threadIdx.y;
+        const int k = vb.z;
         if (i >= d.icells || j >= d.jcells) return;
         const long long c = ijk(d, i, j, k);
         const bool interior = i >= d.istart && i < d.iend && j >= d.jstart && j < d.jend && k >= d.kstart && k < d.kend;
@@ -559,15 +590,19 @@ namespace mhh
     // zeroed after the last substep); the arithmetic per cell is that of
     // k_presout_rk3.
     template<bool SCAL>
-    __global__ void __launch_bounds__(256)
-    k_presout_rk3_x2(Dims d, Prof<float> pr, const float* __restrict__ p,
-                     float* __restrict__ u, float* __restrict__ v, float* __restrict__ w, float* __restrict__ s,
-                     float* __restrict__ ut, float* __restrict__ vt, float* __restrict__ wt, float* __restrict__ st,
-                     float cbdt, float ca, int last)
+    __device__ __forceinline__ void presout_rk3_x2_body(const PresoutP<float>& P, const VBlock& vb)
     {
-        const int i = 2*(blockIdx.x*blockDim.x + threadIdx.x);
-        const int j = blockIdx.y*blockDim.y + threadIdx.y;
-        const int k = blockIdx.z;
+        const Dims& d = P.d;
+        const Prof<float>& pr = P.pr;
+        const float* __restrict__ p = P.p;
+        float* __restrict__ u = P.u; float* __restrict__ v = P.v; float* __restrict__ w = P.w; float* __restrict__ s = P.s;
+        float* __restrict__ ut = P.ut; float* __restrict__ vt = P.vt; float* __restrict__ wt = P.wt;
+        float* __restrict__ st = P.st;
+        const float cbdt = P.cbdt, ca = P.ca;
+        const int last = P.last;
+        const int i = 2*(vb.x*blockDim.x + threadIdx.x);
+        const int j = vb.y*blockDim.y + threadIdx.y;
+        const int k = vb.z;
         if (i >= d.icells || j >= d.jcells) return;
         const long long c = ijk(d, i, j, k);
         const bool row_in = j >= d.jstart && j < d.jend && k >= d.kstart && k < d.kend;
@@ -630,24 +665,21 @@ namespace mhh
         const double cB[3] = {1./3., 15./16., 8./15.};
         const int sn = (substep + 1) % 3;
         dim3 block(32, 8);
+        const PresoutP<TF> prm{d, pr, p, u, v, w, s, ut, vt, wt, st, TF(cB[substep]*dt), TF(cA[sn]), sn == 0};
         if constexpr (sizeof(TF) == 4)
         {
             if (d.icells % 2 == 0 && d.ijcells % 2 == 0)
             {
                 dim3 grid((d.icells/2 + 31)/32, (d.jcells + 7)/8, d.kcells);
-                if (s)
-                    k_presout_rk3_x2<true><<<grid, block, 0, strm>>>(d, pr, p, u, v, w, s, ut, vt, wt, st, TF(cB[substep]*dt), TF(cA[sn]), sn == 0);
-                else
-                    k_presout_rk3_x2<false><<<grid, block, 0, strm>>>(d, pr, p, u, v, w, s, ut, vt, wt, st, TF(cB[substep]*dt), TF(cA[sn]), sn == 0);
+                if (s) launch_body<PresoutP<float>, presout_rk3_x2_body<true>, 256>(grid, block, 0, strm, prm);
+                else launch_body<PresoutP<float>, presout_rk3_x2_body<false>, 256>(grid, block, 0, strm, prm);
                 count_launch();
                 return;
             }
         }
         dim3 grid((d.icells + 31)/32, (d.jcells + 7)/8, d.kcells);
-        if (s)
-            k_presout_rk3<TF, true><<<grid, block, 0, strm>>>(d, pr, p, u, v, w, s, ut, vt, wt, st, TF(cB[substep]*dt), TF(cA[sn]), sn == 0);
-        else
-            k_presout_rk3<TF, false><<<grid, block, 0, strm>>>(d, pr, p, u, v, w, s, ut, vt, wt, st, TF(cB[substep]*dt), TF(cA[sn]), sn == 0);
+        if (s) launch_body<PresoutP<TF>, presout_rk3_body<TF, true>, 256>(grid, block, 0, strm, prm);
+        else launch_body<PresoutP<TF>, presout_rk3_body<TF, false>, 256>(grid, block, 0, strm, prm);
         count_launch();
     }
 

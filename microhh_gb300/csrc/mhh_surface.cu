@@ -8,6 +8,7 @@
 // Richardson-number interpolation stay in float as in the reference, with the
 // float operations rounded one by one so that they match the CPU bit for bit.
 #include "mhh_kernels.cuh"
+#include "mhh_batchable.cuh"
 
 namespace mhh
 {
@@ -47,14 +48,27 @@ namespace mhh
         return (double)__fadd_rn(zL[n-1], __fmul_rn(__fdiv_rn(num, den), dz));
     }
 
+    // Everything the surface-layer kernels of one context read and write.
+    template<typename TF> struct SurfP
+    {
+        Dims d; SurfWork sw;
+        const TF *u, *v, *s;
+        TF *u_bot, *v_bot, *u_flux, *v_flux, *u_grad, *v_grad, *s_bot, *s_flux, *s_grad;
+        double zsl, z0m, z0h, thref_s, threfh_s, thb_s, thbh_s;
+        int thermo, thermo_bc;
+    };
+
     // Filtered wind speed, include/boundary_surface_kernels.h:132-178
     // (interior), in the field precision.
     template<typename TF>
-    __global__ void k_dutot(Dims d, const TF* __restrict__ u, const TF* __restrict__ v,
-                            const TF* __restrict__ ubot, const TF* __restrict__ vbot, double* __restrict__ dutot)
+    __device__ __forceinline__ void dutot_body(const SurfP<TF>& P, const VBlock& vb)
     {
-        const int i = d.istart + blockIdx.x*blockDim.x + threadIdx.x;
-        const int j = d.jstart + blockIdx.y*blockDim.y + threadIdx.y;
+        const Dims& d = P.d;
+        const TF* __restrict__ u = P.u; const TF* __restrict__ v = P.v;
+        const TF* __restrict__ ubot = P.u_bot; const TF* __restrict__ vbot = P.v_bot;
+        double* __restrict__ dutot = P.sw.dutot;
+        const int i = d.istart + vb.x*blockDim.x + threadIdx.x;
+        const int j = d.jstart + vb.y*blockDim.y + threadIdx.y;
         if (i >= d.iend || j >= d.jend) return;
         const long long ii = 1, jj = d.icells;
         const long long ij = i + j*jj;
@@ -111,11 +125,15 @@ namespace mhh
     // Obukhov length and friction velocity, src/boundary_surface.cxx:55-160
     // (all cells; the neutral branch when there is no thermodynamics).
     template<typename TF>
-    __global__ void k_stability(Dims d, SurfWork sw, const TF* __restrict__ s, const TF* __restrict__ s_bot,
-                                const TF* __restrict__ s_flux, double zsl, double z0m, double thref_s, double threfh_s,
-                                double thb_s, double thbh_s, int thermo, int thermo_bc)
+    __device__ __forceinline__ void stability_body(const SurfP<TF>& P, const VBlock& vb)
     {
-        const int n = blockIdx.x*blockDim.x + threadIdx.x;
+        const Dims& d = P.d;
+        const SurfWork& sw = P.sw;
+        const TF* __restrict__ s = P.s; const TF* __restrict__ s_bot = P.s_bot; const TF* __restrict__ s_flux = P.s_flux;
+        const double zsl = P.zsl, z0m = P.z0m, thref_s = P.thref_s, threfh_s = P.threfh_s;
+        const double thb_s = P.thb_s, thbh_s = P.thbh_s;
+        const int thermo = P.thermo, thermo_bc = P.thermo_bc;
+        const int n = vb.x*blockDim.x + threadIdx.x;
         if (n >= d.ijcells) return;
         using CT = TF;
         const CT du = from_d<CT>(sw.dutot[n]);
@@ -148,12 +166,15 @@ namespace mhh
 
     // Momentum fluxes, src/boundary_surface.cxx:163-190 (interior).
     template<typename TF>
-    __global__ void k_surfm(Dims d, SurfWork sw, const TF* __restrict__ u, const TF* __restrict__ v,
-                            const TF* __restrict__ ubot, const TF* __restrict__ vbot,
-                            TF* __restrict__ uflux, TF* __restrict__ vflux, double zsl, double z0m)
+    __device__ __forceinline__ void surfm_body(const SurfP<TF>& P, const VBlock& vb)
     {
-        const int i = d.istart + blockIdx.x*blockDim.x + threadIdx.x;
-        const int j = d.jstart + blockIdx.y*blockDim.y + threadIdx.y;
+        const Dims& d = P.d;
+        const SurfWork& sw = P.sw;
+        const TF* __restrict__ u = P.u; const TF* __restrict__ v = P.v;
+        const TF* __restrict__ ubot = P.u_bot; const TF* __restrict__ vbot = P.v_bot;
+        TF* __restrict__ uflux = P.u_flux; TF* __restrict__ vflux = P.v_flux;
+        const int i = d.istart + vb.x*blockDim.x + threadIdx.x;
+        const int j = d.jstart + vb.y*blockDim.y + threadIdx.y;
         if (i >= d.iend || j >= d.jend) return;
         const long long ii = 1, jj = d.icells;
         const long long ij = i + j*jj;
@@ -168,13 +189,18 @@ namespace mhh
     // Surface gradients of u and v and the scalar surface value, gradient or
     // flux, src/boundary_surface.cxx:255-338 (all cells).
     template<typename TF>
-    __global__ void k_surf_grads(Dims d, SurfWork sw, const TF* __restrict__ u, const TF* __restrict__ v,
-                                 const TF* __restrict__ ubot, const TF* __restrict__ vbot,
-                                 TF* __restrict__ ugrad, TF* __restrict__ vgrad,
-                                 const TF* __restrict__ s, TF* __restrict__ sbot, TF* __restrict__ sgrad,
-                                 TF* __restrict__ sflux, double zsl, double z0h, int thermo, int thermo_bc)
+    __device__ __forceinline__ void surf_grads_body(const SurfP<TF>& P, const VBlock& vb)
     {
-        const int n = blockIdx.x*blockDim.x + threadIdx.x;
+        const Dims& d = P.d;
+        const SurfWork& sw = P.sw;
+        const TF* __restrict__ u = P.u; const TF* __restrict__ v = P.v;
+        const TF* __restrict__ ubot = P.u_bot; const TF* __restrict__ vbot = P.v_bot;
+        TF* __restrict__ ugrad = P.u_grad; TF* __restrict__ vgrad = P.v_grad;
+        const TF* __restrict__ s = P.s; TF* __restrict__ sbot = P.s_bot; TF* __restrict__ sgrad = P.s_grad;
+        TF* __restrict__ sflux = P.s_flux;
+        const double zsl = P.zsl;
+        const int thermo = P.thermo, thermo_bc = P.thermo_bc;
+        const int n = vb.x*blockDim.x + threadIdx.x;
         if (n >= d.ijcells) return;
         const long long c = n + (long long)d.kstart*d.ijcells;
         using CT = TF;
@@ -201,12 +227,17 @@ namespace mhh
 
     // Monin-Obukhov gradients for the next viscosity, include/boundary_surface_kernels.h:180-238.
     template<typename TF>
-    __global__ void k_duvdz(Dims d, SurfWork sw, const TF* __restrict__ u, const TF* __restrict__ v,
-                            const TF* __restrict__ ubot, const TF* __restrict__ vbot, const TF* __restrict__ sflux,
-                            double zsl, double z0m, double threfh_s, int thermo)
+    __device__ __forceinline__ void duvdz_body(const SurfP<TF>& P, const VBlock& vb)
     {
-        const int i = d.istart + blockIdx.x*blockDim.x + threadIdx.x;
-        const int j = d.jstart + blockIdx.y*blockDim.y + threadIdx.y;
+        const Dims& d = P.d;
+        const SurfWork& sw = P.sw;
+        const TF* __restrict__ u = P.u; const TF* __restrict__ v = P.v;
+        const TF* __restrict__ ubot = P.u_bot; const TF* __restrict__ vbot = P.v_bot;
+        const TF* __restrict__ sflux = P.s_flux;
+        const double zsl = P.zsl, threfh_s = P.threfh_s;
+        const int thermo = P.thermo;
+        const int i = d.istart + vb.x*blockDim.x + threadIdx.x;
+        const int j = d.jstart + vb.y*blockDim.y + threadIdx.y;
         if (i >= d.iend || j >= d.jend) return;
         const long long ii = 1, jj = d.icells;
         const long long ij = i + j*jj;
@@ -239,16 +270,16 @@ namespace mhh
         const double zsl = sw.zsl, thref_s = sw.thref_s, threfh_s = sw.threfh_s;
         dim3 b2(32, 8), g2((d.itot + 31)/32, (d.jtot + 7)/8);
         const int nb = (d.ijcells + 255)/256;
-        k_dutot<TF><<<g2, b2, 0, st>>>(d, u, v, u_bot, v_bot, sw.dutot);
+        const SurfP<TF> P{d, sw, u, v, s, u_bot, v_bot, u_flux, v_flux, u_grad, v_grad, s_bot, s_flux, s_grad,
+                          zsl, z0m, z0h, thref_s, threfh_s, sw.thb_s, sw.thbh_s, thermo, thermo_bc};
+        launch_body<SurfP<TF>, dutot_body<TF>, 256>(g2, b2, 0, st, P);
         launch_cyclic2d<double>(sw.dutot, d, st);
-        k_stability<TF><<<nb, 256, 0, st>>>(d, sw, s, s_bot, s_flux, zsl, z0m, thref_s, threfh_s, sw.thb_s, sw.thbh_s,
-                                            thermo, thermo_bc);
-        k_surfm<TF><<<g2, b2, 0, st>>>(d, sw, u, v, u_bot, v_bot, u_flux, v_flux, zsl, z0m);
+        launch_body<SurfP<TF>, stability_body<TF>, 256>(dim3(nb), dim3(256), 0, st, P);
+        launch_body<SurfP<TF>, surfm_body<TF>, 256>(g2, b2, 0, st, P);
         launch_cyclic2d<TF>(u_flux, d, st);
         launch_cyclic2d<TF>(v_flux, d, st);
-        k_surf_grads<TF><<<nb, 256, 0, st>>>(d, sw, u, v, u_bot, v_bot, u_grad, v_grad, s, s_bot, s_grad, s_flux,
-                                             zsl, z0h, thermo, thermo_bc);
-        k_duvdz<TF><<<g2, b2, 0, st>>>(d, sw, u, v, u_bot, v_bot, s_flux, zsl, z0m, threfh_s, thermo);
+        launch_body<SurfP<TF>, surf_grads_body<TF>, 256>(dim3(nb), dim3(256), 0, st, P);
+        launch_body<SurfP<TF>, duvdz_body<TF>, 256>(g2, b2, 0, st, P);
         count_launch(5);
     }
 

@@ -32,6 +32,7 @@
 #include "mhh_kernels.cuh"
 #include "mhh_stencil.cuh"
 #include "mhh_flux.cuh"
+#include "mhh_batchable.cuh"
 
 namespace mhh
 {
@@ -60,10 +61,15 @@ namespace mhh
         size_t flux_smem() { return sizeof(TF)*(size_t(NSLOT)*FPS + 2*4*(NGX + NGY) + NPROF*PLEV); }
     }
 
+    template<typename TF> struct TendFluxP { Dims d; Prof<TF> pr; TendArgs<TF> a; int kchunk; };
+
     template<typename TF, bool SURF, bool SCAL, bool BUOY, bool LIM>
-    __global__ void __launch_bounds__(NTHR, FluxOcc<TF>::v)
-    k_tend_flux(Dims d, Prof<TF> pr, TendArgs<TF> a, int kchunk)
+    __device__ __forceinline__ void tend_flux_body(const TendFluxP<TF>& P, const VBlock& vb)
     {
+        const Dims& d = P.d;
+        const Prof<TF>& pr = P.pr;
+        const TendArgs<TF>& a = P.a;
+        const int kchunk = P.kchunk;
         extern __shared__ __align__(16) unsigned char smem_raw[];
         TF* sm = reinterpret_cast<TF*>(smem_raw);
         TF* gbase = sm + NSLOT*FPS;     // [2 buffers][NGX][4 fields] then [2][NGY][4]
@@ -79,11 +85,11 @@ namespace mhh
         const bool face = warp < NFY || lane < FTY;
         const bool face_x = face && fy < FTY;
         const bool face_y = face && fx < FTX;
-        const int i0 = d.istart + blockIdx.x*FTX;
-        const int j0 = d.jstart + blockIdx.y*FTY;
+        const int i0 = d.istart + vb.x*FTX;
+        const int j0 = d.jstart + vb.y*FTY;
         const int i = i0 + fx, j = j0 + fy;
         const bool cell = fx < FTX && fy < FTY && i < d.iend && j < d.jend;
-        const int k0 = d.kstart + blockIdx.z*kchunk;
+        const int k0 = d.kstart + vb.z*kchunk;
         const int k1 = min(k0 + kchunk, d.kend);
         const int pc = (min(fy, FTY) + FH)*FPW + (fx + FH);   // own (i, j) in a plane
         const int gxi = fy*NFX + fx, gyi = fy*FTX + fx;
@@ -501,15 +507,11 @@ namespace mhh
     static void launch_flux_t(const Dims& d, const Prof<TF>& pr, const TendArgs<TF>& a, int kchunk, cudaStream_t s)
     {
         const size_t smem = flux_smem<TF>();
-        // The shared-memory limit is set once per kernel, outside any stream
-        // capture that a later call may be part of.
-        static const bool attr = cudaFuncSetAttribute(k_tend_flux<TF, SURF, SCAL, BUOY, LIM>,
-            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess;
-        (void)attr;
         kchunk = min(auto_kchunk(kchunk, (long long)((d.itot + FTX - 1)/FTX)*((d.jtot + FTY - 1)/FTY), d.ktot),
                      FKCHUNK_MAX);
         dim3 grid((d.itot + FTX - 1)/FTX, (d.jtot + FTY - 1)/FTY, (d.ktot + kchunk - 1)/kchunk);
-        k_tend_flux<TF, SURF, SCAL, BUOY, LIM><<<grid, NTHR, smem, s>>>(d, pr, a, kchunk);
+        launch_body<TendFluxP<TF>, tend_flux_body<TF, SURF, SCAL, BUOY, LIM>, NTHR, FluxOcc<TF>::v>(
+            grid, dim3(NTHR), smem, s, TendFluxP<TF>{d, pr, a, kchunk});
         count_launch();
     }
 

@@ -19,6 +19,7 @@
 // and the edge terms keep only the w gradients (include/diff_kernels.h:57-103);
 // that level is computed from the planes directly.
 #include "mhh_kernels.cuh"
+#include "mhh_batchable.cuh"
 
 namespace mhh
 {
@@ -78,13 +79,29 @@ namespace mhh
             asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" :: "r"(s), "l"(src), "r"(n) : "memory");
     }
 
-    template<typename TF, bool SURF, bool THERMO>
-    __global__ void __launch_bounds__(VNT)
-    k_visc_planes(Dims d, Prof<TF> pr, const TF* __restrict__ u, const TF* __restrict__ v, const TF* __restrict__ w,
-                  const TF* __restrict__ th, TF* __restrict__ evisc, const TF* __restrict__ mlen2,
-                  const double* __restrict__ dudz, const double* __restrict__ dvdz, const double* __restrict__ dbdz,
-                  TF tpr, int kchunk)
+    template<typename TF> struct ViscPlanesP
     {
+        Dims d; Prof<TF> pr;
+        const TF *u, *v, *w, *th;
+        TF* evisc;
+        const TF* mlen2;
+        const double *dudz, *dvdz, *dbdz;
+        TF tpr; int kchunk;
+    };
+
+    template<typename TF, bool SURF, bool THERMO>
+    __device__ __forceinline__ void visc_planes_body(const ViscPlanesP<TF>& P, const VBlock& vb)
+    {
+        const Dims& d = P.d;
+        const Prof<TF>& pr = P.pr;
+        const TF* __restrict__ u = P.u; const TF* __restrict__ v = P.v; const TF* __restrict__ w = P.w;
+        const TF* __restrict__ th = P.th;
+        TF* __restrict__ evisc = P.evisc;
+        const TF* __restrict__ mlen2 = P.mlen2;
+        const double* __restrict__ dudz = P.dudz; const double* __restrict__ dvdz = P.dvdz;
+        const double* __restrict__ dbdz = P.dbdz;
+        const TF tpr = P.tpr;
+        const int kchunk = P.kchunk;
         extern __shared__ __align__(16) unsigned char smem_raw[];
         TF* sm = reinterpret_cast<TF*>(smem_raw);
         TF* exy = sm + VNSLOT*VPS;          // [2][NXY], by iteration parity
@@ -99,10 +116,10 @@ namespace mhh
         const int ex = warp < VNY ? lane : VTX;
         const int ey = warp < VNY ? warp : lane;
         const bool edge = warp < VNY || lane < VNY;
-        const int i0 = d.istart + blockIdx.x*VTX, j0 = d.jstart + blockIdx.y*VTY;
+        const int i0 = d.istart + vb.x*VTX, j0 = d.jstart + vb.y*VTY;
         const int i = i0 + ex, j = j0 + ey;
         const bool cell = ex < VTX && ey < VTY && i < d.iend && j < d.jend;
-        const int k0 = d.kstart + blockIdx.z*kchunk;
+        const int k0 = d.kstart + vb.z*kchunk;
         const int k1 = min(k0 + kchunk, d.kend);
         const int pc = (min(ey, VTY) + VH)*VPW + (ex + VH);
 
@@ -295,14 +312,11 @@ namespace mhh
                             double tpr, int kchunk, cudaStream_t s)
     {
         const size_t smem = visc_smem<TF>();
-        static const bool attr = cudaFuncSetAttribute(k_visc_planes<TF, SURF, THERMO>,
-            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess;
-        (void)attr;
         kchunk = min(auto_kchunk(kchunk, (long long)((d.itot + VTX - 1)/VTX)*((d.jtot + VTY - 1)/VTY), d.ktot),
                      VKCHUNK_MAX);
         dim3 grid((d.itot + VTX - 1)/VTX, (d.jtot + VTY - 1)/VTY, (d.ktot + kchunk - 1)/kchunk);
-        k_visc_planes<TF, SURF, THERMO><<<grid, VNT, smem, s>>>(d, pr, u, v, w, th, evisc, mlen2, dudz, dvdz, dbdz,
-                                                                TF(tpr), kchunk);
+        launch_body<ViscPlanesP<TF>, visc_planes_body<TF, SURF, THERMO>, VNT>(grid, dim3(VNT), smem, s,
+            ViscPlanesP<TF>{d, pr, u, v, w, th, evisc, mlen2, dudz, dvdz, dbdz, TF(tpr), kchunk});
         count_launch();
     }
 

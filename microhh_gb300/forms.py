@@ -84,6 +84,10 @@ def ensemble_workload(mhh, nmembers=64, steps=5):
     n0 = mhh.launch_count()
     t_graph = timed(mhh.ENS_GRAPHS, steps)
     launches = mhh.launch_count() - n0
+    timed(mhh.ENS_BATCHED, 2)         # eager step + batch plan + capture
+    n0 = mhh.launch_count()
+    t_batch = timed(mhh.ENS_BATCHED, steps)
+    launches_b = mhh.launch_count() - n0
     timed(mhh.ENS_STREAMS, 1)
     t_streams = timed(mhh.ENS_STREAMS, steps)
     ens.close()
@@ -96,8 +100,11 @@ def ensemble_workload(mhh, nmembers=64, steps=5):
         "sequential": cells * steps / t_seq,
         "streams": cells * steps / t_streams,
         "graphs": cells * steps / t_graph,
+        "batched": cells * steps / t_batch,
         "graphs_over_sequential": t_seq / t_graph,
+        "batched_over_sequential": t_seq / t_batch,
         "graph_kernel_launches_per_step": launches / steps,
+        "batched_kernel_launches_per_step": launches_b / steps,
         "autotune": report,
     }
 

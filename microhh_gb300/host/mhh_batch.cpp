@@ -166,9 +166,11 @@ namespace mhh_host
                     for (int step=0; step<n; ++step) eager_step();
                     return;
                 }
-                if (mode != MHH_ENS_GRAPHS) throw std::runtime_error("unknown ensemble mode");
+                if (mode != MHH_ENS_GRAPHS && mode != MHH_ENS_BATCHED) throw std::runtime_error("unknown ensemble mode");
                 for (auto* h : members)
                     if (!has_fixed_step(*h)) throw std::runtime_error("graph mode needs adaptivestep=false in every member");
+                if ((mode == MHH_ENS_BATCHED) != batched) drop_graphs();
+                batched = mode == MHH_ENS_BATCHED;
                 int done = 0;
                 if (!captured && done < n)
                 {
@@ -178,8 +180,19 @@ namespace mhh_host
                     ++done;
                     if (done < n)
                     {
-                        capture();
-                        launch_graphs();
+                        if (batched)
+                        {
+                            // The plan records the members' next substeps
+                            // without advancing their time loops.
+                            capture_batched();
+                            launch_graphs();
+                            for (auto* h : members) advance_step_host(*h);
+                        }
+                        else
+                        {
+                            capture();
+                            launch_graphs();
+                        }
                         ++done;
                     }
                 }
@@ -213,6 +226,53 @@ namespace mhh_host
                     cuda_ok(cudaEventRecord(joins[i], streams[i]), "record");
                     cuda_ok(cudaStreamWaitEvent(main, joins[i], 0), "wait");
                 }
+            }
+
+            // One batch plan over all members (mhh_batch_create), its three
+            // substeps captured into one graph each: a substep of the whole
+            // ensemble is one graph whose kernel nodes are the batched stages.
+            void capture_batched()
+            {
+                drop_graphs();
+                const size_t n = members.size();
+                std::vector<mhh_ctx*> ctx(n);
+                std::vector<mhh_substep_config> cfg(n);
+                std::vector<mhh_fields> f(n);
+                std::vector<mhh_bcfields> bc(n);
+                std::vector<double> dt(n);
+                for (size_t i=0; i<n; ++i)
+                {
+                    ctx[i] = ctx_of(*members[i]);
+                    members[i]->visit([&](auto& m) { m.substep_args(cfg[i], f[i], bc[i], dt[i]); });
+                }
+                cuda_ok(cudaStreamSynchronize(main), "sync");
+                for (auto st : streams) cuda_ok(cudaStreamSynchronize(st), "sync");
+                if (mhh_batch_create((int)n, ctx.data(), cfg.data(), f.data(), bc.data(), dt.data(), &plan) != MHH_OK)
+                {
+                    plan = nullptr;
+                    throw std::runtime_error(std::string("batch plan: ") + mhh_last_error());
+                }
+                gkernels = 0;
+                for (int q=0; q<3; ++q)
+                {
+                    int nl = 0;
+                    mhh_batch_launches(plan, q, &nl);
+                    gkernels += nl;
+                    cudaGraph_t graph = nullptr;
+                    cuda_ok(cudaStreamBeginCapture(main, cudaStreamCaptureModeThreadLocal), "begin capture");
+                    const int rc = mhh_batch_substep(plan, q, main);
+                    cuda_ok(cudaStreamEndCapture(main, &graph), "end capture");
+                    if (rc != MHH_OK)
+                    {
+                        if (graph) cudaGraphDestroy(graph);
+                        throw std::runtime_error(std::string("batch substep: ") + mhh_last_error());
+                    }
+                    const cudaError_t e = cudaGraphInstantiate(&gexec[q], graph, 0);
+                    cudaGraphDestroy(graph);
+                    cuda_ok(e, "graph instantiate");
+                }
+                mhh_launch_count_add(-gkernels);   // captured, not yet run
+                captured = true;
             }
 
             void capture()
@@ -259,6 +319,7 @@ namespace mhh_host
             void drop_graphs()
             {
                 for (auto& g : gexec) if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+                if (plan) { mhh_batch_destroy(plan); plan = nullptr; }
                 captured = false;
             }
 
@@ -270,6 +331,8 @@ namespace mhh_host
             cudaGraphExec_t gexec[3] = {nullptr, nullptr, nullptr};
             long long gkernels = 0;
             bool captured = false;
+            bool batched = false;
+            mhh_batch* plan = nullptr;
     };
 
     // Times a scratch copy of one member per grid size under each candidate

@@ -921,6 +921,15 @@ namespace mhh_host
     }
 
     template<typename TF>
+    void Model<TF>::substep_args(mhh_substep_config& c, mhh_fields& f, mhh_bcfields& b, double& dt) const
+    {
+        c = cfg;
+        f = fields->dev();
+        b = fields->bc();
+        dt = timeloop->get_dt();
+    }
+
+    template<typename TF>
     void Model<TF>::advance_substep_host()
     {
         timeloop->advance_substep();

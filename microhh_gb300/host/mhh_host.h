@@ -366,6 +366,9 @@ namespace mhh_host
             // Advances the host-side time loop by one substep without
             // launching (after the replay of a captured substep).
             void advance_substep_host();
+            // The arguments of this model's fused substep (mhh_substep_begin/end)
+            // and its time step, for a batched substep over many models.
+            void substep_args(mhh_substep_config& c, mhh_fields& f, mhh_bcfields& b, double& dt) const;
             bool adaptive() const { return adaptive_; }
             const std::string& ini() const { return ini_text; }
             const std::vector<double>& levels() const { return z_full; }

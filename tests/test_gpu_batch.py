@@ -40,7 +40,7 @@ def alone(mhh, case, nsteps):
     return out
 
 
-@pytest.mark.parametrize("mode", [0, 1, 2], ids=["sequential", "streams", "graphs"])
+@pytest.mark.parametrize("mode", [0, 1, 2, 3], ids=["sequential", "streams", "graphs", "batched"])
 def test_ensemble_identical_to_alone(mhh, mode):
     cs = members()
     ref = [alone(mhh, c, 4) for c in cs]
@@ -55,6 +55,34 @@ def test_ensemble_identical_to_alone(mhh, mode):
         for n in c.prognostic_names():
             assert np.array_equal(m.get(n), r[n]), (c.name, n, mode)
     ens.close()
+
+
+def test_batched_launches_scale_with_stages(mhh):
+    """Batched mode launches one kernel per stage for all members (one per
+    group of members with the same FFT length in the transform stages), so
+    a step launches far fewer kernels than the members' own graphs, and
+    doubling the members of the same sizes does not add launches."""
+    def launches_per_step(cs, mode):
+        models = [mhh.Model(c, precision=mhh.FP32) for c in cs]
+        ens = mhh.Ensemble(models)
+        ens.run_steps(2, mode)
+        ens.synchronize()
+        n0 = mhh.launch_count()
+        ens.run_steps(2, mode)
+        ens.synchronize()
+        n = (mhh.launch_count() - n0) / 2
+        ens.close()
+        for m in models:
+            m.close()
+        return n
+    cs = members()
+    per_graph = launches_per_step(cs, mhh.ENS_GRAPHS)
+    per_batch = launches_per_step(cs, mhh.ENS_BATCHED)
+    assert per_batch <= per_graph / 2, (per_batch, per_graph)
+    twice = members() + [c for c in members()]
+    for q, c in enumerate(twice[4:]):
+        c.fields["th"] = c.fields["th"] + 0.01 * (q + 1)
+    assert launches_per_step(twice, mhh.ENS_BATCHED) == per_batch
 
 
 def test_ensemble_autotune_keeps_state_and_parity(mhh):
