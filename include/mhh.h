@@ -355,7 +355,8 @@ int mhh_substep_end(mhh_ctx* ctx, const mhh_substep_config* cfg, const mhh_field
    allocates the launch tables; call it after one ordinary substep of every
    context (kernel attributes are set on first use) and outside any stream
    capture.  A configuration with a kernel that cannot run batched (the
-   buffer layer, the per-cell kernel variants) returns MHH_ERR_UNSUPPORTED.
+   separate pressure right-hand-side and scatter kernels of the option
+   pres_fuse = 0) returns MHH_ERR_UNSUPPORTED.
    mhh_batch_substep launches substep 0, 1 or 2 of all contexts on the
    stream; mhh_batch_launches gives its number of launches. */
 typedef struct mhh_batch mhh_batch;

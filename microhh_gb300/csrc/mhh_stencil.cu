@@ -168,16 +168,32 @@ namespace mhh
     // viscosity (src/diff_smag2.cxx:47-269) in one pass; evisc holds the
     // result at interior cells.
     // ---------------------------------------------------------------------
-    template<typename TF, bool SURF, bool THERMO>
-    __global__ void __launch_bounds__(256)
-    k_viscosity(Dims d, Prof<TF> pr, const TF* __restrict__ u, const TF* __restrict__ v, const TF* __restrict__ w,
-                const TF* __restrict__ th, TF* __restrict__ evisc, const TF* __restrict__ mlen2,
-                const double* __restrict__ dudz, const double* __restrict__ dvdz, const double* __restrict__ dbdz,
-                TF cs, TF tpr, TF visc, int mason)
+    template<typename TF> struct ViscP
     {
-        const int i = d.istart + blockIdx.x*blockDim.x + threadIdx.x;
-        const int j = d.jstart + blockIdx.y*blockDim.y + threadIdx.y;
-        const int k = d.kstart + blockIdx.z;
+        Dims d; Prof<TF> pr;
+        const TF *u, *v, *w, *th;
+        TF* evisc;
+        const TF* mlen2;
+        const double *dudz, *dvdz, *dbdz;
+        TF cs, tpr, visc; int mason;
+    };
+
+    template<typename TF, bool SURF, bool THERMO>
+    __device__ __forceinline__ void viscosity_body(const ViscP<TF>& P, const VBlock& vb)
+    {
+        const Dims& d = P.d;
+        const Prof<TF>& pr = P.pr;
+        const TF* __restrict__ u = P.u; const TF* __restrict__ v = P.v; const TF* __restrict__ w = P.w;
+        const TF* __restrict__ th = P.th;
+        TF* __restrict__ evisc = P.evisc;
+        const TF* __restrict__ mlen2 = P.mlen2;
+        const double* __restrict__ dudz = P.dudz; const double* __restrict__ dvdz = P.dvdz;
+        const double* __restrict__ dbdz = P.dbdz;
+        const TF cs = P.cs, tpr = P.tpr, visc = P.visc;
+        const int mason = P.mason;
+        const int i = d.istart + vb.x*blockDim.x + threadIdx.x;
+        const int j = d.jstart + vb.y*blockDim.y + threadIdx.y;
+        const int k = d.kstart + vb.z;
         if (i >= d.iend || j >= d.jend) return;
         const long long ii = 1, jj = d.icells, kk = d.ijcells;
         const long long c = ijk(d, i, j, k);
@@ -284,14 +300,11 @@ namespace mhh
                                                                     tpr, surf, thermo, o.visc_kchunk, s);
         if (!planes)
         {
-            if (surf && thermo)
-                k_viscosity<TF, true, true><<<grid, block, 0, s>>>(d, pr, u, v, w, th, evisc, mlen2, dudz, dvdz, dbdz, TF(cs), TF(tpr), TF(visc), mason);
-            else if (surf)
-                k_viscosity<TF, true, false><<<grid, block, 0, s>>>(d, pr, u, v, w, th, evisc, mlen2, dudz, dvdz, dbdz, TF(cs), TF(tpr), TF(visc), mason);
-            else if (thermo)
-                k_viscosity<TF, false, true><<<grid, block, 0, s>>>(d, pr, u, v, w, th, evisc, mlen2, dudz, dvdz, dbdz, TF(cs), TF(tpr), TF(visc), mason);
-            else
-                k_viscosity<TF, false, false><<<grid, block, 0, s>>>(d, pr, u, v, w, th, evisc, mlen2, dudz, dvdz, dbdz, TF(cs), TF(tpr), TF(visc), mason);
+            const ViscP<TF> P{d, pr, u, v, w, th, evisc, mlen2, dudz, dvdz, dbdz, TF(cs), TF(tpr), TF(visc), mason};
+            if (surf && thermo) launch_body<ViscP<TF>, viscosity_body<TF, true, true>, 256>(grid, block, 0, s, P);
+            else if (surf) launch_body<ViscP<TF>, viscosity_body<TF, true, false>, 256>(grid, block, 0, s, P);
+            else if (thermo) launch_body<ViscP<TF>, viscosity_body<TF, false, true>, 256>(grid, block, 0, s, P);
+            else launch_body<ViscP<TF>, viscosity_body<TF, false, false>, 256>(grid, block, 0, s, P);
             count_launch();
         }
         if (!surf)
@@ -309,13 +322,17 @@ namespace mhh
     // before the pressure solve (thermo buoyancy, advection, diffusion,
     // large-scale pressure force), one interior cell per thread.
     // ---------------------------------------------------------------------
+    template<typename TF> struct TendP { Dims d; Prof<TF> pr; TendArgs<TF> a; };
+
     template<typename TF, int ADV, int DIF, bool SURF, bool SCAL, bool BUOY, bool FORCE>
-    __global__ void __launch_bounds__(256)
-    k_tendency(Dims d, Prof<TF> pr, TendArgs<TF> a)
+    __device__ __forceinline__ void tendency_body(const TendP<TF>& P, const VBlock& vb)
     {
-        const int i = d.istart + blockIdx.x*blockDim.x + threadIdx.x;
-        const int j = d.jstart + blockIdx.y*blockDim.y + threadIdx.y;
-        const int k = d.kstart + blockIdx.z;
+        const Dims& d = P.d;
+        const Prof<TF>& pr = P.pr;
+        const TendArgs<TF>& a = P.a;
+        const int i = d.istart + vb.x*blockDim.x + threadIdx.x;
+        const int j = d.jstart + vb.y*blockDim.y + threadIdx.y;
+        const int k = d.kstart + vb.z;
         if (i >= d.iend || j >= d.jend) return;
         const long long c = ijk(d, i, j, k);
         const long long ij = i + (long long)j*d.icells;
@@ -373,7 +390,7 @@ namespace mhh
     {
         dim3 block(32, 8);
         dim3 grid((d.itot + 31)/32, (d.jtot + 7)/8, d.ktot);
-        k_tendency<TF, ADV, DIF, SURF, SCAL, BUOY, FORCE><<<grid, block, 0, s>>>(d, pr, a);
+        launch_body<TendP<TF>, tendency_body<TF, ADV, DIF, SURF, SCAL, BUOY, FORCE>, 256>(grid, block, 0, s, TendP<TF>{d, pr, a});
         count_launch();
     }
 
@@ -487,14 +504,25 @@ namespace mhh
     // for u, v, s at the full levels and w (towards zero) at the half levels
     // inside the layer; levels with sigma = 0 are below it and untouched.
     // ---------------------------------------------------------------------
-    template<typename TF>
-    __global__ void k_buffer(Dims d, const TF* __restrict__ prof, int kb, const TF* __restrict__ u,
-                             const TF* __restrict__ v, const TF* __restrict__ w, const TF* __restrict__ s,
-                             TF* __restrict__ ut, TF* __restrict__ vt, TF* __restrict__ wt, TF* __restrict__ st)
+    template<typename TF> struct BufferP
     {
-        const int i = d.istart + blockIdx.x*blockDim.x + threadIdx.x;
-        const int j = d.jstart + blockIdx.y*blockDim.y + threadIdx.y;
-        const int k = kb + blockIdx.z;
+        Dims d; const TF* prof; int kb;
+        const TF *u, *v, *w, *s;
+        TF *ut, *vt, *wt, *st;
+    };
+
+    template<typename TF>
+    __device__ __forceinline__ void buffer_body(const BufferP<TF>& P, const VBlock& vb)
+    {
+        const Dims& d = P.d;
+        const TF* __restrict__ prof = P.prof;
+        const int kb = P.kb;
+        const TF* __restrict__ u = P.u; const TF* __restrict__ v = P.v; const TF* __restrict__ w = P.w;
+        const TF* __restrict__ s = P.s;
+        TF* __restrict__ ut = P.ut; TF* __restrict__ vt = P.vt; TF* __restrict__ wt = P.wt; TF* __restrict__ st = P.st;
+        const int i = d.istart + vb.x*blockDim.x + threadIdx.x;
+        const int j = d.jstart + vb.y*blockDim.y + threadIdx.y;
+        const int k = kb + vb.z;
         if (i >= d.iend || j >= d.jend || k >= d.kend) return;
         const int kc = d.kcells;
         const TF sf = prof[k], sh = prof[kc + k];
@@ -514,7 +542,7 @@ namespace mhh
     {
         if (kb >= d.kend) return;
         dim3 block(32, 8), grid((d.itot + 31)/32, (d.jtot + 7)/8, d.kend - kb);
-        k_buffer<TF><<<grid, block, 0, strm>>>(d, prof, kb, u, v, w, s, ut, vt, wt, st);
+        launch_body<BufferP<TF>, buffer_body<TF>, 256>(grid, block, 0, strm, BufferP<TF>{d, prof, kb, u, v, w, s, ut, vt, wt, st});
         count_launch();
     }
 

@@ -11,6 +11,7 @@
 // src/advec_2i5.cxx:150-728, include/diff_kernels.h:144-484 and
 // src/thermo_dry.cxx:165-181).
 #include "mhh_kernels.cuh"
+#include "mhh_batchable.cuh"
 #include "mhh_stencil.cuh"
 
 namespace mhh
@@ -56,10 +57,14 @@ namespace mhh
     // Two blocks per SM for float; double needs the full register file.
     template<typename TF> struct LesOcc { static constexpr int v = sizeof(TF) == 4 ? 2 : 1; };
 
+    template<typename TF> struct TendLesP { Dims d; Prof<TF> pr; TendArgs<TF> a; };
+
     template<typename TF, bool SURF, bool SCAL, bool BUOY>
-    __global__ void __launch_bounds__(TX*TY, LesOcc<TF>::v)
-    k_tend_les(Dims d, Prof<TF> pr, TendArgs<TF> a)
+    __device__ __forceinline__ void tend_les_body(const TendLesP<TF>& P, const VBlock& vb)
     {
+        const Dims& d = P.d;
+        const Prof<TF>& pr = P.pr;
+        const TendArgs<TF>& a = P.a;
         extern __shared__ __align__(16) unsigned char smem_raw[];
         TF* sm = reinterpret_cast<TF*>(smem_raw);
         // Plane slots: 0,1 u; 2,3 v; 4,5 w; 6 s; 7,8,9 evisc (addressed by
@@ -71,11 +76,11 @@ namespace mhh
         TF* ps = sm + 6*PS;
 
         const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + ty*TX;
-        const int i0 = d.istart + blockIdx.x*TX;
-        const int j0 = d.jstart + blockIdx.y*TY;
+        const int i0 = d.istart + vb.x*TX;
+        const int j0 = d.jstart + vb.y*TY;
         const int i = i0 + tx, j = j0 + ty;
         const bool active = i < d.iend && j < d.jend;
-        const int k0 = d.kstart + blockIdx.z*KCHUNK;
+        const int k0 = d.kstart + vb.z*KCHUNK;
         const int k1 = min(k0 + KCHUNK, d.kend);
 
         const TF* __restrict__ u = a.u;
@@ -299,10 +304,8 @@ namespace mhh
         const size_t smem = sizeof(TF)*NPLANE*PS;
         dim3 block(TX, TY);
         dim3 grid((d.itot + TX - 1)/TX, (d.jtot + TY - 1)/TY, (d.ktot + KCHUNK - 1)/KCHUNK);
-        static const bool attr = cudaFuncSetAttribute(k_tend_les<TF, SURF, SCAL, BUOY>,
-            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess;
-        (void)attr;
-        k_tend_les<TF, SURF, SCAL, BUOY><<<grid, block, smem, s>>>(d, pr, a);
+        launch_body<TendLesP<TF>, tend_les_body<TF, SURF, SCAL, BUOY>, TX*TY, LesOcc<TF>::v>(grid, block, smem, s,
+                                                                                     TendLesP<TF>{d, pr, a});
         count_launch();
     }
 
