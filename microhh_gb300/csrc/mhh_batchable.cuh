@@ -71,12 +71,22 @@ namespace mhh
         BODY(p, vblock_self());
     }
 
+    // The context's parameters are copied to shared memory first: the body
+    // reads them as often as it reads kernel parameters, and from global
+    // memory each read would be a load instruction of its own.
     template<class P, void (*BODY)(const P&, const VBlock&), int MAXT, int MINB>
     __global__ void __launch_bounds__(MAXT, MINB) k_many(const P* __restrict__ ps, BatchMap map)
     {
+        static_assert(sizeof(P) % 4 == 0, "parameter structs are word-sized");
+        __shared__ __align__(16) unsigned int pbuf[sizeof(P)/4];
         VBlock vb;
         const int m = batch_find(map, vb);
-        BODY(ps[m], vb);
+        const unsigned int* src = reinterpret_cast<const unsigned int*>(ps + m);
+        const int tid = threadIdx.x + blockDim.x*(threadIdx.y + blockDim.y*threadIdx.z);
+        const int nt = blockDim.x*blockDim.y*blockDim.z;
+        for (int q = tid; q < (int)(sizeof(P)/4); q += nt) pbuf[q] = __ldg(src + q);
+        __syncthreads();
+        BODY(*reinterpret_cast<const P*>(pbuf), vb);
     }
 
     // One recorded launch of one context.

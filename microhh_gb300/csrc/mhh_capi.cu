@@ -1421,6 +1421,7 @@ struct mhh_batch
 {
     struct Group
     {
+        int stage;
         const void* fn;
         dim3 block;
         size_t smem;
@@ -1432,6 +1433,11 @@ struct mhh_batch
     int n;
     std::vector<Group> groups[3];
     std::vector<void*> mem;
+    // Groups of one stage (different contexts) run side by side: the extra
+    // groups of a stage go to their own streams, forked from and joined into
+    // the caller's stream.
+    std::vector<cudaStream_t> side;
+    std::vector<cudaEvent_t> events;    // [0] fork, [1..] joins
 };
 
 namespace
@@ -1439,6 +1445,8 @@ namespace
     void batch_free(mhh_batch* b)
     {
         for (void* p : b->mem) cudaFree(p);
+        for (auto st : b->side) cudaStreamDestroy(st);
+        for (auto e : b->events) cudaEventDestroy(e);
         delete b;
     }
 
@@ -1513,6 +1521,7 @@ int mhh_batch_create(int n, mhh_ctx* const* ctx, const mhh_substep_config* cfg, 
                     { mem.push_back(m); done[m] = 1; }
                 }
                 mhh_batch::Group g{};
+                g.stage = (int)st;
                 g.fn = L0.fn; g.block = L0.block; g.nmem = (int)mem.size();
                 const size_t psz = L0.params.size();
                 std::vector<unsigned char> params(psz*mem.size());
@@ -1544,6 +1553,28 @@ int mhh_batch_create(int n, mhh_ctx* const* ctx, const mhh_substep_config* cfg, 
         }
     }
     cudaStreamDestroy(scratch);
+    // Side streams for the largest number of groups in one stage.
+    size_t width = 1;
+    for (int q=0; q<3 && !rc; ++q)
+        for (size_t a=0; a<b->groups[q].size(); )
+        {
+            size_t e = a;
+            while (e < b->groups[q].size() && b->groups[q][e].stage == b->groups[q][a].stage) ++e;
+            width = std::max(width, e - a);
+            a = e;
+        }
+    for (size_t w=1; w<width && !rc; ++w)
+    {
+        cudaStream_t st;
+        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) { rc = fail(MHH_ERR_CUDA, "stream"); break; }
+        b->side.push_back(st);
+    }
+    for (size_t w=0; w<width && !rc; ++w)
+    {
+        cudaEvent_t e;
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) { rc = fail(MHH_ERR_CUDA, "event"); break; }
+        b->events.push_back(e);
+    }
     if (!rc && cudaDeviceSynchronize() != cudaSuccess) rc = fail(MHH_ERR_CUDA, "batch: set-up");
     if (rc) { batch_free(b); return rc; }
     *out = b;
@@ -1553,15 +1584,36 @@ int mhh_batch_create(int n, mhh_ctx* const* ctx, const mhh_substep_config* cfg, 
 int mhh_batch_substep(mhh_batch* b, int substep, cudaStream_t s)
 {
     if (!b || substep < 0 || substep > 2) return fail(MHH_ERR_ARG, "bad argument");
-    for (const auto& g : b->groups[substep])
+    auto launch = [&](const mhh_batch::Group& g, cudaStream_t st)
     {
         mhh::BatchMap map{g.start, g.grid, g.nmem};
         const void* params = g.params;
         void* args[] = {(void*)&params, (void*)&map};
-        if (cudaLaunchKernel(g.fn, dim3(g.nblocks), g.block, args, g.smem, s) != cudaSuccess)
-            return fail(MHH_ERR_CUDA, "batch: launch");
+        return cudaLaunchKernel(g.fn, dim3(g.nblocks), g.block, args, g.smem, st) == cudaSuccess;
+    };
+    const auto& gs = b->groups[substep];
+    for (size_t a=0; a<gs.size(); )
+    {
+        size_t e = a;
+        while (e < gs.size() && gs[e].stage == gs[a].stage) ++e;
+        bool ok = true;
+        if (e - a == 1) ok = launch(gs[a], s);
+        else
+        {
+            ok = cudaEventRecord(b->events[0], s) == cudaSuccess;
+            for (size_t g=a+1; g<e && ok; ++g)
+            {
+                cudaStream_t st = b->side[g - a - 1];
+                ok = cudaStreamWaitEvent(st, b->events[0], 0) == cudaSuccess && launch(gs[g], st)
+                     && cudaEventRecord(b->events[g - a], st) == cudaSuccess;
+            }
+            ok = ok && launch(gs[a], s);
+            for (size_t g=a+1; g<e && ok; ++g) ok = cudaStreamWaitEvent(s, b->events[g - a], 0) == cudaSuccess;
+        }
+        if (!ok) return fail(MHH_ERR_CUDA, "batch: launch");
+        a = e;
     }
-    count_launch((int)b->groups[substep].size());
+    count_launch((int)gs.size());
     return check_cuda("batch substep");
 }
 
