@@ -26,9 +26,10 @@ enum mhh_ensemble_mode
     MHH_ENS_SEQUENTIAL = 0,  /* one member after another on one stream */
     MHH_ENS_STREAMS = 1,     /* every member on its own stream, substep by substep */
     MHH_ENS_GRAPHS = 2,      /* one CUDA-graph launch per RK3 substep for all members */
-    MHH_ENS_BATCHED = 3      /* as GRAPHS, with one kernel launch per stage over all members
-                                (mhh_batch_substep); members whose kernels cannot run batched
-                                make this an MHH_ERR_UNSUPPORTED error */
+    MHH_ENS_BATCHED = 3      /* as GRAPHS, with one kernel launch per stage over all members of
+                                one grid size (mhh_batch_substep), the sizes as parallel
+                                branches; members whose kernels cannot run batched make this
+                                an error */
 };
 
 int mhh_ensemble_create(mhh_ensemble** out);

@@ -228,39 +228,63 @@ namespace mhh_host
                 }
             }
 
-            // One batch plan over all members (mhh_batch_create), its three
-            // substeps captured into one graph each: a substep of the whole
-            // ensemble is one graph whose kernel nodes are the batched stages.
+            // Batch plans over the members (mhh_batch_create), one per grid
+            // size: within a plan every stage is one kernel over all its
+            // members, and the plans run as parallel branches of the graph,
+            // so that members of one size do not wait at every stage for the
+            // tails of the other sizes.  A substep of the whole ensemble is
+            // one graph whose kernel nodes are the batched stages.
             void capture_batched()
             {
                 drop_graphs();
-                const size_t n = members.size();
-                std::vector<mhh_ctx*> ctx(n);
-                std::vector<mhh_substep_config> cfg(n);
-                std::vector<mhh_fields> f(n);
-                std::vector<mhh_bcfields> bc(n);
-                std::vector<double> dt(n);
-                for (size_t i=0; i<n; ++i)
+                std::map<std::tuple<int, int, int>, std::vector<size_t>> buckets;
+                for (size_t i=0; i<members.size(); ++i)
                 {
-                    ctx[i] = ctx_of(*members[i]);
-                    members[i]->visit([&](auto& m) { m.substep_args(cfg[i], f[i], bc[i], dt[i]); });
+                    mhh_grid g;
+                    members[i]->visit([&](auto& m) { g = m.get_grid().get_grid_data(); });
+                    buckets[std::make_tuple(g.itot, g.jtot, g.ktot)].push_back(i);
                 }
                 cuda_ok(cudaStreamSynchronize(main), "sync");
                 for (auto st : streams) cuda_ok(cudaStreamSynchronize(st), "sync");
-                if (mhh_batch_create((int)n, ctx.data(), cfg.data(), f.data(), bc.data(), dt.data(), &plan) != MHH_OK)
+                for (auto& kv : buckets)
                 {
-                    plan = nullptr;
-                    throw std::runtime_error(std::string("batch plan: ") + mhh_last_error());
+                    const size_t n = kv.second.size();
+                    std::vector<mhh_ctx*> ctx(n);
+                    std::vector<mhh_substep_config> cfg(n);
+                    std::vector<mhh_fields> f(n);
+                    std::vector<mhh_bcfields> bc(n);
+                    std::vector<double> dt(n);
+                    for (size_t q=0; q<n; ++q)
+                    {
+                        ModelHandle* h = members[kv.second[q]];
+                        ctx[q] = ctx_of(*h);
+                        h->visit([&](auto& m) { m.substep_args(cfg[q], f[q], bc[q], dt[q]); });
+                    }
+                    mhh_batch* p = nullptr;
+                    if (mhh_batch_create((int)n, ctx.data(), cfg.data(), f.data(), bc.data(), dt.data(), &p) != MHH_OK)
+                        throw std::runtime_error(std::string("batch plan: ") + mhh_last_error());
+                    plans.push_back(p);
                 }
                 gkernels = 0;
                 for (int q=0; q<3; ++q)
                 {
-                    int nl = 0;
-                    mhh_batch_launches(plan, q, &nl);
-                    gkernels += nl;
+                    for (auto* p : plans)
+                    {
+                        int nl = 0;
+                        mhh_batch_launches(p, q, &nl);
+                        gkernels += nl;
+                    }
                     cudaGraph_t graph = nullptr;
                     cuda_ok(cudaStreamBeginCapture(main, cudaStreamCaptureModeThreadLocal), "begin capture");
-                    const int rc = mhh_batch_substep(plan, q, main);
+                    int rc = MHH_OK;
+                    cuda_ok(cudaEventRecord(fork, main), "record");
+                    for (size_t b=0; b<plans.size() && rc == MHH_OK; ++b)
+                    {
+                        cuda_ok(cudaStreamWaitEvent(streams[b], fork, 0), "wait");
+                        rc = mhh_batch_substep(plans[b], q, streams[b]);
+                        cuda_ok(cudaEventRecord(joins[b], streams[b]), "record");
+                        cuda_ok(cudaStreamWaitEvent(main, joins[b], 0), "wait");
+                    }
                     cuda_ok(cudaStreamEndCapture(main, &graph), "end capture");
                     if (rc != MHH_OK)
                     {
@@ -319,7 +343,8 @@ namespace mhh_host
             void drop_graphs()
             {
                 for (auto& g : gexec) if (g) { cudaGraphExecDestroy(g); g = nullptr; }
-                if (plan) { mhh_batch_destroy(plan); plan = nullptr; }
+                for (auto* p : plans) mhh_batch_destroy(p);
+                plans.clear();
                 captured = false;
             }
 
@@ -332,7 +357,7 @@ namespace mhh_host
             long long gkernels = 0;
             bool captured = false;
             bool batched = false;
-            mhh_batch* plan = nullptr;
+            std::vector<mhh_batch*> plans;
     };
 
     // Times a scratch copy of one member per grid size under each candidate

@@ -58,10 +58,10 @@ def test_ensemble_identical_to_alone(mhh, mode):
 
 
 def test_batched_launches_scale_with_stages(mhh):
-    """Batched mode launches one kernel per stage for all members (one per
-    group of members with the same FFT length in the transform stages), so
-    a step launches far fewer kernels than the members' own graphs, and
-    doubling the members of the same sizes does not add launches."""
+    """Batched mode launches one kernel per stage for all members of one grid
+    size, so the launches of a step grow with the number of distinct sizes,
+    not with the number of members: doubling the members (same sizes, other
+    states) keeps the count, while the members' own graphs double it."""
     def launches_per_step(cs, mode):
         models = [mhh.Model(c, precision=mhh.FP32) for c in cs]
         ens = mhh.Ensemble(models)
@@ -75,14 +75,17 @@ def test_batched_launches_scale_with_stages(mhh):
         for m in models:
             m.close()
         return n
-    cs = members()
-    per_graph = launches_per_step(cs, mhh.ENS_GRAPHS)
-    per_batch = launches_per_step(cs, mhh.ENS_BATCHED)
-    assert per_batch <= per_graph / 2, (per_batch, per_graph)
-    twice = members() + [c for c in members()]
+    once = members()
+    twice = members() + members()
     for q, c in enumerate(twice[4:]):
         c.fields["th"] = c.fields["th"] + 0.01 * (q + 1)
-    assert launches_per_step(twice, mhh.ENS_BATCHED) == per_batch
+    batch_once = launches_per_step(once, mhh.ENS_BATCHED)
+    batch_twice = launches_per_step(twice, mhh.ENS_BATCHED)
+    graph_once = launches_per_step(once, mhh.ENS_GRAPHS)
+    graph_twice = launches_per_step(twice, mhh.ENS_GRAPHS)
+    assert batch_twice == batch_once, (batch_once, batch_twice)
+    assert graph_twice == 2 * graph_once, (graph_once, graph_twice)
+    assert batch_twice <= graph_twice / 2, (batch_twice, graph_twice)
 
 
 def test_ensemble_autotune_keeps_state_and_parity(mhh):
