@@ -352,7 +352,9 @@ int mhh_substep_end(mhh_ctx* ctx, const mhh_substep_config* cfg, const mhh_field
    fixed full time step).  Every context gets the kernels and parameters of
    its own mhh_substep_begin/end, so its results are the same bit for bit.
    mhh_batch_create records the contexts' substeps without running them and
-   allocates the launch tables; call it after one ordinary substep of every
+   builds the launch parameters on the host (no device memory; the kernels
+   take up to 32 KB of parameters per launch, larger groups are split into
+   several launches); call it after one ordinary substep of every
    context (kernel attributes are set on first use) and outside any stream
    capture.  A configuration with a kernel that cannot run batched (the
    separate pressure right-hand-side and scatter kernels of the option

@@ -4,11 +4,14 @@
 // A kernel of the substep is written as a body over a parameter struct P and
 // a block position (VBlock) instead of blockIdx / gridDim.  Two entry points
 // wrap the same body: k_one<P, BODY>(P) for a launch of one context, and
-// k_many<P, BODY>(const P*, BatchMap) for a launch over many contexts, where
-// the contexts' grids are laid end to end in x: context m owns the blocks
-// [start[m], start[m+1]) and decomposes its local block index into its own
-// (gx, gy, gz) grid.  A body therefore runs with the same parameters and
-// block positions in both, and gives the same results bit for bit.
+// k_many<P, BODY>(ManyArgs<P>) for a launch over up to ManyArgs<P>::NMAX
+// contexts, where the contexts' grids are laid end to end in x: context m
+// owns the blocks [start[m], start[m+1]) and decomposes its local block
+// index into its own (gx, gy, gz) grid.  A body therefore runs with the same
+// parameters and block positions in both, and gives the same results bit for
+// bit.  Both entry points take their parameters in the kernel parameter
+// space (up to 32 KB, __grid_constant__), which the compiler treats as
+// constant: a body reads them as cheaply in either.
 //
 // launch_body() is the one launch site.  Normally it launches k_one.  While
 // a batch plan records a context's substep (BatchRecorder), it appends the
@@ -17,6 +20,7 @@
 // the same stage into one launch.
 #pragma once
 
+#include <cstddef>
 #include <cstring>
 #include <vector>
 
@@ -38,26 +42,33 @@ namespace mhh
         return b;
     }
 
-    // Block map of a launch over n contexts (device arrays).
-    struct BatchMap
+    // Parameters of a launch over n <= NMAX contexts: the block offsets
+    // (n + 1 prefix sums of the contexts' block counts), the contexts' grids
+    // and their parameter structs.
+    template<class P>
+    struct ManyArgs
     {
-        const int* start;     // n + 1 prefix sums of the contexts' block counts
-        const int4* grid;     // (gx, gy, gz, 0) of each context
+        static constexpr int NMAX_FIT = (32000 - 32) / (int)(sizeof(P) + sizeof(int) + sizeof(int4));
+        static constexpr int NMAX = NMAX_FIT < 1 ? 1 : (NMAX_FIT > 128 ? 128 : NMAX_FIT);
+        int4 grid[NMAX];
+        P p[NMAX];
+        int start[NMAX + 1];
         int n;
     };
 
     // The context of this block and its block position within the context.
-    __device__ __forceinline__ int batch_find(const BatchMap& m, VBlock& vb)
+    template<class P>
+    __device__ __forceinline__ int batch_find(const ManyArgs<P>& a, VBlock& vb)
     {
         const int b = blockIdx.x;
-        int lo = 0, hi = m.n - 1;
+        int lo = 0, hi = a.n - 1;
         while (lo < hi)
         {
             const int mid = (lo + hi + 1) >> 1;
-            if (__ldg(m.start + mid) <= b) lo = mid; else hi = mid - 1;
+            if (a.start[mid] <= b) lo = mid; else hi = mid - 1;
         }
-        const int4 g = __ldg(m.grid + lo);
-        const int local = b - __ldg(m.start + lo);
+        const int4 g = a.grid[lo];
+        const int local = b - a.start[lo];
         vb.gx = g.x; vb.gy = g.y; vb.gz = g.z;
         vb.x = local % g.x;
         vb.y = (local / g.x) % g.y;
@@ -71,31 +82,24 @@ namespace mhh
         BODY(p, vblock_self());
     }
 
-    // The context's parameters are copied to shared memory first: the body
-    // reads them as often as it reads kernel parameters, and from global
-    // memory each read would be a load instruction of its own.
     template<class P, void (*BODY)(const P&, const VBlock&), int MAXT, int MINB>
-    __global__ void __launch_bounds__(MAXT, MINB) k_many(const P* __restrict__ ps, BatchMap map)
+    __global__ void __launch_bounds__(MAXT, MINB) k_many(const __grid_constant__ ManyArgs<P> a)
     {
-        static_assert(sizeof(P) % 4 == 0, "parameter structs are word-sized");
-        __shared__ __align__(16) unsigned int pbuf[sizeof(P)/4];
         VBlock vb;
-        const int m = batch_find(map, vb);
-        const unsigned int* src = reinterpret_cast<const unsigned int*>(ps + m);
-        const int tid = threadIdx.x + blockDim.x*(threadIdx.y + blockDim.y*threadIdx.z);
-        const int nt = blockDim.x*blockDim.y*blockDim.z;
-        for (int q = tid; q < (int)(sizeof(P)/4); q += nt) pbuf[q] = __ldg(src + q);
-        __syncthreads();
-        BODY(*reinterpret_cast<const P*>(pbuf), vb);
+        const int m = batch_find(a, vb);
+        BODY(a.p[m], vb);
     }
 
-    // One recorded launch of one context.
+    // One recorded launch of one context, with the layout of the k_many
+    // parameter struct it would join.
     struct RecordedLaunch
     {
         const void* fn;                       // the k_many entry point
         dim3 grid, block;
         size_t smem;
         std::vector<unsigned char> params;    // the bytes of P
+        int nmax;                             // ManyArgs<P>::NMAX
+        size_t args_size, off_grid, off_p, off_start, off_n;
     };
 
     // While set (host thread-local), launch_body records instead of launching.
@@ -128,6 +132,11 @@ namespace mhh
             l.grid = grid; l.block = block; l.smem = smem;
             l.params.resize(sizeof(P));
             std::memcpy(l.params.data(), &p, sizeof(P));
+            using A = ManyArgs<P>;
+            l.nmax = A::NMAX;
+            l.args_size = sizeof(A);
+            l.off_grid = offsetof(A, grid); l.off_p = offsetof(A, p);
+            l.off_start = offsetof(A, start); l.off_n = offsetof(A, n);
             r->launches.push_back(std::move(l));
             return;
         }

@@ -1426,13 +1426,10 @@ struct mhh_batch
         dim3 block;
         size_t smem;
         int nmem, nblocks;
-        void* params;          // device: nmem parameter structs
-        int* start;            // device: nmem + 1 block offsets
-        int4* grid;            // device: nmem grids
+        std::vector<unsigned char> args;   // the k_many parameter struct (ManyArgs)
     };
     int n;
     std::vector<Group> groups[3];
-    std::vector<void*> mem;
     // Groups of one stage (different contexts) run side by side: the extra
     // groups of a stage go to their own streams, forked from and joined into
     // the caller's stream.
@@ -1444,7 +1441,6 @@ namespace
 {
     void batch_free(mhh_batch* b)
     {
-        for (void* p : b->mem) cudaFree(p);
         for (auto st : b->side) cudaStreamDestroy(st);
         for (auto e : b->events) cudaEventDestroy(e);
         delete b;
@@ -1520,35 +1516,36 @@ int mhh_batch_create(int n, mhh_ctx* const* ctx, const mhh_substep_config* cfg, 
                         && L.block.z == L0.block.z && L.params.size() == L0.params.size())
                     { mem.push_back(m); done[m] = 1; }
                 }
-                mhh_batch::Group g{};
-                g.stage = (int)st;
-                g.fn = L0.fn; g.block = L0.block; g.nmem = (int)mem.size();
+                // One launch per chunk of at most nmax contexts (the kernel
+                // parameter space holds their parameter structs).
                 const size_t psz = L0.params.size();
-                std::vector<unsigned char> params(psz*mem.size());
-                std::vector<int> start(mem.size() + 1, 0);
-                std::vector<int4> grid(mem.size());
-                long long total = 0;
-                for (size_t q2=0; q2<mem.size(); ++q2)
+                for (size_t c0=0; c0<mem.size() && !rc; c0 += (size_t)L0.nmax)
                 {
-                    const mhh::RecordedLaunch& L = rec[mem[q2]][st];
-                    std::memcpy(params.data() + q2*psz, L.params.data(), psz);
-                    grid[q2] = make_int4((int)L.grid.x, (int)L.grid.y, (int)L.grid.z, 0);
-                    start[q2] = (int)total;
-                    total += (long long)L.grid.x*L.grid.y*L.grid.z;
-                    g.smem = std::max(g.smem, L.smem);
+                    const size_t nc = std::min(mem.size() - c0, (size_t)L0.nmax);
+                    mhh_batch::Group g{};
+                    g.stage = (int)st;
+                    g.fn = L0.fn; g.block = L0.block; g.nmem = (int)nc;
+                    g.args.assign(L0.args_size, 0);
+                    unsigned char* A = g.args.data();
+                    long long total = 0;
+                    for (size_t q2=0; q2<nc; ++q2)
+                    {
+                        const mhh::RecordedLaunch& L = rec[mem[c0 + q2]][st];
+                        std::memcpy(A + L0.off_p + q2*psz, L.params.data(), psz);
+                        const int4 gr = make_int4((int)L.grid.x, (int)L.grid.y, (int)L.grid.z, 0);
+                        std::memcpy(A + L0.off_grid + q2*sizeof(int4), &gr, sizeof(int4));
+                        const int st0 = (int)total;
+                        std::memcpy(A + L0.off_start + q2*sizeof(int), &st0, sizeof(int));
+                        total += (long long)L.grid.x*L.grid.y*L.grid.z;
+                        g.smem = std::max(g.smem, L.smem);
+                    }
+                    if (total <= 0 || total > 0x7fffffffLL) { rc = fail(MHH_ERR_UNSUPPORTED, "batch: grid too large"); break; }
+                    const int tot = (int)total, ncs = (int)nc;
+                    std::memcpy(A + L0.off_start + nc*sizeof(int), &tot, sizeof(int));
+                    std::memcpy(A + L0.off_n, &ncs, sizeof(int));
+                    g.nblocks = tot;
+                    b->groups[q].push_back(std::move(g));
                 }
-                start[mem.size()] = (int)total;
-                if (total <= 0 || total > 0x7fffffffLL) { rc = fail(MHH_ERR_UNSUPPORTED, "batch: grid too large"); break; }
-                g.nblocks = (int)total;
-                if (cudaMalloc(&g.params, params.size()) != cudaSuccess ||
-                    cudaMalloc((void**)&g.start, sizeof(int)*start.size()) != cudaSuccess ||
-                    cudaMalloc((void**)&g.grid, sizeof(int4)*grid.size()) != cudaSuccess)
-                { rc = fail(MHH_ERR_CUDA, "batch: cudaMalloc"); break; }
-                b->mem.push_back(g.params); b->mem.push_back(g.start); b->mem.push_back(g.grid);
-                cudaMemcpy(g.params, params.data(), params.size(), cudaMemcpyHostToDevice);
-                cudaMemcpy(g.start, start.data(), sizeof(int)*start.size(), cudaMemcpyHostToDevice);
-                cudaMemcpy(g.grid, grid.data(), sizeof(int4)*grid.size(), cudaMemcpyHostToDevice);
-                b->groups[q].push_back(g);
             }
         }
     }
@@ -1586,9 +1583,7 @@ int mhh_batch_substep(mhh_batch* b, int substep, cudaStream_t s)
     if (!b || substep < 0 || substep > 2) return fail(MHH_ERR_ARG, "bad argument");
     auto launch = [&](const mhh_batch::Group& g, cudaStream_t st)
     {
-        mhh::BatchMap map{g.start, g.grid, g.nmem};
-        const void* params = g.params;
-        void* args[] = {(void*)&params, (void*)&map};
+        void* args[] = {(void*)g.args.data()};
         return cudaLaunchKernel(g.fn, dim3(g.nblocks), g.block, args, g.smem, st) == cudaSuccess;
     };
     const auto& gs = b->groups[substep];
