@@ -10,14 +10,16 @@
 // index into its own (gx, gy, gz) grid.  A body therefore runs with the same
 // parameters and block positions in both, and gives the same results bit for
 // bit.  Both entry points take their parameters in the kernel parameter
-// space (up to 32 KB, __grid_constant__), which the compiler treats as
-// constant: a body reads them as cheaply in either.
+// space (up to 32 KB, __grid_constant__); k_many copies its block's struct
+// to shared memory first.
 //
 // launch_body() is the one launch site.  Normally it launches k_one.  While
 // a batch plan records a context's substep (BatchRecorder), it appends the
 // launch (the k_many symbol, the grid, block, shared memory and the bytes of
 // P) to the recording instead; the plan then groups equal k_many symbols of
-// the same stage into one launch.
+// the same stage into one launch.  A group of one context launches k_one
+// with its own grid: k_many's parameter struct is sized for NMAX contexts,
+// and the launch of a 32 KB parameter block costs more than its one body.
 #pragma once
 
 #include <cstddef>
@@ -82,12 +84,25 @@ namespace mhh
         BODY(p, vblock_self());
     }
 
+    // The block's parameters are staged in shared memory before the body
+    // runs: read through a run-time index into the parameter space they would
+    // be loads the compiler may not hoist across the body's global stores,
+    // which changes where it contracts products into FMAs and so the last bit
+    // of float results.  From shared memory the body compiles to the same
+    // arithmetic as in k_one.
     template<class P, void (*BODY)(const P&, const VBlock&), int MAXT, int MINB>
     __global__ void __launch_bounds__(MAXT, MINB) k_many(const __grid_constant__ ManyArgs<P> a)
     {
+        static_assert(sizeof(P) % 4 == 0, "parameter structs are word-sized");
+        __shared__ __align__(16) unsigned int pbuf[sizeof(P)/4];
         VBlock vb;
         const int m = batch_find(a, vb);
-        BODY(a.p[m], vb);
+        const unsigned int* src = reinterpret_cast<const unsigned int*>(&a.p[m]);
+        const int tid = threadIdx.x + blockDim.x*(threadIdx.y + blockDim.y*threadIdx.z);
+        const int nt = blockDim.x*blockDim.y*blockDim.z;
+        for (int q = tid; q < (int)(sizeof(P)/4); q += nt) pbuf[q] = src[q];
+        __syncthreads();
+        BODY(*reinterpret_cast<const P*>(pbuf), vb);
     }
 
     // One recorded launch of one context, with the layout of the k_many
@@ -95,6 +110,7 @@ namespace mhh
     struct RecordedLaunch
     {
         const void* fn;                       // the k_many entry point
+        const void* fn_one;                   // the k_one entry point
         dim3 grid, block;
         size_t smem;
         std::vector<unsigned char> params;    // the bytes of P
@@ -129,6 +145,7 @@ namespace mhh
         {
             RecordedLaunch l;
             l.fn = reinterpret_cast<const void*>(k_many<P, BODY, MAXT, MINB>);
+            l.fn_one = reinterpret_cast<const void*>(k_one<P, BODY, MAXT, MINB>);
             l.grid = grid; l.block = block; l.smem = smem;
             l.params.resize(sizeof(P));
             std::memcpy(l.params.data(), &p, sizeof(P));

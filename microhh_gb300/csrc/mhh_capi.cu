@@ -1425,8 +1425,9 @@ struct mhh_batch
         const void* fn;
         dim3 block;
         size_t smem;
-        int nmem, nblocks;
-        std::vector<unsigned char> args;   // the k_many parameter struct (ManyArgs)
+        int nmem;
+        dim3 grid;
+        std::vector<unsigned char> args;   // ManyArgs (k_many), or P of one context (k_one)
     };
     int n;
     std::vector<Group> groups[3];
@@ -1525,6 +1526,13 @@ int mhh_batch_create(int n, mhh_ctx* const* ctx, const mhh_substep_config* cfg, 
                     mhh_batch::Group g{};
                     g.stage = (int)st;
                     g.fn = L0.fn; g.block = L0.block; g.nmem = (int)nc;
+                    if (nc == 1)
+                    {
+                        const mhh::RecordedLaunch& L = rec[mem[c0]][st];
+                        g.fn = L.fn_one; g.grid = L.grid; g.smem = L.smem; g.args = L.params;
+                        b->groups[q].push_back(std::move(g));
+                        continue;
+                    }
                     g.args.assign(L0.args_size, 0);
                     unsigned char* A = g.args.data();
                     long long total = 0;
@@ -1543,7 +1551,7 @@ int mhh_batch_create(int n, mhh_ctx* const* ctx, const mhh_substep_config* cfg, 
                     const int tot = (int)total, ncs = (int)nc;
                     std::memcpy(A + L0.off_start + nc*sizeof(int), &tot, sizeof(int));
                     std::memcpy(A + L0.off_n, &ncs, sizeof(int));
-                    g.nblocks = tot;
+                    g.grid = dim3((unsigned)tot);
                     b->groups[q].push_back(std::move(g));
                 }
             }
@@ -1584,7 +1592,7 @@ int mhh_batch_substep(mhh_batch* b, int substep, cudaStream_t s)
     auto launch = [&](const mhh_batch::Group& g, cudaStream_t st)
     {
         void* args[] = {(void*)g.args.data()};
-        return cudaLaunchKernel(g.fn, dim3(g.nblocks), g.block, args, g.smem, st) == cudaSuccess;
+        return cudaLaunchKernel(g.fn, g.grid, g.block, args, g.smem, st) == cudaSuccess;
     };
     const auto& gs = b->groups[substep];
     for (size_t a=0; a<gs.size(); )
