@@ -642,7 +642,7 @@ int mhh_set_option(const char* name, int value)
     }
     if (!std::strcmp(name, "tdma_kernel"))
     {
-        if (value < -1 || value > 2) return fail(MHH_ERR_ARG, "tdma_kernel is -1, 0, 1 or 2");
+        if (value < -1 || value > 3) return fail(MHH_ERR_ARG, "tdma_kernel is -1, 0, 1, 2 or 3");
         set_tdma_variant(value);
         return MHH_OK;
     }
@@ -690,7 +690,7 @@ int mhh_ctx_set_option(mhh_ctx* c, const char* name, int value)
     }
     else if (!std::strcmp(name, "tdma_kernel"))
     {
-        if (!reset && (value < -1 || value > 2)) return fail(MHH_ERR_ARG, "tdma_kernel is -2, -1, 0, 1 or 2");
+        if (!reset && (value < -1 || value > 3)) return fail(MHH_ERR_ARG, "tdma_kernel is -2, -1, 0, 1, 2 or 3");
         c->opt_tdma = value;
     }
     else if (!std::strcmp(name, "tendency_kchunk") || !std::strcmp(name, "viscosity_kchunk"))
@@ -910,7 +910,7 @@ int mhh_ctx_destroy(mhh_ctx* c)
     // stream reaches it; the caller has finished its own work on the fields.
     for (auto& p : c->dprof) if (p) cudaFreeAsync(p, c->setup);
     fft_plan_free(&c->pw.px, c->setup); fft_plan_free(&c->pw.py, c->setup);
-    void* ptrs[] = {c->pw.pk, c->pw.work, c->pw.dcm, c->pw.rtab, c->pw.wtab, c->pw.gtab, c->pw.htab, c->pw.stab, c->pw.stabd, c->pw.bmati, c->pw.bmatj, c->pw.a, c->pw.c, c->pw.dz2, c->pw.dz2rho,
+    void* ptrs[] = {c->pw.pk, c->pw.work, c->pw.dcm, c->pw.rtab, c->pw.wtab, c->pw.gtab, c->pw.htab, c->pw.stab, c->pw.stabd, c->pw.gftab, c->pw.hftab, c->pw.fmode, c->pw.bmati, c->pw.bmatj, c->pw.a, c->pw.c, c->pw.dz2, c->pw.dz2rho,
                     c->red, c->statbuf, c->bufprof, c->sw.fm, c->sw.fh, c->sw.phim, c->sw.phih, c->sw.ustar, c->sw.obuk, c->sw.dudz, c->sw.dvdz, c->sw.dbdz, c->sw.dutot,
                     c->sw.nobuk, c->sw.zL, c->sw.f, c->sw.mlen2, c->sw.mlen2f};
     for (void* p : ptrs) if (p) cudaFreeAsync(p, c->setup);

@@ -141,13 +141,18 @@ namespace mhh
         double* htab;         // same shape: backward coefficient of the rescaled recurrence
         float* stab;          // same shape: output scale dz^2/den in float
         double* stabd;        // same shape: output scale dz^2/den
+        float* gftab;         // same shape: gtab in float
+        float* hftab;         // same shape: htab in float
+        unsigned char* fmode; // (itot/2+1)*(jtot/2+1): 1 where the group's recurrence may run in float
         void* dcm;            // ktot values (TF): each level's mean, (X_00/jtot)/itot
         int niu, nju;
     };
 
     // Tridiagonal kernel choice: 0 = the reference's operation order,
-    // 1 = the rescaled recurrence (two FP64 FMAs per cell); -1 = automatic
-    // (0 for double fields, 1 for float fields).
+    // 1 = the rescaled recurrence (two FP64 FMAs per cell), 2 = the same with
+    // four columns per thread, 3 = the rescaled recurrence in float for the
+    // column groups whose sweeps damp (float fields only; 1 for double
+    // fields); -1 = automatic (0 for double fields, 3 for float fields).
     int tdma_variant();
     void set_tdma_variant(int v);
     // Complex sequence pairs per block of the column (y) FFT: 4 or 8.

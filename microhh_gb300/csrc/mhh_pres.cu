@@ -1075,12 +1075,16 @@ namespace mhh
     // (k_tdma_col) needs two FMAs per cell, with one thread per column
     // (k_tdma_scaled: the same with four columns per thread).
     // ---------------------------------------------------------------------
+    constexpr double TDMA_FLOAT_GAMMA = 0.999;
+
     __global__ void k_tdma_table(int niu, int nju, int ktot, const double* __restrict__ bmati,
                                  const double* __restrict__ bmatj, const double* __restrict__ a,
                                  const double* __restrict__ c, const double* __restrict__ dz2rho,
                                  const double* __restrict__ dz2, double* __restrict__ rtab,
                                  double* __restrict__ wtab, double* __restrict__ gtab, double* __restrict__ htab,
-                                 float* __restrict__ stab, double* __restrict__ stabd)
+                                 float* __restrict__ stab, double* __restrict__ stabd,
+                                 float* __restrict__ gftab, float* __restrict__ hftab,
+                                 unsigned char* __restrict__ fmode)
     {
         const int iu = blockIdx.x*blockDim.x + threadIdx.x;
         const int ju = blockIdx.y;
@@ -1118,6 +1122,26 @@ namespace mhh
             gtab[base + k*stride] = k ? a[k]*(dz2[k-1]/rtab[base + (k-1)*stride])/dz2[k] : 0.;
             htab[base + k*stride] = k < ktot-1 ? c[k]*(dz2[k+1]/rtab[base + (k+1)*stride])/dz2[k] : 0.;
         }
+        // Float sweeps where the forward sweep damps: a rounding error of z_k
+        // enters the next level multiplied by g_{k+1}, and as |g| -> 1 (small
+        // |lambda| dz^2: the largest horizontal scales) the forward values
+        // become running sums whose round-off grows with the level.  With
+        // max |g| <= TDMA_FLOAT_GAMMA the float solve of a column stays
+        // within about ten float roundings of its largest value (measured on
+        // 256 uniform levels with random right-hand sides: 9 ulp at |g| =
+        // 0.999, 4 ulp at 0.9).  The large backward factor h at the top
+        // level (the Neumann row) multiplies a value that s scales down, and
+        // adds no more.  The groups above the bound and the mean mode keep
+        // FP64.
+        double gam = 0.;
+        for (int k=0; k<ktot; ++k)
+        {
+            const double g = gtab[base + k*stride], h = htab[base + k*stride];
+            gftab[base + k*stride] = float(g);
+            hftab[base + k*stride] = float(h);
+            gam = fmax(gam, fabs(g));
+        }
+        fmode[base] = (!mean_mode && gam <= TDMA_FLOAT_GAMMA) ? 1 : 0;
     }
 
     // The k loops run in batches of levels (TDMA_KF forward, TDMA_KBK
@@ -1148,6 +1172,8 @@ namespace mhh
         const float* stab;
         const double* stabd;
         TF* pk; double* work; TF* dcm;
+        const float *gftab, *hftab;
+        const unsigned char* fmode;
     };
 
     template<typename TF>
@@ -1395,16 +1421,16 @@ namespace mhh
     constexpr int TDC_KF = 8;
     constexpr int TDC_KB = 4;
 
+    template<typename TF>
+    __device__ __forceinline__ void tdma_col_fp64(const TdmaP<TF>& A, int col, long long base);
+
     // At most 64 registers, so that eight blocks (32 warps) fit on an SM:
     // the loads of one warp's next levels overlap the FP64 recurrences of
     // the others.
     template<typename TF>
     __device__ __forceinline__ void tdma_col_body(const TdmaP<TF>& A, const VBlock& vb)
     {
-        const int itot = A.itot, jtot = A.jtot, ktot = A.ktot, niu = A.niu, nju = A.nju;
-        const double* __restrict__ gtab = A.gtab; const double* __restrict__ htab = A.htab;
-        const float* __restrict__ stab = A.stab; const double* __restrict__ stabd = A.stabd;
-        TF* __restrict__ pk = A.pk; double* __restrict__ work = A.work; TF* __restrict__ dcm = A.dcm;
+        const int itot = A.itot, jtot = A.jtot, niu = A.niu;
         const int t = vb.x*blockDim.x + threadIdx.x;
         const int iu = t >> 2, q = t & 3;
         const int ju = vb.y;
@@ -1415,9 +1441,20 @@ namespace mhh
         // that coincides with the first column has no lane.
         if (((q & 1) && i1 < 0) || ((q & 2) && j1 < 0)) return;
         const int col = ((q & 1) ? i1 : iu) + ((q & 2) ? j1 : ju)*itot;
-        const long long stride = (long long)niu*nju;
+        tdma_col_fp64<TF>(A, col, iu + (long long)ju*niu);
+    }
+
+    // One column's rescaled solve with the elimination in FP64 (forward
+    // values in the FP64 work array).
+    template<typename TF>
+    __device__ __forceinline__ void tdma_col_fp64(const TdmaP<TF>& A, int col, long long base)
+    {
+        const int itot = A.itot, jtot = A.jtot, ktot = A.ktot;
+        const double* __restrict__ gtab = A.gtab; const double* __restrict__ htab = A.htab;
+        const float* __restrict__ stab = A.stab; const double* __restrict__ stabd = A.stabd;
+        TF* __restrict__ pk = A.pk; double* __restrict__ work = A.work; TF* __restrict__ dcm = A.dcm;
+        const long long stride = (long long)A.niu*A.nju;
         const long long kk = (long long)itot*jtot;
-        const long long base = iu + (long long)ju*niu;
 
         // Forward: z_k = p_k - g_k z_{k-1}.
         double z = 0.;
@@ -1473,6 +1510,87 @@ namespace mhh
         }
     }
 
+    // The rescaled solve in float for the column groups whose sweeps damp
+    // (fmode, set with the tables), in FP64 for the others.  A float column
+    // keeps its forward values in pk itself, where the backward sweep
+    // overwrites them with the solution: 16 bytes per cell move instead of
+    // 24 (float right-hand side and solution, FP64 work array), the tables
+    // are read in float, no FP64 instruction runs, and the loads run sixteen
+    // levels ahead of the recurrence.  Lanes as in k_tdma_col; a group's
+    // four lanes take the same branch.
+    constexpr int TDF_KF = 16;
+    constexpr int TDF_KB = 8;
+
+    __device__ __forceinline__ void tdma_mixed_body(const TdmaP<float>& A, const VBlock& vb)
+    {
+        const int itot = A.itot, jtot = A.jtot, ktot = A.ktot, niu = A.niu;
+        const int t = vb.x*blockDim.x + threadIdx.x;
+        const int iu = t >> 2, q = t & 3;
+        const int ju = vb.y;
+        if (iu >= niu) return;
+        const int i1 = (iu == 0 || 2*iu == itot) ? -1 : itot - iu;
+        const int j1 = (ju == 0 || 2*ju == jtot) ? -1 : jtot - ju;
+        if (((q & 1) && i1 < 0) || ((q & 2) && j1 < 0)) return;
+        const int col = ((q & 1) ? i1 : iu) + ((q & 2) ? j1 : ju)*itot;
+        const long long base = iu + (long long)ju*niu;
+        if (!A.fmode[base])
+        {
+            tdma_col_fp64<float>(A, col, base);
+            return;
+        }
+        const float* __restrict__ gf = A.gftab; const float* __restrict__ hf = A.hftab;
+        const float* __restrict__ stab = A.stab;
+        float* __restrict__ pk = A.pk;
+        const long long stride = (long long)niu*A.nju;
+        const long long kk = (long long)itot*jtot;
+
+        // Forward: z_k = p_k - g_k z_{k-1}, stored over p_k.
+        float z = 0.f;
+        for (int k0=0; k0<ktot; k0+=TDF_KF)
+        {
+            const int nk = min(TDF_KF, ktot - k0);
+            float g[TDF_KF], pv[TDF_KF];
+            #pragma unroll
+            for (int b=0; b<TDF_KF; ++b)
+                if (b < nk)
+                {
+                    g[b] = __ldg(gf + base + (long long)(k0 + b)*stride);
+                    pv[b] = pk[col + (long long)(k0 + b)*kk];
+                }
+            #pragma unroll
+            for (int b=0; b<TDF_KF; ++b)
+                if (b < nk)
+                {
+                    z = fmaf(-g[b], z, pv[b]);
+                    pk[col + (long long)(k0 + b)*kk] = z;
+                }
+        }
+        // Backward: xi_k = z_k - h_k xi_{k+1}; x_k = s_k xi_k.
+        pk[col + (long long)(ktot - 1)*kk] = z*__ldg(stab + base + (long long)(ktot - 1)*stride);
+        float xi = z;
+        for (int k0=ktot-2; k0>=0; k0-=TDF_KB)
+        {
+            const int nk = min(TDF_KB, k0 + 1);
+            float h[TDF_KB], sv[TDF_KB], zv[TDF_KB];
+            #pragma unroll
+            for (int b=0; b<TDF_KB; ++b)
+                if (b < nk)
+                {
+                    const long long k = k0 - b;
+                    h[b] = __ldg(hf + base + k*stride);
+                    sv[b] = __ldg(stab + base + k*stride);
+                    zv[b] = pk[col + k*kk];
+                }
+            #pragma unroll
+            for (int b=0; b<TDF_KB; ++b)
+                if (b < nk)
+                {
+                    xi = fmaf(-h[b], xi, zv[b]);
+                    pk[col + (long long)(k0 - b)*kk] = xi*sv[b];
+                }
+        }
+    }
+
     int tdma_table(PresWork& pw, int itot, int jtot, int ktot, cudaStream_t s)
     {
         pw.niu = itot/2 + 1;
@@ -1484,9 +1602,13 @@ namespace mhh
         if (cudaMallocAsync((void**)&pw.htab, sizeof(double)*n, s) != cudaSuccess) return MHH_ERR_CUDA;
         if (cudaMallocAsync((void**)&pw.stab, sizeof(float)*n, s) != cudaSuccess) return MHH_ERR_CUDA;
         if (cudaMallocAsync((void**)&pw.stabd, sizeof(double)*n, s) != cudaSuccess) return MHH_ERR_CUDA;
+        if (cudaMallocAsync((void**)&pw.gftab, sizeof(float)*n, s) != cudaSuccess) return MHH_ERR_CUDA;
+        if (cudaMallocAsync((void**)&pw.hftab, sizeof(float)*n, s) != cudaSuccess) return MHH_ERR_CUDA;
+        if (cudaMallocAsync((void**)&pw.fmode, (size_t)pw.niu*pw.nju, s) != cudaSuccess) return MHH_ERR_CUDA;
         dim3 grid((pw.niu + 127)/128, pw.nju);
         k_tdma_table<<<grid, 128, 0, s>>>(pw.niu, pw.nju, ktot, pw.bmati, pw.bmatj, pw.a, pw.c, pw.dz2rho, pw.dz2,
-                                    pw.rtab, pw.wtab, pw.gtab, pw.htab, pw.stab, pw.stabd);
+                                    pw.rtab, pw.wtab, pw.gtab, pw.htab, pw.stab, pw.stabd, pw.gftab, pw.hftab,
+                                    pw.fmode);
         count_launch();
         return cudaStreamSynchronize(s) == cudaSuccess ? MHH_OK : MHH_ERR_CUDA;
     }
@@ -1496,9 +1618,20 @@ namespace mhh
     {
         dim3 grid((pw.niu + 127)/128, pw.nju);
         TF* dcm = static_cast<TF*>(pw.dcm);
-        const int v = o.tdma < 0 ? (sizeof(TF) == 4 ? 1 : 0) : o.tdma;
+        int v = o.tdma < 0 ? (sizeof(TF) == 4 ? 3 : 0) : o.tdma;
+        if (v == 3 && sizeof(TF) == 8) v = 1;
         const TdmaP<TF> A{d.itot, d.jtot, d.ktot, pw.niu, pw.nju, pw.rtab, pw.wtab, pw.a, pw.dz2, pw.gtab, pw.htab,
-                          pw.stab, pw.stabd, pk, pw.work, dcm};
+                          pw.stab, pw.stabd, pk, pw.work, dcm, pw.gftab, pw.hftab, pw.fmode};
+        if constexpr (sizeof(TF) == 4)
+        {
+            if (v == 3)
+            {
+                dim3 gridc((4*pw.niu + 127)/128, pw.nju);
+                launch_body<TdmaP<float>, tdma_mixed_body, 128, 8>(gridc, dim3(128), 0, s, A);
+                count_launch();
+                return;
+            }
+        }
         if (v == 1)
         {
             dim3 gridc((4*pw.niu + 127)/128, pw.nju);
