@@ -388,6 +388,136 @@ namespace mhh
     // The float transform with the fused right-hand side keeps five blocks
     // per SM (at most 51 registers): its batched loads need the residency to
     // cover the latency of HBM.
+    // ---- warp-synchronous 512-point schedule --------------------------------
+    // For n = 512 = 8 x 64 one warp transforms one complex sequence with a
+    // single block-wide dependency (its input tile): a decimation-in-
+    // frequency radix-8 stage splits the sequence into eight 64-point
+    // sub-sequences,
+    //   s_r[i] = w512^(i r) DFT8_q(z[i + 64 q])[r],  X[8K + r] = DFT64(s_r)[K],
+    // and each 64-point transform runs as 8 x 8 within the warp:
+    //   A[t][k1] = w64^(t k1) DFT8_m(s_r[t + 8 m])[k1],
+    //   X_r[k1 + 8 k2] = DFT8_t(A[t][k1])[k2].
+    // The exchanges between the three radix-8 passes go through the warp's
+    // own shared-memory region with __syncwarp (an 8 x 8 transpose among
+    // eight lanes is 16 shared accesses per lane; with __shfl_xor_sync it is
+    // 24 shuffles and 48 selects), so a tile needs block barriers only after
+    // its load and before its store, against one per stage in the Stockham
+    // schedule.  The last pass writes the natural order over the warp's own
+    // real input, which no other warp reads.
+    //
+    // Positions within a sub-sequence block: rows of eight complex elements,
+    // row index XOR (r & 1) and column index XOR row, so that eight lanes
+    // reading a row or a column, and the four sub-blocks a warp touches at
+    // once, spread over all banks.
+    __device__ __forceinline__ int w512_pos(int r, int row, int col)
+    {
+        return r*64 + ((row ^ (r & 1)) << 3) + (col ^ row);
+    }
+
+    // Twiddles of the schedule, n entries in shared memory: w512^(i r) at
+    // (r-1)*64 + i for r = 1..7, i = 0..63, then w64^(t k1) = w512^(8 t k1)
+    // at 448 + k1*8 + t.
+    template<typename TF>
+    __device__ __forceinline__ void w512_twiddles(typename C2<TF>::T* tw, const TF* __restrict__ twt)
+    {
+        using T2 = typename C2<TF>::T;
+        for (int e = threadIdx.x; e < 512; e += blockDim.x)
+        {
+            const int idx = e < 448 ? ((e & 63)*((e >> 6) + 1)) & 511 : (8*(e & 7)*((e - 448) >> 3)) & 511;
+            T2 w; w.x = twt[2*idx]; w.y = twt[2*idx + 1];
+            tw[e] = w;
+        }
+    }
+
+    // Complex input element k of the pair (hx, hy): z = x + i y (forward) or
+    // the conjugated halfcomplex pair (inverse), as in the first Stockham
+    // stage.
+    template<typename TF, bool INV, int N>
+    __device__ __forceinline__ typename C2<TF>::T pair_in(const TF* __restrict__ hx, const TF* __restrict__ hy, int k)
+    {
+        typename C2<TF>::T u;
+        if (!INV)
+        {
+            u.x = hx[k]; u.y = hy[k];
+        }
+        else
+        {
+            const int kk = k <= N/2 ? k : N - k;
+            const bool real_only = (kk == 0) || (2*kk == N);
+            const TF sg = k <= N/2 ? TF(1) : TF(-1);
+            const int km = real_only ? kk : N - kk;
+            const TF xr = hx[kk], yr = hy[kk];
+            const TF xi = real_only ? TF(0) : sg*hx[km];
+            const TF yi = real_only ? TF(0) : sg*hy[km];
+            u.x = xr - yi;
+            u.y = -(xi + yr);
+        }
+        return u;
+    }
+
+    // The transform of complex sequence q (warp q; q < P) of a tile whose
+    // 2P real sequences sit at rin + s*ns.  work holds P regions of 512
+    // complex elements at stride ss.  On return (after __syncwarp) the
+    // natural-order result of sequence q is at reinterpret_cast<T2*>(rin +
+    // 2q*ns).
+    template<typename TF, bool INV>
+    __device__ __forceinline__ void fft512_warp(TF* rin, int ns, typename C2<TF>::T* work, int ss,
+                                                const typename C2<TF>::T* __restrict__ tw, int P)
+    {
+        using T2 = typename C2<TF>::T;
+        const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        if (q >= P) return;
+        const TF* hx = rin + (2*q)*ns;
+        const TF* hy = hx + ns;
+        T2* z = work + q*ss;
+        // Pass 1: radix 8 over stride 64, twiddles w512^(i r).
+        #pragma unroll
+        for (int h=0; h<2; ++h)
+        {
+            const int i = lane + 32*h;
+            T2 u[8];
+            #pragma unroll
+            for (int b=0; b<8; ++b) u[b] = pair_in<TF, INV, 512>(hx, hy, i + 64*b);
+            dft8<TF, T2>(u);
+            #pragma unroll
+            for (int r=1; r<8; ++r) u[r] = cmul(u[r], tw[(r - 1)*64 + i]);
+            #pragma unroll
+            for (int r=0; r<8; ++r) z[w512_pos(r, i >> 3, i & 7)] = u[r];
+        }
+        __syncwarp();
+        // Pass 2: radix 8 over m within each sub-sequence, twiddles w64^(t k1),
+        // in place (a lane's writes are the elements it read).
+        #pragma unroll
+        for (int h=0; h<2; ++h)
+        {
+            const int pp = lane + 32*h, r = pp >> 3, t = pp & 7;
+            T2 a[8];
+            #pragma unroll
+            for (int m=0; m<8; ++m) a[m] = z[w512_pos(r, m, t)];
+            dft8<TF, T2>(a);
+            #pragma unroll
+            for (int k1=1; k1<8; ++k1) a[k1] = cmul(a[k1], tw[448 + k1*8 + t]);
+            #pragma unroll
+            for (int k1=0; k1<8; ++k1) z[w512_pos(r, k1, t)] = a[k1];
+        }
+        __syncwarp();
+        // Pass 3: radix 8 over t; X[r + 8 k1 + 64 k2] in natural order over
+        // the warp's real input (read only by this warp, in pass 1).
+        T2* out = reinterpret_cast<T2*>(rin + (2*q)*ns);
+        #pragma unroll
+        for (int h=0; h<2; ++h)
+        {
+            const int pp = lane + 32*h, r = pp >> 3, k1 = pp & 7;
+            T2 a[8];
+            #pragma unroll
+            for (int t=0; t<8; ++t) a[t] = z[w512_pos(r, k1, t)];
+            dft8<TF, T2>(a);
+            #pragma unroll
+            for (int k2=0; k2<8; ++k2) out[r + 8*k1 + 64*k2] = a[k2];
+        }
+        __syncwarp();
+    }
+
     template<typename TF> struct FftP { FftPlan pl; TF* data; SeqLayout L; int Prt; TF scale; FftFuse<TF> fz; };
     template<typename TF, int FUSE> struct FftOcc { static constexpr int v = (FUSE == 1 && sizeof(TF) == 4) ? 5 : 1; };
 
@@ -415,7 +545,9 @@ namespace mhh
         const long long s0 = (long long)vb.x*2*P;
         const int nloc = (int)min((long long)2*P, L.nseq - s0);
 
-        if (NFIX)
+        constexpr bool WARP = NFIX == 512;
+        if (WARP) w512_twiddles<TF>(tws, twtab<TF>(pl));
+        else if (NFIX)
         {
             const TF* tt = twtab<TF>(pl);
             for (int e = threadIdx.x; e < n; e += blockDim.x)
@@ -520,6 +652,18 @@ namespace mhh
         asm volatile("cp.async.wait_group 0;\n" ::: "memory");
         __syncthreads();
 
+        // 2-3. With n = 512 the warp-synchronous schedule, whose result is
+        //      the natural order over each sequence pair's real input.
+        T2* res;
+        T2* other;
+        if constexpr (WARP)
+        {
+            fft512_warp<TF, INV>(r1, ns, buf0, n, tws, P);
+            __syncthreads();
+            res = nullptr; other = buf0;
+        }
+        else
+        {
         // 2. Complex input: z = x + i y (forward) or conj(X + i Y) (inverse).
         for (int e = threadIdx.x; e < P*n; e += blockDim.x)
         {
@@ -547,8 +691,6 @@ namespace mhh
         __syncthreads();
 
         // 3. FFT.
-        T2* res;
-        T2* other;
         if (NFIX)
         {
             T2* src = buf0;
@@ -562,6 +704,7 @@ namespace mhh
             res = which ? buf1 : buf0;
             other = which ? buf0 : buf1;
         }
+        }
         TF* rout = reinterpret_cast<TF*>(other);
 
         // 4. Real outputs into the other buffer, [2P][n].
@@ -570,11 +713,12 @@ namespace mhh
             const int q = e / n, k = e - q*n;
             TF* ox = rout + (2*q)*ns;
             TF* oy = rout + (2*q+1)*ns;
+            const T2* rq = WARP ? reinterpret_cast<const T2*>(r1 + (2*q)*ns) : res + q*n;
             if (!INV)
             {
                 if (k <= n/2)
                 {
-                    const T2 a = res[q*n + k], b = res[q*n + (n - k) % n];
+                    const T2 a = rq[k], b = rq[(n - k) % n];
                     const TF xr = TF(0.5)*(a.x + b.x), xi = TF(0.5)*(a.y - b.y);
                     const TF yr = TF(0.5)*(a.y + b.y), yi = TF(-0.5)*(a.x - b.x);
                     ox[k] = xr; oy[k] = yr;
@@ -583,7 +727,7 @@ namespace mhh
             }
             else
             {
-                const T2 a = res[q*n + k];
+                const T2 a = rq[k];
                 ox[k] = a.x*scale;
                 oy[k] = -a.y*scale;
             }
@@ -722,6 +866,23 @@ namespace mhh
         return yseq ? TF(-0.5)*(a.x - b.x) : TF(0.5)*(a.y - b.y);
     }
 
+    // The same from a natural-order complex result rq of the pair (yseq: the
+    // pair's second real sequence).
+    template<typename TF, bool INV, int N>
+    __device__ __forceinline__ TF fft_real_nat(const typename C2<TF>::T* __restrict__ rq, int yseq, int k, TF scale)
+    {
+        using T2 = typename C2<TF>::T;
+        if (INV)
+        {
+            const T2 a = rq[k];
+            return yseq ? -a.y*scale : a.x*scale;
+        }
+        const int kk = k <= N/2 ? k : N - k;
+        const T2 a = rq[kk], b = rq[kk == 0 ? 0 : N - kk];
+        if (k <= N/2) return yseq ? TF(0.5)*(a.y + b.y) : TF(0.5)*(a.x + b.x);
+        return yseq ? TF(-0.5)*(a.x - b.x) : TF(0.5)*(a.y - b.y);
+    }
+
     template<typename TF> struct FftpP { TF* data; SeqLayout L; TF scale; FftFuse<TF> fz; const TF* twt; long long ntiles; };
 
     template<typename TF, bool INV, int N, int P, int FUSE, bool ROWS>
@@ -741,8 +902,11 @@ namespace mhh
         T2* bufs = reinterpret_cast<T2*>(smem_raw);
         T2* work = bufs + BUF;
         T2* tws = bufs + 3*BUF;
-        for (int e = threadIdx.x; e < N; e += blockDim.x)
-        { T2 w; w.x = twt[2*e]; w.y = twt[2*e+1]; tws[e] = w; }
+        constexpr bool WARP = N == 512;
+        if (WARP) w512_twiddles<TF>(tws, twt);
+        else
+            for (int e = threadIdx.x; e < N; e += blockDim.x)
+            { T2 w; w.x = twt[2*e]; w.y = twt[2*e+1]; tws[e] = w; }
 
         // Asynchronous copies of tile t into input buffer b (a missing
         // sequence reads as zero).  Each thread computes the base of the
@@ -794,13 +958,31 @@ namespace mhh
                 tile_index<TF>(x, L, fz, s0, (int)min((long long)2*P, L.nseq - s0), N, true);
             }
 
-            // The swizzle pays off for rows; the padded column stride
-            // already spreads the column stores.
-            fft_first_stage<TF, INV, N, P, NS, SS, ROWS>(reinterpret_cast<const TF*>(in), work, tws);
-            T2* src = work;
-            T2* dst = in;
-            FixedStages<TF, N, P, 1, fixed_radix(N, 0), SS, ROWS>::run(src, dst, tws);
-            const T2* res = src;
+            const T2* res = work;
+            TF* inr = reinterpret_cast<TF*>(in);
+            if constexpr (WARP)
+            {
+                fft512_warp<TF, INV>(inr, NS, work, SS, tws, P);
+                __syncthreads();
+            }
+            else
+            {
+                // The swizzle pays off for rows; the padded column stride
+                // already spreads the column stores.
+                fft_first_stage<TF, INV, N, P, NS, SS, ROWS>(inr, work, tws);
+                T2* src = work;
+                T2* dst = in;
+                FixedStages<TF, N, P, 1, fixed_radix(N, 0), SS, ROWS>::run(src, dst, tws);
+                res = src;
+            }
+            // Real output k of real sequence ls of the tile.
+            auto out_at = [&](int ls, int k) -> TF
+            {
+                if constexpr (WARP)
+                    return fft_real_nat<TF, INV, N>(reinterpret_cast<const T2*>(inr + (ls & ~1)*NS), ls & 1, k, scale);
+                else
+                    return fft_real_out<TF, INV, N, SS, ROWS>(res, ls, k, scale);
+            };
 
             const long long s0 = t*2*P;
             const int nloc = (int)min((long long)2*P, L.nseq - s0);
@@ -813,7 +995,7 @@ namespace mhh
                     const int ls = e / N, i = e - ls*N;
                     if (ls < nloc)
                     {
-                        TF val = fft_real_out<TF, INV, N, SS, ROWS>(res, ls, i, scale);
+                        TF val = out_at(ls, i);
                         if (fz.dcm) val = add_rn(val, fz.dcm[x.sk[ls]]);
                         const long long c = x.sc[ls] + i;
                         fz.p[c] = val;
@@ -826,7 +1008,7 @@ namespace mhh
                 for (int e = threadIdx.x; e < 2*P*N; e += blockDim.x)
                 {
                     const int ls = e / N, j = e - ls*N;
-                    if (ls < nloc) data[(s0 + ls)*(long long)N + j] = fft_real_out<TF, INV, N, SS, ROWS>(res, ls, j, scale);
+                    if (ls < nloc) data[(s0 + ls)*(long long)N + j] = out_at(ls, j);
                 }
             }
             else
@@ -837,7 +1019,7 @@ namespace mhh
                     const long long st = (long long)(blockDim.x/(2*P))*L.itot;
                     TF* dp = data + seq_base(L, s0 + ls, N) + (long long)(threadIdx.x/(2*P))*L.itot;
                     for (int j = threadIdx.x/(2*P); j < N; j += blockDim.x/(2*P), dp += st)
-                        *dp = fft_real_out<TF, INV, N, SS, ROWS>(res, ls, j, scale);
+                        *dp = out_at(ls, j);
                 }
             }
             cur ^= 1;
@@ -849,8 +1031,9 @@ namespace mhh
     static void launch_fftp(const FftPlan& pl, TF* data, SeqLayout L, TF scale, const FftFuse<TF>& fz, cudaStream_t s)
     {
         using T2 = typename C2<TF>::T;
-        // 8 pairs (16 columns, 64-byte rows of a tile) run with 512 threads.
-        constexpr int NT = P == 8 ? 512 : 256;
+        // 8 pairs (16 columns, 64-byte rows of a tile) run with 512 threads;
+        // the warp-synchronous 512-point schedule with one warp per pair.
+        constexpr int NT = N == 512 ? 32*P : (P == 8 ? 512 : 256);
         const size_t smem = sizeof(T2)*((size_t)3*fftp_buf(N, P, ROWS) + N);
         const long long ntiles = (L.nseq + 2*P - 1) / (2*P);
         // Attribute and residency are set once per kernel, outside any stream

@@ -380,6 +380,55 @@ def test_fft_roundtrip_and_dft(mhh, itot, jtot):
     del X
 
 
+@pytest.mark.parametrize("pipe", [1, 0], ids=["prefetching", "tile_per_block"])
+@pytest.mark.parametrize("precision", [64, 32], ids=["fp64", "fp32"])
+def test_fft512_warp_schedule(mhh, precision, pipe):
+    """The warp-synchronous 512-point schedule (rows and columns, both FFT
+    kernels) against numpy's DFT in halfcomplex order, and the inverse pair
+    returning itot*jtot times the input."""
+    import ctypes
+    import torch
+    itot = jtot = 512
+    ktot = 3
+    desc = mhh.GridDesc(itot, jtot, ktot, 1, 1, 1, 1.0, 1.0, 1.0)
+    phys = mhh.Physics(visc=1e-5, svisc=1e-5, cs=0.23, tpr=1/3., dnmax=0.4, swmason=1, cflmax=1.,
+                       thref0=300., thermo=0, surface=0, z0m=0.1, z0h=0.1)
+    z = np.linspace(0.1, 0.9, ktot)
+    h = ctypes.c_void_p()
+    kern, _ = mhh.load()
+    mhh.check(kern.mhh_ctx_create(ctypes.byref(desc), z.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                  precision, ctypes.byref(phys), ctypes.byref(h)))
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal((ktot, jtot, itot))
+    dt = torch.float64 if precision == 64 else torch.float32
+    # Float: the transforms' round-off, a few eps times log2(512).
+    tol = 1e-12 if precision == 64 else 3e-6
+    mhh.set_option("fft_pipeline", pipe)
+    try:
+        t = torch.tensor(x, dtype=dt, device="cuda")
+        mhh.check(kern.mhh_fft_forward(h, ctypes.c_void_p(t.data_ptr()), None))
+        torch.cuda.synchronize()
+        got = t.double().cpu().numpy()
+        # Halfcomplex along x, then along y of those rows.
+        ref = x if precision == 64 else x.astype(np.float32).astype(np.float64)
+        Fx = np.fft.fft(ref, axis=2)
+        hx = np.empty_like(x)
+        hx[:, :, :itot // 2 + 1] = Fx[:, :, :itot // 2 + 1].real
+        hx[:, :, itot // 2 + 1:] = Fx[:, :, 1:itot // 2][:, :, ::-1].imag
+        Fy = np.fft.fft(hx, axis=1)
+        exp = np.empty_like(x)
+        exp[:, :jtot // 2 + 1, :] = Fy[:, :jtot // 2 + 1, :].real
+        exp[:, jtot // 2 + 1:, :] = Fy[:, 1:jtot // 2, :][:, ::-1, :].imag
+        assert np.abs(got - exp).max() <= tol * np.abs(exp).max()
+        mhh.check(kern.mhh_fft_backward(h, ctypes.c_void_p(t.data_ptr()), None))
+        torch.cuda.synchronize()
+        back = t.double().cpu().numpy()
+        assert np.abs(back - itot * jtot * ref).max() <= tol * itot * jtot * np.abs(ref).max()
+    finally:
+        mhh.set_option("fft_pipeline", 1)
+        kern.mhh_ctx_destroy(h)
+
+
 def test_divergence_after_projection(mhh):
     case = cases.drycbl(48, 32, 24, 4800., 3200., 2400., seed=41, noise_z=800.)
     # FP32: the FFTs and the gradient run in float (eps 6e-8 times the
@@ -450,7 +499,8 @@ def test_pressure_fusion_is_bitwise(mhh, precision):
     the same fields bit for bit as the separate kernels (a fixed FFT length
     and a run-time-plan length)."""
     for case in (cases.drycbl(40, 24, 20, 4000., 2400., 2000., seed=63, noise_z=600.),
-                 cases.drycbl(60, 40, 24, 6000., 4000., 2400., seed=64, noise_z=600.)):
+                 cases.drycbl(60, 40, 24, 6000., 4000., 2400., seed=64, noise_z=600.),
+                 cases.drycbl(512, 512, 6, 25600., 25600., 600., seed=67, noise_z=400.)):
         out = []
         for fuse in (0, 1):
             mhh.set_option("pres_fuse", fuse)
@@ -467,10 +517,11 @@ def test_pressure_fusion_is_bitwise(mhh, precision):
 @pytest.mark.parametrize("precision", [64, 32], ids=["fp64", "fp32"])
 def test_fft_pipeline_is_bitwise(mhh, precision):
     """The persistent, prefetching FFT kernels give the same fields bit for
-    bit as one tile per block (fixed lengths 64, 48, 128, 96; partial last
-    tiles)."""
+    bit as one tile per block (fixed lengths 64, 48, 128, 96, and 512 with
+    the warp-synchronous schedule; partial last tiles)."""
     for case in (cases.drycbl(64, 48, 20, 6400., 4800., 2000., seed=65, noise_z=600.),
-                 cases.drycbl(128, 96, 13, 12800., 9600., 1300., seed=66, noise_z=600.)):
+                 cases.drycbl(128, 96, 13, 12800., 9600., 1300., seed=66, noise_z=600.),
+                 cases.drycbl(512, 512, 6, 25600., 25600., 600., seed=68, noise_z=400.)):
         out = []
         for pipe, pairs in ((0, 4), (1, 4), (1, 8)):
             mhh.set_option("fft_pipeline", pipe)
