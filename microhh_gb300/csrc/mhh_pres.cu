@@ -460,7 +460,16 @@ namespace mhh
     // complex elements at stride ss.  On return (after __syncwarp) the
     // natural-order result of sequence q is at reinterpret_cast<T2*>(rin +
     // 2q*ns).
-    template<typename TF, bool INV>
+    // Position of X[k] in the result of fft512_warp: natural order, or with
+    // SWAP the two low octal digits exchanged (pass 3 then stores lane-
+    // consecutive elements; the column stores read pairs of adjacent k, which
+    // this order keeps in different banks).
+    template<bool SWAP> __device__ __forceinline__ int w512_res(int k)
+    {
+        return SWAP ? (((k & 7) << 3) | ((k >> 3) & 7) | (k & ~63)) : k;
+    }
+
+    template<typename TF, bool INV, bool SWAP>
     __device__ __forceinline__ void fft512_warp(TF* rin, int ns, typename C2<TF>::T* work, int ss,
                                                 const typename C2<TF>::T* __restrict__ tw, int P)
     {
@@ -501,8 +510,8 @@ namespace mhh
             for (int k1=0; k1<8; ++k1) z[w512_pos(r, k1, t)] = a[k1];
         }
         __syncwarp();
-        // Pass 3: radix 8 over t; X[r + 8 k1 + 64 k2] in natural order over
-        // the warp's real input (read only by this warp, in pass 1).
+        // Pass 3: radix 8 over t; X[r + 8 k1 + 64 k2] at w512_res over the
+        // warp's real input (read only by this warp, in pass 1).
         T2* out = reinterpret_cast<T2*>(rin + (2*q)*ns);
         #pragma unroll
         for (int h=0; h<2; ++h)
@@ -513,7 +522,7 @@ namespace mhh
             for (int t=0; t<8; ++t) a[t] = z[w512_pos(r, k1, t)];
             dft8<TF, T2>(a);
             #pragma unroll
-            for (int k2=0; k2<8; ++k2) out[r + 8*k1 + 64*k2] = a[k2];
+            for (int k2=0; k2<8; ++k2) out[SWAP ? pp + 64*k2 : r + 8*k1 + 64*k2] = a[k2];
         }
         __syncwarp();
     }
@@ -658,7 +667,7 @@ namespace mhh
         T2* other;
         if constexpr (WARP)
         {
-            fft512_warp<TF, INV>(r1, ns, buf0, n, tws, P);
+            fft512_warp<TF, INV, false>(r1, ns, buf0, n, tws, P);
             __syncthreads();
             res = nullptr; other = buf0;
         }
@@ -866,19 +875,19 @@ namespace mhh
         return yseq ? TF(-0.5)*(a.x - b.x) : TF(0.5)*(a.y - b.y);
     }
 
-    // The same from a natural-order complex result rq of the pair (yseq: the
+    // The same from the result rq of the pair from fft512_warp (yseq: the
     // pair's second real sequence).
-    template<typename TF, bool INV, int N>
+    template<typename TF, bool INV, int N, bool SWAP>
     __device__ __forceinline__ TF fft_real_nat(const typename C2<TF>::T* __restrict__ rq, int yseq, int k, TF scale)
     {
         using T2 = typename C2<TF>::T;
         if (INV)
         {
-            const T2 a = rq[k];
+            const T2 a = rq[w512_res<SWAP>(k)];
             return yseq ? -a.y*scale : a.x*scale;
         }
         const int kk = k <= N/2 ? k : N - k;
-        const T2 a = rq[kk], b = rq[kk == 0 ? 0 : N - kk];
+        const T2 a = rq[w512_res<SWAP>(kk)], b = rq[w512_res<SWAP>(kk == 0 ? 0 : N - kk)];
         if (k <= N/2) return yseq ? TF(0.5)*(a.y + b.y) : TF(0.5)*(a.x + b.x);
         return yseq ? TF(-0.5)*(a.x - b.x) : TF(0.5)*(a.y - b.y);
     }
@@ -962,7 +971,7 @@ namespace mhh
             TF* inr = reinterpret_cast<TF*>(in);
             if constexpr (WARP)
             {
-                fft512_warp<TF, INV>(inr, NS, work, SS, tws, P);
+                fft512_warp<TF, INV, !ROWS>(inr, NS, work, SS, tws, P);
                 __syncthreads();
             }
             else
@@ -979,7 +988,7 @@ namespace mhh
             auto out_at = [&](int ls, int k) -> TF
             {
                 if constexpr (WARP)
-                    return fft_real_nat<TF, INV, N>(reinterpret_cast<const T2*>(inr + (ls & ~1)*NS), ls & 1, k, scale);
+                    return fft_real_nat<TF, INV, N, !ROWS>(reinterpret_cast<const T2*>(inr + (ls & ~1)*NS), ls & 1, k, scale);
                 else
                     return fft_real_out<TF, INV, N, SS, ROWS>(res, ls, k, scale);
             };
