@@ -384,17 +384,21 @@ namespace mhh_host
     {
         Field3d<TF>* f = by_name(name);
         const long long n = grid.get_grid_data().ncells;
-        cuda_check(cudaMemcpyAsync(data, f->fld_g, sizeof(TF)*n, cudaMemcpyDeviceToHost, s), "get field");
         const double off = offset(name);
-        if (off != 0.)
+        if (off == 0.)
         {
-            // Native values are physical: the offset is added on the host,
-            // rounded to the field precision.
-            cuda_check(cudaStreamSynchronize(s), "get field");
-            TF* out = static_cast<TF*>(data);
-            const TF o = TF(off);
-            for (long long q=0; q<n; ++q) out[q] += o;
+            cuda_check(cudaMemcpyAsync(data, f->fld_g, sizeof(TF)*n, cudaMemcpyDeviceToHost, s), "get field");
+            return;
         }
+        // Native values are physical: the offset is added (rounded to the
+        // field precision) on the device, in a stream-ordered scratch copy,
+        // so that the copy to the host stays one DMA transfer.
+        void* tmp = nullptr;
+        cuda_check(cudaMallocAsync(&tmp, sizeof(TF)*n, s), "get field");
+        cuda_check(cudaMemcpyAsync(tmp, f->fld_g, sizeof(TF)*n, cudaMemcpyDeviceToDevice, s), "get field");
+        check(mhh_field_shift(grid.ctx(), tmp, off, s), "field_shift");
+        cuda_check(cudaMemcpyAsync(data, tmp, sizeof(TF)*n, cudaMemcpyDeviceToHost, s), "get field");
+        cuda_check(cudaFreeAsync(tmp, s), "get field");
     }
 
     // ---------------------------------------------------------------------

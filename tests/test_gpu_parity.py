@@ -468,6 +468,30 @@ def test_profile_statistics(mhh, precision):
         assert np.allclose(var, ref_var, rtol=1e-9, atol=1e-14 * max(ref_var.max(), 1e-30)), name
 
 
+def test_native_fields_carry_the_scalar_offset(mhh):
+    """Native-precision copies of the FP32 form: get_native returns the stored
+    anomaly plus thref0 rounded in float (added on the device), set_native
+    stores the value minus thref0 rounded in float; the velocities copy as
+    they are."""
+    case = cases.drycbl(32, 32, 32, 3200., 3200., 3200., seed=71, noise_z=800.)
+    m = mhh.Model(case, precision=mhh.FP32)
+    m.run_steps(2)
+    off = m.scalar_offset()
+    assert off == 300.
+    for name, o in (("u", 0.), ("th", off)):
+        stored = (m.get(name) - o).astype(np.float32)    # exact: float values plus 300 in double
+        expect = stored + np.float32(o)
+        out = np.empty(m.shape, dtype=np.float32)
+        m.get_native(name, out.ctypes.data)
+        m.synchronize()
+        assert np.array_equal(out, expect), name
+        back = (expect * np.float32(1.001)).astype(np.float32)
+        m.set_native(name, back.ctypes.data)
+        m.synchronize()
+        assert np.array_equal((m.get(name) - o).astype(np.float32), back - np.float32(o)), name
+    m.close()
+
+
 @pytest.mark.parametrize("precision", [64, 32], ids=["fp64", "fp32"])
 def test_restart_is_bitwise(mhh, precision, tmp_path):
     """Save after two steps, load into a fresh model and run two more: the
