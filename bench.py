@@ -272,13 +272,15 @@ def run_ours(args, world, rank, local):
     host_out = {nm: torch.empty_like(host_in[nm]).pin_memory() for nm in names}
     m2 = mhh.Model(case, precision=mhh.FP32)
     m2.run_steps(1, fused=True)
-    # Untimed pass over the same page-locked buffers: the first device
-    # access to freshly pinned pages costs about 15x a later one (one-time
-    # mapping), which a job that reuses its staging buffers pays once.
-    for nm in names:
-        m2.set_native(nm, host_in[nm].data_ptr())
-        m2.get_native(nm, host_out[nm].data_ptr())
-    m2.synchronize()
+    # Untimed passes over the same page-locked buffers: on the GB300 machine the
+    # first two device passes over pinned pages that the CPU has written cost
+    # about 10x a later one (13-20 ms against 1.3-1.5 ms per 277 MB field),
+    # a one-time cost that a job reusing its staging buffers pays once.
+    for _ in range(2):
+        for nm in names:
+            m2.set_native(nm, host_in[nm].data_ptr())
+            m2.get_native(nm, host_out[nm].data_ptr())
+        m2.synchronize()
     barrier(world)
     t0 = time.perf_counter()
     for nm in names:
