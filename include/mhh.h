@@ -139,13 +139,18 @@ int mhh_ctx_estimate_bytes(const mhh_grid_desc* desc, int precision, size_t* byt
    "tdma_kernel" 0 = the Thomas recurrence in the reference's operation order,
    1 = the rescaled recurrence (two FP64 FMAs per cell) with one column per
    thread, 2 = the same with the four columns of one eigenvalue per thread,
-   -1 = automatic (0 for FP64 contexts, 1 for FP32 contexts; the default). */
+   3 = the rescaled recurrence in float for the column groups whose forward
+   sweep damps (max |g| <= 0.999) and in FP64 for the others (FP32 contexts;
+   1 in FP64 contexts), -1 = automatic (0 for FP64 contexts, 3 for FP32
+   contexts; the default). */
 int mhh_set_option(const char* name, int value);
 /* "fft_pipeline": 1 (the default) runs the fixed-length FFTs as persistent
    blocks that load their next tile while transforming the current one; 0
    runs one tile per block.  Both give identical results.
    "fft_column_pairs": complex sequence pairs per tile of the y FFT, 8 (the
-   default: 16 adjacent columns, 512 threads per block, float fields) or 4.  "pres_fuse": 1 (the default) computes the Poisson
+   default: 16 adjacent columns, 512 threads per block, float fields; 256
+   threads for the 512-point warp-synchronous schedule, one warp per pair)
+   or 4.  "pres_fuse": 1 (the default) computes the Poisson
    right-hand side inside the forward x FFT and stores the inverse x FFT into
    the ghost layout of p; 0 runs them as separate kernels. */
 /* "tendency_kchunk" / "viscosity_kchunk": levels per block of the marching
