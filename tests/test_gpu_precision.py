@@ -1,6 +1,6 @@
 """The precision form against the FP64 oracle over a 10-minute average.
 
-Config 0 (the dry CBL at 64x64x64, 6400x6400x4000 m, dt = 2 s) runs 600 steps
+The dry CBL at 64x64x64 (6400x6400x4000 m, dt = 2 s) runs 600 steps
 in the oracle, the plain FP64 path and the FP32 form; the horizontal mean and
 variance profiles of u, v, w and theta are averaged over the last 300 steps
 (10 minutes) and compared level by level with the oracle's, normalised as in
@@ -10,7 +10,7 @@ theta's mean by its range, variances by their maximum).
 Bounds:
 - FP64: round-off only.  The fields end 1.6e-11 (relative L2) from the
   oracle's and the averaged profiles 3e-13; held to 1e-9 and 1e-10.
-- FP32 form: the benchmark spec's 0.5% for every averaged profile (measured
+- FP32 form: 0.5% for every averaged profile (measured
   2.4e-6 on a GB300); the fields themselves are held to 1e-2 relative L2
   (measured 1.4e-4 for u).
 """
