@@ -126,7 +126,7 @@ def test_against_oracle_fp64(mhh, oracle_lib, name, make):
             assert max_err(a, b) <= 10 * tol, (name, n, nsteps, max_err(a, b))
 
 
-def test_config0_drycbl_64cubed_fp64(mhh, oracle_lib):
+def test_drycbl_64cubed_fp64_1_and_100_steps(mhh, oracle_lib):
     """The dry CBL configuration exactly (64x64x64, 6400x6400x4000 m,
     Advec_2i5, Smagorinsky, Monin-Obukhov surface, dt = 2 s): one RK3 step at
     the FP64 tolerance, then 100 steps at TOL_100.
@@ -152,7 +152,7 @@ def test_config0_drycbl_64cubed_fp64(mhh, oracle_lib):
     m.close(); o.close()
 
 
-def test_config1_channel_256x192x128_fp64(mhh, oracle_lib):
+def test_channel_256x192x128_fp64(mhh, oracle_lib):
     """The channel DNS configuration exactly (256x192x128, tanh-stretched
     wall-normal levels, Advec_2, Diff_2, dpdx forcing, adaptive time step):
     one RK3 step at the FP64 tolerance."""
