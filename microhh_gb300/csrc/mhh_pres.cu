@@ -388,42 +388,43 @@ namespace mhh
     // The float transform with the fused right-hand side keeps five blocks
     // per SM (at most 51 registers): its batched loads need the residency to
     // cover the latency of HBM.
-    // ---- warp-synchronous 512-point schedule --------------------------------
-    // For n = 512 = 8 x 64 one warp transforms one complex sequence with a
-    // single block-wide dependency (its input tile): a decimation-in-
-    // frequency radix-8 stage splits the sequence into eight 64-point
+    // ---- warp-synchronous schedule for n = 64 R (R = 2, 4, 8) --------------
+    // For n = 128, 256 and 512 one warp transforms one complex sequence with
+    // a single block-wide dependency (its input tile): a decimation-in-
+    // frequency radix-R stage splits the sequence into R 64-point
     // sub-sequences,
-    //   s_r[i] = w512^(i r) DFT8_q(z[i + 64 q])[r],  X[8K + r] = DFT64(s_r)[K],
+    //   s_r[i] = wn^(i r) DFT_R,q(z[i + 64 q])[r],  X[R K + r] = DFT64(s_r)[K],
     // and each 64-point transform runs as 8 x 8 within the warp:
     //   A[t][k1] = w64^(t k1) DFT8_m(s_r[t + 8 m])[k1],
     //   X_r[k1 + 8 k2] = DFT8_t(A[t][k1])[k2].
-    // The exchanges between the three radix-8 passes go through the warp's
-    // own shared-memory region with __syncwarp (an 8 x 8 transpose among
-    // eight lanes is 16 shared accesses per lane; with __shfl_xor_sync it is
-    // 24 shuffles and 48 selects), so a tile needs block barriers only after
-    // its load and before its store, against one per stage in the Stockham
-    // schedule.  The last pass writes the natural order over the warp's own
-    // real input, which no other warp reads.
+    // The exchanges between the three passes go through the warp's own
+    // shared-memory region with __syncwarp (an 8 x 8 transpose among eight
+    // lanes is 16 shared accesses per lane; with __shfl_xor_sync it is 24
+    // shuffles and 48 selects), so a tile needs block barriers only after its
+    // load and before its store, against one per stage in the Stockham
+    // schedule.  The last pass writes its result over the warp's own real
+    // input, which no other warp reads.
     //
     // Positions within a sub-sequence block: rows of eight complex elements,
     // row index XOR (r & 1) and column index XOR row, so that eight lanes
-    // reading a row or a column, and the four sub-blocks a warp touches at
-    // once, spread over all banks.
-    __device__ __forceinline__ int w512_pos(int r, int row, int col)
+    // reading a row or a column, and the sub-blocks a warp touches at once,
+    // spread over all banks.
+    __device__ __forceinline__ int warp_pos(int r, int row, int col)
     {
         return r*64 + ((row ^ (r & 1)) << 3) + (col ^ row);
     }
 
-    // Twiddles of the schedule, n entries in shared memory: w512^(i r) at
-    // (r-1)*64 + i for r = 1..7, i = 0..63, then w64^(t k1) = w512^(8 t k1)
-    // at 448 + k1*8 + t.
-    template<typename TF>
-    __device__ __forceinline__ void w512_twiddles(typename C2<TF>::T* tw, const TF* __restrict__ twt)
+    // Twiddles of the schedule, n = 64 R entries in shared memory: wn^(i r)
+    // at (r-1)*64 + i for r = 1..R-1, i = 0..63, then w64^(t k1) = wn^(R t k1)
+    // at (R-1)*64 + k1*8 + t.
+    template<typename TF, int R>
+    __device__ __forceinline__ void warp_twiddles(typename C2<TF>::T* tw, const TF* __restrict__ twt)
     {
         using T2 = typename C2<TF>::T;
-        for (int e = threadIdx.x; e < 512; e += blockDim.x)
+        constexpr int N = 64*R, B = (R - 1)*64;
+        for (int e = threadIdx.x; e < N; e += blockDim.x)
         {
-            const int idx = e < 448 ? ((e & 63)*((e >> 6) + 1)) & 511 : (8*(e & 7)*((e - 448) >> 3)) & 511;
+            const int idx = e < B ? ((e & 63)*((e >> 6) + 1)) % N : (R*(e & 7)*((e - B) >> 3)) % N;
             T2 w; w.x = twt[2*idx]; w.y = twt[2*idx + 1];
             tw[e] = w;
         }
@@ -455,77 +456,90 @@ namespace mhh
         return u;
     }
 
-    // The transform of complex sequence q (warp q; q < P) of a tile whose
-    // 2P real sequences sit at rin + s*ns.  work holds P regions of 512
-    // complex elements at stride ss.  On return (after __syncwarp) the
-    // natural-order result of sequence q is at reinterpret_cast<T2*>(rin +
-    // 2q*ns).
-    // Position of X[k] in the result of fft512_warp: natural order, or with
-    // SWAP the two low octal digits exchanged (pass 3 then stores lane-
-    // consecutive elements; the column stores read pairs of adjacent k, which
-    // this order keeps in different banks).
-    template<bool SWAP> __device__ __forceinline__ int w512_res(int k)
+    // Position of X[k] in the result of fft_warp: natural order, or with
+    // SWAP the sub-sequence index r = k mod R and the next octal digit k1
+    // exchanged (pass 3 then stores lane-consecutive elements; the column
+    // stores read pairs of adjacent k, which this order keeps in different
+    // banks).
+    template<int R, bool SWAP> __device__ __forceinline__ int warp_res(int k)
     {
-        return SWAP ? (((k & 7) << 3) | ((k >> 3) & 7) | (k & ~63)) : k;
+        if (!SWAP) return k;
+        const int r = k % R, k1 = (k / R) & 7, k2 = k / (8*R);
+        return r*8 + k1 + 8*R*k2;
     }
 
-    template<typename TF, bool INV, bool SWAP>
-    __device__ __forceinline__ void fft512_warp(TF* rin, int ns, typename C2<TF>::T* work, int ss,
-                                                const typename C2<TF>::T* __restrict__ tw, int P)
+    // The transform of complex sequence q (warp q; q < P) of a tile whose
+    // 2P real sequences sit at rin + s*ns.  work holds P regions of 64 R
+    // complex elements at stride ss.  On return (after __syncwarp) X[k] of
+    // sequence q is at element warp_res<R, SWAP>(k) of
+    // reinterpret_cast<T2*>(rin + 2q*ns).
+    template<typename TF, bool INV, bool SWAP, int R>
+    __device__ __forceinline__ void fft_warp(TF* rin, int ns, typename C2<TF>::T* work, int ss,
+                                             const typename C2<TF>::T* __restrict__ tw, int P)
     {
         using T2 = typename C2<TF>::T;
+        constexpr int N = 64*R, NPAIR = 8*R;
         const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;
         if (q >= P) return;
         const TF* hx = rin + (2*q)*ns;
         const TF* hy = hx + ns;
         T2* z = work + q*ss;
-        // Pass 1: radix 8 over stride 64, twiddles w512^(i r).
+        // Pass 1: radix R over stride 64, twiddles wn^(i r).
         #pragma unroll
         for (int h=0; h<2; ++h)
         {
             const int i = lane + 32*h;
-            T2 u[8];
+            T2 u[R];
             #pragma unroll
-            for (int b=0; b<8; ++b) u[b] = pair_in<TF, INV, 512>(hx, hy, i + 64*b);
-            dft8<TF, T2>(u);
+            for (int b=0; b<R; ++b) u[b] = pair_in<TF, INV, N>(hx, hy, i + 64*b);
+            radix_bfly<TF, N, R, 64>(u, tw);
             #pragma unroll
-            for (int r=1; r<8; ++r) u[r] = cmul(u[r], tw[(r - 1)*64 + i]);
+            for (int r=1; r<R; ++r) u[r] = cmul(u[r], tw[(r - 1)*64 + i]);
             #pragma unroll
-            for (int r=0; r<8; ++r) z[w512_pos(r, i >> 3, i & 7)] = u[r];
+            for (int r=0; r<R; ++r) z[warp_pos(r, i >> 3, i & 7)] = u[r];
         }
         __syncwarp();
         // Pass 2: radix 8 over m within each sub-sequence, twiddles w64^(t k1),
         // in place (a lane's writes are the elements it read).
         #pragma unroll
-        for (int h=0; h<2; ++h)
+        for (int h=0; h<(NPAIR + 31)/32; ++h)
         {
             const int pp = lane + 32*h, r = pp >> 3, t = pp & 7;
-            T2 a[8];
-            #pragma unroll
-            for (int m=0; m<8; ++m) a[m] = z[w512_pos(r, m, t)];
-            dft8<TF, T2>(a);
-            #pragma unroll
-            for (int k1=1; k1<8; ++k1) a[k1] = cmul(a[k1], tw[448 + k1*8 + t]);
-            #pragma unroll
-            for (int k1=0; k1<8; ++k1) z[w512_pos(r, k1, t)] = a[k1];
+            if (pp < NPAIR)
+            {
+                T2 a[8];
+                #pragma unroll
+                for (int m=0; m<8; ++m) a[m] = z[warp_pos(r, m, t)];
+                dft8<TF, T2>(a);
+                #pragma unroll
+                for (int k1=1; k1<8; ++k1) a[k1] = cmul(a[k1], tw[(R - 1)*64 + k1*8 + t]);
+                #pragma unroll
+                for (int k1=0; k1<8; ++k1) z[warp_pos(r, k1, t)] = a[k1];
+            }
         }
         __syncwarp();
-        // Pass 3: radix 8 over t; X[r + 8 k1 + 64 k2] at w512_res over the
+        // Pass 3: radix 8 over t; X[r + R k1 + 8 R k2] at warp_res over the
         // warp's real input (read only by this warp, in pass 1).
         T2* out = reinterpret_cast<T2*>(rin + (2*q)*ns);
         #pragma unroll
-        for (int h=0; h<2; ++h)
+        for (int h=0; h<(NPAIR + 31)/32; ++h)
         {
             const int pp = lane + 32*h, r = pp >> 3, k1 = pp & 7;
-            T2 a[8];
-            #pragma unroll
-            for (int t=0; t<8; ++t) a[t] = z[w512_pos(r, k1, t)];
-            dft8<TF, T2>(a);
-            #pragma unroll
-            for (int k2=0; k2<8; ++k2) out[SWAP ? pp + 64*k2 : r + 8*k1 + 64*k2] = a[k2];
+            if (pp < NPAIR)
+            {
+                T2 a[8];
+                #pragma unroll
+                for (int t=0; t<8; ++t) a[t] = z[warp_pos(r, k1, t)];
+                dft8<TF, T2>(a);
+                #pragma unroll
+                for (int k2=0; k2<8; ++k2) out[SWAP ? pp + 8*R*k2 : r + R*k1 + 8*R*k2] = a[k2];
+            }
         }
         __syncwarp();
     }
+
+    // Lengths that run the warp-synchronous schedule.
+    __host__ __device__ constexpr bool warp_len(int n) { return n == 128 || n == 256 || n == 512; }
 
     template<typename TF> struct FftP { FftPlan pl; TF* data; SeqLayout L; int Prt; TF scale; FftFuse<TF> fz; };
     template<typename TF, int FUSE> struct FftOcc { static constexpr int v = (FUSE == 1 && sizeof(TF) == 4) ? 5 : 1; };
@@ -554,8 +568,8 @@ namespace mhh
         const long long s0 = (long long)vb.x*2*P;
         const int nloc = (int)min((long long)2*P, L.nseq - s0);
 
-        constexpr bool WARP = NFIX == 512;
-        if (WARP) w512_twiddles<TF>(tws, twtab<TF>(pl));
+        constexpr bool WARP = warp_len(NFIX);
+        if constexpr (WARP) warp_twiddles<TF, NFIX/64>(tws, twtab<TF>(pl));
         else if (NFIX)
         {
             const TF* tt = twtab<TF>(pl);
@@ -661,13 +675,14 @@ namespace mhh
         asm volatile("cp.async.wait_group 0;\n" ::: "memory");
         __syncthreads();
 
-        // 2-3. With n = 512 the warp-synchronous schedule, whose result is
-        //      the natural order over each sequence pair's real input.
+        // 2-3. With n = 128, 256 or 512 the warp-synchronous schedule, whose
+        //      result is the natural order over each sequence pair's real
+        //      input.
         T2* res;
         T2* other;
         if constexpr (WARP)
         {
-            fft512_warp<TF, INV, false>(r1, ns, buf0, n, tws, P);
+            fft_warp<TF, INV, false, NFIX/64>(r1, ns, buf0, n, tws, P);
             __syncthreads();
             res = nullptr; other = buf0;
         }
@@ -875,7 +890,7 @@ namespace mhh
         return yseq ? TF(-0.5)*(a.x - b.x) : TF(0.5)*(a.y - b.y);
     }
 
-    // The same from the result rq of the pair from fft512_warp (yseq: the
+    // The same from the result rq of the pair from fft_warp (yseq: the
     // pair's second real sequence).
     template<typename TF, bool INV, int N, bool SWAP>
     __device__ __forceinline__ TF fft_real_nat(const typename C2<TF>::T* __restrict__ rq, int yseq, int k, TF scale)
@@ -883,11 +898,11 @@ namespace mhh
         using T2 = typename C2<TF>::T;
         if (INV)
         {
-            const T2 a = rq[w512_res<SWAP>(k)];
+            const T2 a = rq[warp_res<N/64, SWAP>(k)];
             return yseq ? -a.y*scale : a.x*scale;
         }
         const int kk = k <= N/2 ? k : N - k;
-        const T2 a = rq[w512_res<SWAP>(kk)], b = rq[w512_res<SWAP>(kk == 0 ? 0 : N - kk)];
+        const T2 a = rq[warp_res<N/64, SWAP>(kk)], b = rq[warp_res<N/64, SWAP>(kk == 0 ? 0 : N - kk)];
         if (k <= N/2) return yseq ? TF(0.5)*(a.y + b.y) : TF(0.5)*(a.x + b.x);
         return yseq ? TF(-0.5)*(a.x - b.x) : TF(0.5)*(a.y - b.y);
     }
@@ -911,8 +926,8 @@ namespace mhh
         T2* bufs = reinterpret_cast<T2*>(smem_raw);
         T2* work = bufs + BUF;
         T2* tws = bufs + 3*BUF;
-        constexpr bool WARP = N == 512;
-        if (WARP) w512_twiddles<TF>(tws, twt);
+        constexpr bool WARP = warp_len(N);
+        if constexpr (WARP) warp_twiddles<TF, N/64>(tws, twt);
         else
             for (int e = threadIdx.x; e < N; e += blockDim.x)
             { T2 w; w.x = twt[2*e]; w.y = twt[2*e+1]; tws[e] = w; }
@@ -971,7 +986,7 @@ namespace mhh
             TF* inr = reinterpret_cast<TF*>(in);
             if constexpr (WARP)
             {
-                fft512_warp<TF, INV, !ROWS>(inr, NS, work, SS, tws, P);
+                fft_warp<TF, INV, !ROWS, N/64>(inr, NS, work, SS, tws, P);
                 __syncthreads();
             }
             else
@@ -1041,8 +1056,8 @@ namespace mhh
     {
         using T2 = typename C2<TF>::T;
         // 8 pairs (16 columns, 64-byte rows of a tile) run with 512 threads;
-        // the warp-synchronous 512-point schedule with one warp per pair.
-        constexpr int NT = N == 512 ? 32*P : (P == 8 ? 512 : 256);
+        // the warp-synchronous schedule with one warp per pair.
+        constexpr int NT = warp_len(N) ? 32*P : (P == 8 ? 512 : 256);
         const size_t smem = sizeof(T2)*((size_t)3*fftp_buf(N, P, ROWS) + N);
         const long long ntiles = (L.nseq + 2*P - 1) / (2*P);
         // Attribute and residency are set once per kernel, outside any stream

@@ -382,13 +382,14 @@ def test_fft_roundtrip_and_dft(mhh, itot, jtot):
 
 @pytest.mark.parametrize("pipe", [1, 0], ids=["prefetching", "tile_per_block"])
 @pytest.mark.parametrize("precision", [64, 32], ids=["fp64", "fp32"])
-def test_fft512_warp_schedule(mhh, precision, pipe):
-    """The warp-synchronous 512-point schedule (rows and columns, both FFT
-    kernels) against numpy's DFT in halfcomplex order, and the inverse pair
-    returning itot*jtot times the input."""
+@pytest.mark.parametrize("n", [128, 256, 512])
+def test_fft_warp_schedule(mhh, n, precision, pipe):
+    """The warp-synchronous schedule (n = 64 R, R = 2, 4, 8; rows and columns,
+    both FFT kernels) against numpy's DFT in halfcomplex order, and the
+    inverse pair returning itot*jtot times the input."""
     import ctypes
     import torch
-    itot = jtot = 512
+    itot = jtot = n
     ktot = 3
     desc = mhh.GridDesc(itot, jtot, ktot, 1, 1, 1, 1.0, 1.0, 1.0)
     phys = mhh.Physics(visc=1e-5, svisc=1e-5, cs=0.23, tpr=1/3., dnmax=0.4, swmason=1, cflmax=1.,
@@ -401,7 +402,7 @@ def test_fft512_warp_schedule(mhh, precision, pipe):
     rng = np.random.default_rng(5)
     x = rng.standard_normal((ktot, jtot, itot))
     dt = torch.float64 if precision == 64 else torch.float32
-    # Float: the transforms' round-off, a few eps times log2(512).
+    # Float: the transforms' round-off, a few eps times log2(n).
     tol = 1e-12 if precision == 64 else 3e-6
     mhh.set_option("fft_pipeline", pipe)
     try:
