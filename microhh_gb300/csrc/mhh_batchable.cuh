@@ -9,9 +9,9 @@
 // owns the blocks [start[m], start[m+1]) and decomposes its local block
 // index into its own (gx, gy, gz) grid.  A body therefore runs with the same
 // parameters and block positions in both, and gives the same results bit for
-// bit.  Both entry points take their parameters in the kernel parameter
-// space (up to 32 KB, __grid_constant__); k_many copies its block's struct
-// to shared memory first.
+// bit.  k_one takes P by value and runs the body on a local copy; k_many
+// takes the contexts' structs as up to 32 KB of __grid_constant__ kernel
+// parameters and copies its block's struct to shared memory first.
 //
 // launch_body() is the one launch site.  Normally it launches k_one.  While
 // a batch plan records a context's substep (BatchRecorder), it appends the
