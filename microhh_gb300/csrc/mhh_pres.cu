@@ -1,14 +1,16 @@
 // mhh_pres.cu -- the Pres_2 Poisson solve on the GPU without cuFFT:
 // divergence of the predicted velocity, hand-written real FFTs along x and y
 // (halfcomplex layout, so the spectral solve is the reference's), a Thomas
-// solve per spectral column in double, inverse FFTs and the scatter back into
-// the ghost-cell layout.
+// solve per spectral column (in double; in the float form in float where the
+// column's forward sweep damps), inverse FFTs and the scatter back into the
+// ghost-cell layout.
 //
 // FFT: two real sequences x, y of length n are transformed together as
 // z = x + i y with a mixed-radix (4, 2, 3, 5, 7) Stockham autosort FFT in
-// shared memory (ping-pong buffers, one barrier per stage), then separated by
-// Hermitian symmetry into FFTW's halfcomplex order r_0 .. r_{n/2},
-// i_{(n+1)/2-1} .. i_1 (the convention of src/fft.cxx:145-206).
+// shared memory (ping-pong buffers, one barrier per stage), or for n = 128,
+// 256 and 512 with a warp-synchronous schedule (one warp per sequence), then
+// separated by Hermitian symmetry into FFTW's halfcomplex order r_0 ..
+// r_{n/2}, i_{(n+1)/2-1} .. i_1 (the convention of src/fft.cxx:145-206).
 #include <cmath>
 #include <cstring>
 #include <vector>
