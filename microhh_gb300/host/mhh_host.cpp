@@ -395,9 +395,17 @@ namespace mhh_host
         // so that the copy to the host stays one DMA transfer.
         void* tmp = nullptr;
         cuda_check(cudaMallocAsync(&tmp, sizeof(TF)*n, s), "get field");
-        cuda_check(cudaMemcpyAsync(tmp, f->fld_g, sizeof(TF)*n, cudaMemcpyDeviceToDevice, s), "get field");
-        check(mhh_field_shift(grid.ctx(), tmp, off, s), "field_shift");
-        cuda_check(cudaMemcpyAsync(data, tmp, sizeof(TF)*n, cudaMemcpyDeviceToHost, s), "get field");
+        try
+        {
+            cuda_check(cudaMemcpyAsync(tmp, f->fld_g, sizeof(TF)*n, cudaMemcpyDeviceToDevice, s), "get field");
+            check(mhh_field_shift(grid.ctx(), tmp, off, s), "field_shift");
+            cuda_check(cudaMemcpyAsync(data, tmp, sizeof(TF)*n, cudaMemcpyDeviceToHost, s), "get field");
+        }
+        catch (...)
+        {
+            cudaFreeAsync(tmp, s);
+            throw;
+        }
         cuda_check(cudaFreeAsync(tmp, s), "get field");
     }
 
